@@ -1,0 +1,110 @@
+/*
+ * lprec_gb300 -- C ABI of the GB300 log-polar Radon transform library.
+ *
+ * Drop-in for the native operator class of lprec (src/cuda/lpRgpu.cuh:6-81,
+ * exposed to Python through SWIG in src/cuda/lpRgpu.i:10-41) and for the
+ * parameter precompute that lprec runs in Python (src/lprec/initsgl.py,
+ * initsfwd.py, initsadj.py).  Plain pointers and sizes only; every entry
+ * point returns LP_OK or an error code and never resets the device (the
+ * reference's callErr, src/cuda/callerr.cu:3-8, calls cudaDeviceReset()).
+ * The message of the last error on the calling thread is lp_last_error().
+ *
+ * Device pointers are float32, C-contiguous:
+ *   image    f[S0][N0][N0]
+ *   sinogram R[S0][Nproj][N0]
+ * with S0 <= Nslices (the batch capacity given at precompute time).
+ */
+#ifndef LPREC_GB300_H
+#define LPREC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LP_OK 0
+#define LP_ERR_ARG 1         /* bad argument or malformed parameter arrays */
+#define LP_ERR_CUDA 2        /* a CUDA runtime call or kernel launch failed */
+#define LP_ERR_OOM 3         /* device or host allocation failed */
+#define LP_ERR_STATE 4       /* e.g. lp_fwd before lp_init_fwd */
+#define LP_ERR_UNSUPPORTED 5 /* geometry outside what the kernels handle */
+
+#define LP_PRECISION_REFERENCE 0 /* tables evaluated with the reference's float32 steps */
+#define LP_PRECISION_FP64 1      /* same index sets, every value in float64, rounded once */
+
+typedef struct lp_handle lp_handle;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* lp_last_error(void);
+
+/* Library version, e.g. 100 for 0.1.0. */
+int lp_version(void);
+
+/*
+ * Sizes of the five packed parameter arrays for a geometry:
+ *   sizes[0] glpars (float32)      initsgl.py:55-56
+ *   sizes[1] fwdparsi (int32)      initsfwd.py:96-126 (savePfwdpars)
+ *   sizes[2] fwdparamsf (float32)
+ *   sizes[3] adjparsi (int32)      initsadj.py:205-244 (savePadjpars)
+ *   sizes[4] adjparamsf (float32)
+ * filter is one of "none", "ramp", "shepp-logan", "cosine", "cosine2",
+ * "hamming", "hann", "parzen" (initsadj.py:107,146-173).  Host only.
+ */
+int lp_precompute_sizes(int N0, int Nproj, int Nslices, double cor, int cubic, const char* filter,
+                        int64_t sizes[5]);
+
+/*
+ * Compute the packed parameter arrays (replaces create_gl/create_fwd/
+ * create_adj, lpTransform.py:19-31).  fwdparsi/fwdparamsf may be NULL when
+ * with_fwd is 0.  precision: LP_PRECISION_REFERENCE or LP_PRECISION_FP64.
+ * nthreads: host threads (0 = all).  Host only.
+ */
+int lp_precompute(int N0, int Nproj, int Nslices, double cor, int cubic, const char* filter, int precision,
+                  int with_fwd, int nthreads, float* glpars, int32_t* fwdparsi, float* fwdparamsf,
+                  int32_t* adjparsi, float* adjparamsf);
+
+/*
+ * Create a handle on `device` from glpars (replaces lpRgpu::lpRgpu(size_t
+ * params, int gpu), src/cuda/lpRgpu.cu:7-39).  n = number of floats.
+ */
+int lp_create(const float* glpars, int64_t n, int device, lp_handle** out);
+
+/* Upload forward tables (replaces lpRgpu::initFwd, src/cuda/lpRgpu.cu:61-85). */
+int lp_init_fwd(lp_handle* h, const int32_t* parsi, int64_t ni, const float* parsf, int64_t nf);
+
+/* Upload adjoint tables and filter (replaces lpRgpu::initAdj, src/cuda/lpRgpu.cu:98-133). */
+int lp_init_adj(lp_handle* h, const int32_t* parsi, int64_t ni, const float* parsf, int64_t nf);
+
+/* Free everything the handle owns (replaces lpRgpu::~lpRgpu, src/cuda/lpRgpu.cu:41-58). */
+int lp_destroy(lp_handle* h);
+
+/*
+ * Forward transform R = Radon(f) on device pointers, enqueued on `stream`
+ * (a cudaStream_t; NULL = legacy default stream).  Replaces
+ * lpRgpu::execFwdManyPtr(size_t Rptr, size_t fptr, int Nslices0, int gpu),
+ * src/cuda/lpRgpu.cu:184-193.
+ */
+int lp_fwd(lp_handle* h, float* R, const float* f, int S0, void* stream);
+
+/*
+ * Adjoint / filtered back-projection f = R*(filter(R)) on device pointers.
+ * Replaces lpRgpu::execAdjManyPtr(size_t fptr, size_t Rptr, int Nslices0,
+ * int gpu), src/cuda/lpRgpu.cu:196-207.  R is read only.
+ */
+int lp_adj(lp_handle* h, float* f, const float* R, int S0, void* stream);
+
+/*
+ * Geometry of a handle: out[0..9] = N, N0, Ntheta, Nrho, Nproj (internal),
+ * Nproj (caller), Nslices, cor, osangles, cubic.
+ */
+int lp_get_geometry(const lp_handle* h, int32_t out[10]);
+
+/* Bytes of device memory the handle holds. */
+int lp_device_bytes(const lp_handle* h, int64_t* bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LPREC_GB300_H */

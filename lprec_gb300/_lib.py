@@ -1,0 +1,151 @@
+"""ctypes binding of liblprec_gb300.so (the C ABI declared in include/lprec_gb300.h).
+
+The library is built in-tree by ``lprec_gb300.build``; importing this module
+loads it and raises if it is missing -- there is no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblprec_gb300.so")
+
+LP_OK = 0
+LP_ERR_ARG = 1
+LP_ERR_CUDA = 2
+LP_ERR_OOM = 3
+LP_ERR_STATE = 4
+LP_ERR_UNSUPPORTED = 5
+PRECISION = {"reference": 0, "fp64": 1}
+
+# every symbol include/lprec_gb300.h declares
+EXPORTS = ("lp_last_error", "lp_version", "lp_precompute_sizes", "lp_precompute", "lp_create", "lp_init_fwd",
+           "lp_init_adj", "lp_destroy", "lp_fwd", "lp_adj", "lp_get_geometry", "lp_device_bytes")
+
+
+class LprecError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("lprec_gb300 error %d: %s" % (code, msg))
+        self.code = code
+
+
+_lib = None
+
+c_int, c_int64, c_double, c_void_p, c_char_p = ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p, ctypes.c_char_p
+P_i32 = ctypes.POINTER(ctypes.c_int32)
+P_f32 = ctypes.POINTER(ctypes.c_float)
+P_i64 = ctypes.POINTER(ctypes.c_int64)
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("liblprec_gb300.so is not built (run `python -m lprec_gb300.build`): %s" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    sig = {
+        "lp_last_error": (c_char_p, []),
+        "lp_version": (c_int, []),
+        "lp_precompute_sizes": (c_int, [c_int, c_int, c_int, c_double, c_int, c_char_p, P_i64]),
+        "lp_precompute": (c_int, [c_int, c_int, c_int, c_double, c_int, c_char_p, c_int, c_int, c_int,
+                                  P_f32, P_i32, P_f32, P_i32, P_f32]),
+        "lp_create": (c_int, [P_f32, c_int64, c_int, ctypes.POINTER(c_void_p)]),
+        "lp_init_fwd": (c_int, [c_void_p, P_i32, c_int64, P_f32, c_int64]),
+        "lp_init_adj": (c_int, [c_void_p, P_i32, c_int64, P_f32, c_int64]),
+        "lp_destroy": (c_int, [c_void_p]),
+        "lp_fwd": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+        "lp_adj": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+        "lp_get_geometry": (c_int, [c_void_p, P_i32]),
+        "lp_device_bytes": (c_int, [c_void_p, P_i64]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(rc):
+    if rc != LP_OK:
+        raise LprecError(rc, lib().lp_last_error().decode(errors="replace"))
+
+
+def _ptr(a, ctype):
+    return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+def precompute(N0, Nproj, Nslices, cor, interp_type, filter_type, precision="reference", with_fwd=True,
+               nthreads=0):
+    """Host precompute; returns (glpars, fwdparsi, fwdparamsf, adjparsi, adjparamsf)."""
+    L = lib()
+    cubic = 1 if interp_type == "cubic" else 0
+    filt = (filter_type or "none").encode()
+    sizes = np.zeros(5, dtype=np.int64)
+    check(L.lp_precompute_sizes(int(N0), int(Nproj), int(Nslices), float(cor), cubic, filt, _ptr(sizes, ctypes.c_int64)))
+    gl = np.empty(sizes[0], np.float32)
+    fi = np.empty(sizes[1] if with_fwd else 1, np.int32)
+    ff = np.empty(sizes[2] if with_fwd else 1, np.float32)
+    ai = np.empty(sizes[3], np.int32)
+    af = np.empty(sizes[4], np.float32)
+    check(L.lp_precompute(int(N0), int(Nproj), int(Nslices), float(cor), cubic, filt, PRECISION[precision],
+                          1 if with_fwd else 0, int(nthreads), _ptr(gl, ctypes.c_float), _ptr(fi, ctypes.c_int32),
+                          _ptr(ff, ctypes.c_float), _ptr(ai, ctypes.c_int32), _ptr(af, ctypes.c_float)))
+    if not with_fwd:
+        fi = ff = None
+    return gl, fi, ff, ai, af
+
+
+class Handle:
+    """Owner of one lp_handle (one geometry on one device)."""
+
+    def __init__(self, glpars, device=0):
+        self._h = None
+        L = lib()
+        gl = np.ascontiguousarray(glpars, dtype=np.float32)
+        h = c_void_p()
+        check(L.lp_create(_ptr(gl, ctypes.c_float), gl.size, int(device), ctypes.byref(h)))
+        self._h = h
+        self.device = int(device)
+        g = np.zeros(10, np.int32)
+        check(L.lp_get_geometry(h, _ptr(g, ctypes.c_int32)))
+        (self.N, self.N0, self.Ntheta, self.Nrho, self.Nproj_int, self.Nproj, self.Nslices, self.cor,
+         self.osangles, self.cubic) = [int(x) for x in g]
+        self.has_fwd = False
+        self.has_adj = False
+
+    def init_fwd(self, parsi, parsf):
+        pi = np.ascontiguousarray(parsi, dtype=np.int32)
+        pf = np.ascontiguousarray(parsf, dtype=np.float32)
+        check(lib().lp_init_fwd(self._h, _ptr(pi, ctypes.c_int32), pi.size, _ptr(pf, ctypes.c_float), pf.size))
+        self.has_fwd = True
+
+    def init_adj(self, parsi, parsf):
+        pi = np.ascontiguousarray(parsi, dtype=np.int32)
+        pf = np.ascontiguousarray(parsf, dtype=np.float32)
+        check(lib().lp_init_adj(self._h, _ptr(pi, ctypes.c_int32), pi.size, _ptr(pf, ctypes.c_float), pf.size))
+        self.has_adj = True
+
+    def fwd(self, R_ptr, f_ptr, S0, stream):
+        check(lib().lp_fwd(self._h, c_void_p(R_ptr), c_void_p(f_ptr), int(S0), c_void_p(stream)))
+
+    def adj(self, f_ptr, R_ptr, S0, stream):
+        check(lib().lp_adj(self._h, c_void_p(f_ptr), c_void_p(R_ptr), int(S0), c_void_p(stream)))
+
+    def device_bytes(self):
+        b = np.zeros(1, np.int64)
+        check(lib().lp_device_bytes(self._h, _ptr(b, ctypes.c_int64)))
+        return int(b[0])
+
+    def close(self):
+        if self._h is not None and _lib is not None:
+            _lib.lp_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,604 @@
+// Host side of the library: the C ABI, the handle, conversion of the packed
+// parameter arrays (src/cuda/params.cu:40-145 layout) into the column-major
+// device tables the kernels read, and the fwd/adj pipelines.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/lprec_gb300.h"
+#include "lp_kernels.cuh"
+
+using namespace lpgb;
+
+// ---------------------------------------------------------------------------
+// errors: status codes plus a thread-local message; the device is never reset
+// ---------------------------------------------------------------------------
+static thread_local std::string g_err;
+
+static int set_err(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+// shared with precompute.cpp
+int lp_internal_set_err(int code, const char* msg) { return set_err(code, "%s", msg); }
+
+#define CUDA_TRY(call)                                                                                   \
+  do {                                                                                                   \
+    cudaError_t e_ = (call);                                                                             \
+    if (e_ != cudaSuccess)                                                                               \
+      return set_err(e_ == cudaErrorMemoryAllocation ? LP_ERR_OOM : LP_ERR_CUDA, "%s: %s (%s:%d)", #call, \
+                     cudaGetErrorString(e_), __FILE__, __LINE__);                                        \
+  } while (0)
+
+namespace {
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  void free_() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+template <typename T>
+static cudaError_t dev_alloc(DevBuf<T>& b, size_t n) {
+  b.free_();
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void**)&b.p, n * sizeof(T));
+  if (e == cudaSuccess) b.n = n;
+  return e;
+}
+
+template <typename T>
+static cudaError_t dev_upload(DevBuf<T>& b, const std::vector<T>& v) {
+  cudaError_t e = dev_alloc(b, v.size());
+  if (e != cudaSuccess) return e;
+  if (v.empty()) return cudaSuccess;
+  return cudaMemcpy(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+static inline float qnan() { return nanf(""); }
+
+}  // namespace
+
+struct FwdDev {
+  DevBuf<float2> c2lp[3];  // [Nth][Nrho]
+  DevBuf<float> thc;       // [Nproj]
+  DevBuf<float> rhoc;      // [Nproj][N]
+  DevBuf<int> rows[3];     // internal rows per span (multiples of os only)
+  int nrows[3] = {0, 0, 0};
+  DevBuf<float2> fz;       // [Nk][Nth]
+  int lo = 0, hi = 0;      // theta columns the polar gather reads
+  DevBuf<float> fbuf;      // [Nslices][N][N]
+};
+
+struct AdjDev {
+  DevBuf<float> ta[3];     // [Nth]
+  DevBuf<float> sx[3];     // [Nth][Nrho]
+  DevBuf<int> woff[3];     // [Nth+1]
+  DevBuf<float4> wpt[3];
+  DevBuf<float2> c2lp[3];  // [N0][N0]
+  int clo[3], chi[3];
+  int lo2 = 0, hi2 = 0, W2 = 1;
+  DevBuf<float2> fz;       // [Nk][Nth]
+  DevBuf<float> H;         // [4N] or empty
+  bool filter = false;
+  DevBuf<float> rbuf;      // [Nslices][Nproj][N]
+  DevBuf<float> G[3];      // [Nslices][W2][Nrho]
+};
+
+struct lp_handle {
+  int device = 0;
+  int N = 0, N0 = 0, Nth = 0, Nrho = 0, Nk = 0, Nproj = 0, Nproj0 = 0, Nslices = 0, cor = 0, os = 1, cubic = 1;
+  float cor_f = 0.f;
+  std::vector<float> erho_h;
+  DevBuf<float> erho;
+  DevBuf<float2> spec;     // [Nslices][Nk][Nth]
+  FwdDev* fwd = nullptr;
+  AdjDev* adj = nullptr;
+  FFTPlan plan_rho, plan_th, plan_filt;
+};
+
+static void free_fwd(FwdDev* f) {
+  if (!f) return;
+  for (int k = 0; k < 3; ++k) {
+    f->c2lp[k].free_();
+    f->rows[k].free_();
+  }
+  f->thc.free_();
+  f->rhoc.free_();
+  f->fz.free_();
+  f->fbuf.free_();
+  delete f;
+}
+
+static void free_adj(AdjDev* a) {
+  if (!a) return;
+  for (int k = 0; k < 3; ++k) {
+    a->ta[k].free_();
+    a->sx[k].free_();
+    a->woff[k].free_();
+    a->wpt[k].free_();
+    a->c2lp[k].free_();
+    a->G[k].free_();
+  }
+  a->fz.free_();
+  a->H.free_();
+  a->rbuf.free_();
+  delete a;
+}
+
+// Hermitian extension of the half kernel fZ[Nrho][Nth/2+1] (cuFFT R2C layout,
+// lpRgpu.cu:28-34) to the rho-half / theta-full layout [Nrho/2+1][Nth].  Only
+// the Hermitian part of the kernel affects C2R output, so the kt = 0 and
+// kt = Nth/2 columns are symmetrised.
+static std::vector<float2> extend_kernel(const float* v, int Nrho, int Nth) {
+  const int nh = Nth / 2 + 1;
+  const int Nk = Nrho / 2 + 1;
+  auto at = [&](int kr, int kt) {
+    const size_t i = 2 * ((size_t)kr * nh + kt);
+    return std::make_pair((double)v[i], (double)v[i + 1]);
+  };
+  std::vector<float2> out((size_t)Nk * Nth);
+  for (int kr = 0; kr < Nk; ++kr) {
+    const int mr = (Nrho - kr) % Nrho;
+    for (int kt = 0; kt < Nth; ++kt) {
+      double re, im;
+      if (kt == 0 || kt == Nth / 2) {
+        auto a = at(kr, kt);
+        auto b = at(mr, kt);
+        re = 0.5 * (a.first + b.first);
+        im = 0.5 * (a.second - b.second);
+      } else if (kt < Nth / 2) {
+        auto a = at(kr, kt);
+        re = a.first;
+        im = a.second;
+      } else {
+        auto b = at(mr, Nth - kt);
+        re = b.first;
+        im = -b.second;
+      }
+      out[(size_t)kr * Nth + kt] = make_float2((float)re, (float)im);
+    }
+  }
+  return out;
+}
+
+static bool finite_coord(float v, float lim) { return isfinite(v) && fabsf(v) < lim; }
+
+// taps of one axis for coordinate t: first index and count
+static inline int first_tap(float t, int cubic) { return (int)floorf(t) - (cubic ? 1 : 0); }
+
+extern "C" {
+
+const char* lp_last_error(void) { return g_err.c_str(); }
+
+int lp_version(void) { return 100; }
+
+int lp_create(const float* glpars, int64_t n, int device, lp_handle** out) {
+  if (!glpars || !out) return set_err(LP_ERR_ARG, "lp_create: null pointer");
+  *out = nullptr;
+  if (n < 10) return set_err(LP_ERR_ARG, "lp_create: glpars too short (%lld)", (long long)n);
+  lp_handle h0;
+  h0.device = device;
+  h0.N = (int)glpars[0];
+  h0.N0 = (int)glpars[1];
+  h0.Nth = (int)glpars[2];
+  h0.Nrho = (int)glpars[3];
+  const int nspan = (int)glpars[4];
+  h0.Nproj = (int)glpars[5];
+  h0.Nslices = (int)glpars[6];
+  h0.cor_f = glpars[7];
+  h0.cor = (int)glpars[7];
+  h0.os = (int)glpars[8];
+  h0.cubic = (int)glpars[9];
+  if (nspan != 3) return set_err(LP_ERR_UNSUPPORTED, "lp_create: Nspan=%d (only 3 is supported)", nspan);
+  if (h0.N < 16 || h0.N % 16 != 0 || h0.N > 8192)
+    return set_err(LP_ERR_UNSUPPORTED, "lp_create: N=%d must be a multiple of 16 in [16, 8192]", h0.N);
+  if (h0.Nth != h0.N || h0.Nrho != 2 * h0.N) return set_err(LP_ERR_ARG, "lp_create: Ntheta/Nrho inconsistent");
+  if (h0.N0 < 1 || h0.N0 > h0.N || h0.os < 1 || h0.Nproj < 1 || h0.Nproj % h0.os != 0 || h0.Nslices < 1)
+    return set_err(LP_ERR_ARG, "lp_create: inconsistent geometry");
+  if (h0.N / 2 - h0.cor < 0 || h0.N / 2 - h0.cor + h0.N0 > h0.N)
+    return set_err(LP_ERR_ARG, "lp_create: cor=%d out of range", h0.cor);
+  if ((int64_t)n < 10 + (int64_t)h0.Nrho * h0.Nth)
+    return set_err(LP_ERR_ARG, "lp_create: glpars too short for erho");
+  h0.Nproj0 = h0.Nproj / h0.os;
+  h0.Nk = h0.Nrho / 2 + 1;
+  lp_handle* h = new lp_handle(h0);
+  h->erho_h.resize(h->Nrho);
+  for (int r = 0; r < h->Nrho; ++r) h->erho_h[r] = glpars[10 + (size_t)r * h->Nth];
+  h->plan_rho = make_fft_plan(h->Nrho);
+  h->plan_th = make_fft_plan(h->Nth);
+  h->plan_filt = make_fft_plan(4 * h->N);
+  DeviceGuard g(device);
+  cudaError_t e = configure_kernels(h->N);
+  if (e == cudaSuccess) e = dev_upload(h->erho, h->erho_h);
+  if (e == cudaSuccess) e = dev_alloc(h->spec, (size_t)h->Nslices * h->Nk * h->Nth);
+  if (e != cudaSuccess) {
+    h->erho.free_();
+    h->spec.free_();
+    delete h;
+    return set_err(e == cudaErrorMemoryAllocation ? LP_ERR_OOM : LP_ERR_CUDA, "lp_create: %s",
+                   cudaGetErrorString(e));
+  }
+  *out = h;
+  return LP_OK;
+}
+
+int lp_init_fwd(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, int64_t nf) {
+  if (!h || !pi || !pf) return set_err(LP_ERR_ARG, "lp_init_fwd: null pointer");
+  const int N = h->N, Nth = h->Nth, Nrho = h->Nrho, Nproj = h->Nproj;
+  // layout: Npids[3], pids[k]..., Ncids, cids  |  lp2C1[3], lp2C2[3], p2lp1[3], p2lp2[3], fZ
+  if (ni < 4) return set_err(LP_ERR_ARG, "lp_init_fwd: parsi too short");
+  int64_t npids[3];
+  int64_t sum_p = 0;
+  for (int k = 0; k < 3; ++k) {
+    npids[k] = pi[k];
+    if (npids[k] < 0 || npids[k] > (int64_t)Nproj * N) return set_err(LP_ERR_ARG, "lp_init_fwd: bad Npids");
+    sum_p += npids[k];
+  }
+  if (ni < 3 + sum_p + 1) return set_err(LP_ERR_ARG, "lp_init_fwd: parsi too short");
+  const int32_t* pids[3];
+  int64_t o = 3;
+  for (int k = 0; k < 3; ++k) {
+    pids[k] = pi + o;
+    o += npids[k];
+  }
+  const int64_t ncids = pi[o];
+  const int32_t* cids = pi + o + 1;
+  if (ncids < 0 || ncids > (int64_t)Nrho * Nth || ni != o + 1 + ncids)
+    return set_err(LP_ERR_ARG, "lp_init_fwd: parsi size %lld inconsistent", (long long)ni);
+  const int64_t nh = Nth / 2 + 1;
+  if (nf != 6 * ncids + 2 * sum_p + 2 * (int64_t)Nrho * nh)
+    return set_err(LP_ERR_ARG, "lp_init_fwd: parsf size %lld inconsistent", (long long)nf);
+  const float* lp2C1 = pf;
+  const float* lp2C2 = pf + 3 * ncids;
+  const float* p2lp1 = pf + 6 * ncids;
+  const float* p2lp2 = p2lp1 + sum_p;
+  const float* fzv = p2lp2 + sum_p;
+
+  FwdDev* F = new FwdDev();
+  const float lim = 8.0f * (float)Nrho;
+  // dense column-major Cartesian coordinates of every log-polar point
+  std::vector<float2> c2lp((size_t)Nth * Nrho);
+  for (int k = 0; k < 3; ++k) {
+    std::fill(c2lp.begin(), c2lp.end(), make_float2(qnan(), qnan()));
+    for (int64_t i = 0; i < ncids; ++i) {
+      const int idx = cids[i];
+      const float x = lp2C1[k * ncids + i], y = lp2C2[k * ncids + i];
+      if (idx < 0 || idx >= Nrho * Nth || !finite_coord(x, lim) || !finite_coord(y, lim)) {
+        free_fwd(F);
+        return set_err(LP_ERR_ARG, "lp_init_fwd: bad cids/lp2C entry %lld", (long long)i);
+      }
+      const int r = idx / Nth, t = idx % Nth;
+      c2lp[(size_t)t * Nrho + r] = make_float2(x, y);
+    }
+    DeviceGuard g(h->device);
+    cudaError_t e = dev_upload(F->c2lp[k], c2lp);
+    if (e != cudaSuccess) {
+      free_fwd(F);
+      return set_err(LP_ERR_OOM, "lp_init_fwd: %s", cudaGetErrorString(e));
+    }
+  }
+  // polar points: every span must own whole sinogram rows with one theta coordinate
+  std::vector<float> thc(Nproj, qnan());
+  std::vector<float> rhoc((size_t)Nproj * N, 0.f);
+  std::vector<int> owner(Nproj, -1);
+  std::vector<int> cnt(Nproj, 0);
+  int64_t off = 0;
+  int lo = Nth, hi = -1;
+  bool wraps = false;
+  for (int k = 0; k < 3; ++k) {
+    for (int64_t i = 0; i < npids[k]; ++i) {
+      const int idx = pids[k][i];
+      const float t = p2lp1[off + i], rr = p2lp2[off + i];
+      if (idx < 0 || idx >= Nproj * N || !finite_coord(t, lim) || !finite_coord(rr, lim)) {
+        free_fwd(F);
+        return set_err(LP_ERR_ARG, "lp_init_fwd: bad pids/p2lp entry");
+      }
+      const int row = idx / N, x = idx % N;
+      if (owner[row] == -1) {
+        owner[row] = k;
+        thc[row] = t;
+      } else if (owner[row] != k || thc[row] != t) {
+        free_fwd(F);
+        return set_err(LP_ERR_UNSUPPORTED,
+                       "lp_init_fwd: sinogram row %d is not one span with one log-polar angle", row);
+      }
+      cnt[row]++;
+      rhoc[(size_t)row * N + x] = rr;
+    }
+    off += npids[k];
+  }
+  std::vector<int> rows[3];
+  for (int row = 0; row < Nproj; ++row) {
+    if (owner[row] < 0 || cnt[row] != N) {
+      free_fwd(F);
+      return set_err(LP_ERR_UNSUPPORTED, "lp_init_fwd: sinogram row %d not covered exactly once", row);
+    }
+    if (row % h->os == 0) rows[owner[row]].push_back(row);
+    const int c = first_tap(thc[row], h->cubic);
+    const int n = h->cubic ? 4 : 2;
+    if (c < 0 || c + n - 1 >= Nth) wraps = true;
+    lo = std::min(lo, c);
+    hi = std::max(hi, c + n - 1);
+  }
+  if (wraps) {
+    lo = 0;
+    hi = Nth - 1;
+  }
+  F->lo = lo;
+  F->hi = hi;
+  {
+    DeviceGuard g(h->device);
+    cudaError_t e = dev_upload(F->thc, thc);
+    if (e == cudaSuccess) e = dev_upload(F->rhoc, rhoc);
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+      F->nrows[k] = (int)rows[k].size();
+      e = dev_upload(F->rows[k], rows[k]);
+    }
+    if (e == cudaSuccess) e = dev_upload(F->fz, extend_kernel(fzv, Nrho, Nth));
+    if (e == cudaSuccess) e = dev_alloc(F->fbuf, (size_t)h->Nslices * N * N);
+    if (e != cudaSuccess) {
+      free_fwd(F);
+      return set_err(e == cudaErrorMemoryAllocation ? LP_ERR_OOM : LP_ERR_CUDA, "lp_init_fwd: %s",
+                     cudaGetErrorString(e));
+    }
+  }
+  free_fwd(h->fwd);
+  h->fwd = F;
+  return LP_OK;
+}
+
+int lp_init_adj(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, int64_t nf) {
+  if (!h || !pi || !pf) return set_err(LP_ERR_ARG, "lp_init_adj: null pointer");
+  const int N = h->N, N0 = h->N0, Nth = h->Nth, Nrho = h->Nrho, Nproj = h->Nproj;
+  // layout: Ncids, Nlpids, Nwids, cids, lpids, wids, flag |
+  //         C2lp1[3], C2lp2[3], lp2p1[3], lp2p2[3], lp2p1w[3], lp2p2w[3], fZ, filter[4N]?
+  if (ni < 4) return set_err(LP_ERR_ARG, "lp_init_adj: parsi too short");
+  const int64_t nc = pi[0], nl = pi[1], nw = pi[2];
+  if (nc < 0 || nl < 0 || nw < 0 || nc > (int64_t)N * N || nl > (int64_t)Nrho * Nth || nw > (int64_t)Nrho * Nth ||
+      ni != 3 + nc + nl + nw + 1)
+    return set_err(LP_ERR_ARG, "lp_init_adj: parsi size %lld inconsistent", (long long)ni);
+  const int32_t* cids = pi + 3;
+  const int32_t* lpids = cids + nc;
+  const int32_t* wids = lpids + nl;
+  const int flag = wids[nw];
+  const int64_t nh = Nth / 2 + 1;
+  const int64_t nbase = 6 * nc + 6 * nl + 6 * nw + 2 * (int64_t)Nrho * nh;
+  if (nf != nbase + (flag == 1 ? 4 * (int64_t)N : 0))
+    return set_err(LP_ERR_ARG, "lp_init_adj: parsf size %lld inconsistent", (long long)nf);
+  const float* C2lp1 = pf;
+  const float* C2lp2 = C2lp1 + 3 * nc;
+  const float* lp2p1 = C2lp2 + 3 * nc;
+  const float* lp2p2 = lp2p1 + 3 * nl;
+  const float* lp2p1w = lp2p2 + 3 * nl;
+  const float* lp2p2w = lp2p1w + 3 * nw;
+  const float* fzv = lp2p2w + 3 * nw;
+  const float* filt = fzv + 2 * (size_t)Nrho * nh;
+  const float lim = 8.0f * (float)std::max(Nrho, Nproj);
+
+  AdjDev* A = new AdjDev();
+  auto fail = [&](int code, const char* msg) {
+    free_adj(A);
+    return set_err(code, "lp_init_adj: %s", msg);
+  };
+  DeviceGuard g(h->device);
+  const int off = N / 2 - N0 / 2;
+  int lo2 = Nth, hi2 = -1;
+  bool wraps = false;
+  for (int k = 0; k < 3; ++k) {
+    std::vector<float> ta(Nth, qnan());
+    std::vector<float> sx((size_t)Nth * Nrho, qnan());
+    for (int64_t i = 0; i < nl; ++i) {
+      const int idx = lpids[i];
+      const float s = lp2p2[k * nl + i], a = lp2p1[k * nl + i];
+      if (idx < 0 || idx >= Nrho * Nth || !finite_coord(s, lim) || !finite_coord(a, lim))
+        return fail(LP_ERR_ARG, "bad lpids/lp2p entry");
+      const int r = idx / Nth, t = idx % Nth;
+      if (isnan(ta[t])) ta[t] = a;
+      else if (ta[t] != a) return fail(LP_ERR_UNSUPPORTED, "log-polar column with more than one angle coordinate");
+      sx[(size_t)t * Nrho + r] = s;
+    }
+    // wrap points grouped by column
+    std::vector<int> woff(Nth + 1, 0);
+    for (int64_t i = 0; i < nw; ++i) {
+      const int idx = wids[i];
+      if (idx < 0 || idx >= Nrho * Nth) return fail(LP_ERR_ARG, "bad wids entry");
+      if (!finite_coord(lp2p2w[k * nw + i], lim) || !finite_coord(lp2p1w[k * nw + i], lim))
+        return fail(LP_ERR_ARG, "bad wrap coordinate");
+      woff[idx % Nth + 1]++;
+    }
+    for (int t = 0; t < Nth; ++t) woff[t + 1] += woff[t];
+    std::vector<float4> wpt(std::max<int64_t>(nw, 1));
+    std::vector<int> fillp(woff.begin(), woff.end() - 1);
+    for (int64_t i = 0; i < nw; ++i) {
+      const int idx = wids[i];
+      const int r = idx / Nth, t = idx % Nth;
+      wpt[fillp[t]++] = make_float4((float)r, lp2p2w[k * nw + i], lp2p1w[k * nw + i], 0.f);
+    }
+    int clo = Nth, chi = -1;
+    for (int t = 0; t < Nth; ++t) {
+      if (!isnan(ta[t]) || woff[t + 1] > woff[t]) {
+        clo = std::min(clo, t);
+        chi = std::max(chi, t);
+      }
+    }
+    A->clo[k] = clo;
+    A->chi[k] = chi;
+    // Cartesian pixels of the output window
+    std::vector<float2> c2((size_t)N0 * N0, make_float2(qnan(), qnan()));
+    for (int64_t i = 0; i < nc; ++i) {
+      const int idx = cids[i];
+      const float tt = C2lp1[k * nc + i], tr = C2lp2[k * nc + i];
+      if (idx < 0 || idx >= N * N || !finite_coord(tt, lim) || !finite_coord(tr, lim))
+        return fail(LP_ERR_ARG, "bad cids/C2lp entry");
+      const int Y = idx / N - off, X = idx % N - off;
+      if (Y < 0 || Y >= N0 || X < 0 || X >= N0) continue;
+      c2[(size_t)Y * N0 + X] = make_float2(tt, tr);
+      const int c = first_tap(tt, h->cubic);
+      const int n = h->cubic ? 4 : 2;
+      if (c < 0 || c + n - 1 >= Nth) wraps = true;
+      lo2 = std::min(lo2, c);
+      hi2 = std::max(hi2, c + n - 1);
+    }
+    cudaError_t e = dev_upload(A->ta[k], ta);
+    if (e == cudaSuccess) e = dev_upload(A->sx[k], sx);
+    if (e == cudaSuccess) e = dev_upload(A->woff[k], woff);
+    if (e == cudaSuccess) e = dev_upload(A->wpt[k], wpt);
+    if (e == cudaSuccess) e = dev_upload(A->c2lp[k], c2);
+    if (e != cudaSuccess) return fail(LP_ERR_OOM, cudaGetErrorString(e));
+  }
+  if (hi2 < lo2) {
+    lo2 = 0;
+    hi2 = 0;
+  }
+  if (wraps) {
+    lo2 = 0;
+    hi2 = Nth - 1;
+  }
+  A->lo2 = lo2;
+  A->hi2 = hi2;
+  A->W2 = hi2 - lo2 + 1;
+  cudaError_t e = dev_upload(A->fz, extend_kernel(fzv, Nrho, Nth));
+  if (e == cudaSuccess && flag == 1) {
+    if (h->N > 3200) return fail(LP_ERR_UNSUPPORTED, "FBP filter supports N <= 3200");
+    std::vector<float> Hh(4 * (size_t)N);
+    for (int kk = 0; kk < 4 * N; ++kk) Hh[kk] = filt[(kk + 2 * N) % (4 * N)];
+    e = dev_upload(A->H, Hh);
+    A->filter = true;
+  }
+  if (e == cudaSuccess) e = dev_alloc(A->rbuf, (size_t)h->Nslices * Nproj * N);
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = dev_alloc(A->G[k], (size_t)h->Nslices * A->W2 * Nrho);
+  if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? LP_ERR_OOM : LP_ERR_CUDA, cudaGetErrorString(e));
+  free_adj(h->adj);
+  h->adj = A;
+  return LP_OK;
+}
+
+int lp_destroy(lp_handle* h) {
+  if (!h) return LP_OK;
+  DeviceGuard g(h->device);
+  free_fwd(h->fwd);
+  free_adj(h->adj);
+  h->erho.free_();
+  h->spec.free_();
+  delete h;
+  return LP_OK;
+}
+
+int lp_get_geometry(const lp_handle* h, int32_t out[10]) {
+  if (!h || !out) return set_err(LP_ERR_ARG, "lp_get_geometry: null pointer");
+  const int32_t v[10] = {h->N, h->N0, h->Nth, h->Nrho, h->Nproj, h->Nproj0, h->Nslices, h->cor, h->os, h->cubic};
+  memcpy(out, v, sizeof(v));
+  return LP_OK;
+}
+
+int lp_device_bytes(const lp_handle* h, int64_t* bytes) {
+  if (!h || !bytes) return set_err(LP_ERR_ARG, "lp_device_bytes: null pointer");
+  int64_t b = h->erho.n * 4 + h->spec.n * 8;
+  if (h->fwd) {
+    for (int k = 0; k < 3; ++k) b += h->fwd->c2lp[k].n * 8 + h->fwd->rows[k].n * 4;
+    b += h->fwd->thc.n * 4 + h->fwd->rhoc.n * 4 + h->fwd->fz.n * 8 + h->fwd->fbuf.n * 4;
+  }
+  if (h->adj) {
+    for (int k = 0; k < 3; ++k)
+      b += h->adj->ta[k].n * 4 + h->adj->sx[k].n * 4 + h->adj->woff[k].n * 4 + h->adj->wpt[k].n * 16 +
+           h->adj->c2lp[k].n * 8 + h->adj->G[k].n * 4;
+    b += h->adj->fz.n * 8 + h->adj->H.n * 4 + h->adj->rbuf.n * 4;
+  }
+  *bytes = b;
+  return LP_OK;
+}
+
+int lp_fwd(lp_handle* h, float* R, const float* f, int S0, void* stream) {
+  if (!h) return set_err(LP_ERR_ARG, "lp_fwd: null handle");
+  if (!h->fwd) return set_err(LP_ERR_STATE, "lp_fwd: forward tables not initialised (lp_init_fwd)");
+  if (S0 < 0 || S0 > h->Nslices) return set_err(LP_ERR_ARG, "lp_fwd: S0=%d outside [0, %d]", S0, h->Nslices);
+  if (S0 == 0) return LP_OK;
+  if (!R || !f) return set_err(LP_ERR_ARG, "lp_fwd: null data pointer");
+  DeviceGuard g(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  FwdDev* F = h->fwd;
+  FwdIngestArgs ia{f, F->fbuf.p, h->N, h->N0, h->N / 2 - h->N0 / 2, h->cubic};
+  CUDA_TRY(launch_fwd_ingest(ia, S0, st));
+  if (h->cubic) {
+    ColPrefilterArgs ca{F->fbuf.p, h->N, h->N};
+    CUDA_TRY(launch_col_prefilter(ca, S0, st));
+  }
+  for (int k = 0; k < 3; ++k) {
+    FwdC2LPArgs a1{F->fbuf.p, h->spec.p, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, h->cubic,
+                   h->plan_rho};
+    CUDA_TRY(launch_fwd_c2lp(a1, S0, st));
+    ThetaConvArgs a2{h->spec.p, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), 0, h->Nth - 1,
+                     F->lo, F->hi, 0, h->plan_th};
+    CUDA_TRY(launch_theta_conv(a2, S0, st));
+    FwdLP2PolarArgs a3{h->spec.p, R, F->thc.p, F->rhoc.p, F->rows[k].p, F->nrows[k], h->N, h->N0, h->Nth,
+                       h->Nrho, h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho};
+    CUDA_TRY(launch_fwd_lp2polar(a3, S0, st));
+  }
+  return LP_OK;
+}
+
+int lp_adj(lp_handle* h, float* f, const float* R, int S0, void* stream) {
+  if (!h) return set_err(LP_ERR_ARG, "lp_adj: null handle");
+  if (!h->adj) return set_err(LP_ERR_STATE, "lp_adj: adjoint tables not initialised (lp_init_adj)");
+  if (S0 < 0 || S0 > h->Nslices) return set_err(LP_ERR_ARG, "lp_adj: S0=%d outside [0, %d]", S0, h->Nslices);
+  if (S0 == 0) return LP_OK;
+  if (!R || !f) return set_err(LP_ERR_ARG, "lp_adj: null data pointer");
+  DeviceGuard g(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  AdjDev* A = h->adj;
+  AdjIngestArgs ia{R, A->rbuf.p, A->filter ? A->H.p : nullptr, h->N, h->N0, h->Nproj, h->Nproj0, h->os,
+                   h->N / 2 - h->cor, h->cubic, h->plan_filt};
+  CUDA_TRY(launch_adj_ingest(ia, S0, st));
+  if (h->cubic) {
+    ColPrefilterArgs ca{A->rbuf.p, h->Nproj, h->N};
+    CUDA_TRY(launch_col_prefilter(ca, S0, st));
+  }
+  for (int k = 0; k < 3; ++k) {
+    if (A->chi[k] < A->clo[k]) {
+      CUDA_TRY(cudaMemsetAsync(A->G[k].p, 0, A->G[k].n * sizeof(float), st));
+      continue;
+    }
+    AdjPolar2LPArgs a1{A->rbuf.p, h->spec.p, A->ta[k].p, A->sx[k].p, A->woff[k].p, A->wpt[k].p, h->N, h->Nth,
+                       h->Nrho, h->Nk, h->Nproj, h->cubic, A->clo[k], A->chi[k], h->plan_rho};
+    CUDA_TRY(launch_adj_polar2lp(a1, S0, st));
+    ThetaConvArgs a2{h->spec.p, A->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), A->clo[k],
+                     A->chi[k], A->lo2, A->hi2, 0, h->plan_th};
+    CUDA_TRY(launch_theta_conv(a2, S0, st));
+    AdjLPColsArgs a3{h->spec.p, A->G[k].p, h->Nth, h->Nrho, h->Nk, A->lo2, A->hi2, A->W2, h->plan_rho};
+    CUDA_TRY(launch_adj_lpcols(a3, S0, st));
+  }
+  AdjLP2CartArgs a4{A->G[0].p, A->G[1].p, A->G[2].p, A->c2lp[0].p, A->c2lp[1].p, A->c2lp[2].p, f,
+                    h->N0, h->Nth, h->Nrho, A->lo2, A->W2, h->cubic, h->N0 * h->N0};
+  CUDA_TRY(launch_adj_lp2cart(a4, S0, st));
+  return LP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,105 @@
+// Kernel argument blocks and launch helpers shared by lp_kernels.cu and lp_handle.cu.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fft_device.cuh"
+
+namespace lpgb {
+
+// ---- forward ----------------------------------------------------------------
+struct FwdIngestArgs {        // centre f into the padded grid, prefilter rows
+  const float* fin;           // [S][N0][N0] caller's image
+  float* fbuf;                // [S][N][N]
+  int N, N0, off, cubic;
+};
+
+struct ColPrefilterArgs {     // prefilter along the slow axis, in place
+  float* img;                 // [S][H][W]
+  int H, W;
+};
+
+struct FwdC2LPArgs {          // Cartesian -> log-polar gather, e^rho, FFT along rho
+  const float* fbuf;          // [S][N][N] prefiltered image
+  float2* spec;               // [S][Nk][Nth] spectrum (Nk = N+1 rho frequencies)
+  const float2* c2lp;         // [Nth][Nrho] texel coordinates (x, y); x = NaN outside the disk
+  const float* erho;          // [Nrho]
+  int N, Nth, Nrho, Nk, cubic;
+  FFTPlan plan;               // length Nrho
+};
+
+struct ThetaConvArgs {        // FFT along theta, multiply by the kernel, inverse
+  float2* spec;               // [S][Nk][Nth]
+  const float2* fz;           // [Nk][Nth] Hermitian-extended kernel
+  int Nth, Nk;
+  float scale;
+  int in_lo, in_hi;           // columns outside [in_lo, in_hi] are read as 0
+  int out_lo, out_hi;         // only these columns are written back
+  int conj_fz;
+  FFTPlan plan;               // length Nth
+};
+
+struct FwdLP2PolarArgs {      // inverse FFT along rho of theta-combined columns, polar gather
+  const float2* spec;         // [S][Nk][Nth]
+  float* Rout;                // [S][Nproj0][N0] caller's sinogram
+  const float* thc;           // [Nproj] theta texel coordinate per internal angle row
+  const float* rhoc;          // [Nproj][N] rho texel coordinate per polar point
+  const int* rows;            // internal rows handled by this launch
+  int nrows;
+  int N, N0, Nth, Nrho, Nk, Nproj0, os, cor_off, cubic;
+  FFTPlan plan;               // length Nrho
+};
+
+// ---- adjoint ----------------------------------------------------------------
+struct AdjIngestArgs {        // cor shift, angle step, edge padding, FBP filter, row prefilter
+  const float* Rin;           // [S][Nproj0][N0]
+  float* rbuf;                // [S][Nproj][N]
+  const float* H;             // [4N] filter in FFT order, or null
+  int N, N0, Nproj, Nproj0, os, cor_off, cubic;
+  FFTPlan plan;               // length 4N (filter)
+};
+
+struct AdjPolar2LPArgs {      // polar -> log-polar gather (+ wrap points), FFT along rho
+  const float* rbuf;          // [S][Nproj][N] prefiltered sinogram
+  float2* spec;               // [S][Nk][Nth]
+  const float* ta;            // [Nth] angle texel coordinate per column (NaN: no points)
+  const float* sx;            // [Nth][Nrho] s texel coordinate (NaN: not a point)
+  const int* woff;            // [Nth+1] wrap-point offsets per column
+  const float4* wpt;          // wrap points: (rho, s coordinate, angle coordinate, 0)
+  int N, Nth, Nrho, Nk, Nproj, cubic;
+  int clo, chi;
+  FFTPlan plan;               // length Nrho
+};
+
+struct AdjLPColsArgs {        // inverse FFT along rho, write real log-polar columns
+  const float2* spec;         // [S][Nk][Nth]
+  float* G;                   // [S][W2][Nrho]
+  int Nth, Nrho, Nk, lo2, hi2, W2;
+  FFTPlan plan;
+};
+
+struct AdjLP2CartArgs {       // log-polar -> Cartesian gather summed over spans, crop
+  const float* G0;
+  const float* G1;
+  const float* G2;            // [S][W2][Nrho] per span
+  const float2* c2lp0;
+  const float2* c2lp1;
+  const float2* c2lp2;        // [N0][N0] (theta, rho) texel coordinates per span; NaN outside disk
+  float* fout;                // [S][N0][N0]
+  int N0, Nth, Nrho, lo2, W2, cubic;
+  int npix;
+};
+
+// launches (defined in lp_kernels.cu); return the launch error
+cudaError_t launch_fwd_ingest(const FwdIngestArgs& a, int S, cudaStream_t st);
+cudaError_t launch_col_prefilter(const ColPrefilterArgs& a, int S, cudaStream_t st);
+cudaError_t launch_fwd_c2lp(const FwdC2LPArgs& a, int S, cudaStream_t st);
+cudaError_t launch_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st);
+cudaError_t launch_fwd_lp2polar(const FwdLP2PolarArgs& a, int S, cudaStream_t st);
+cudaError_t launch_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st);
+cudaError_t launch_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st);
+cudaError_t launch_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st);
+cudaError_t launch_adj_lp2cart(const AdjLP2CartArgs& a, int S, cudaStream_t st);
+cudaError_t configure_kernels(int N);
+
+}  // namespace lpgb

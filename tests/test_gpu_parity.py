@@ -1,0 +1,138 @@
+"""GPU path against the oracle on identical float32 tables (relative L2 <= 1e-5).
+
+Tables come either from the reference's own precompute (fixtures made by
+tests/golden/make_golden.py) or from this library's precompute; the oracle is
+fed exactly the same packed arrays, so any difference is the kernels'.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import lprec_oracle as O
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+NAMES = ['glpars', 'fwdparsi', 'fwdparamsf', 'adjparsi', 'adjparamsf']
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _handle(packed):
+    from lprec_gb300 import _lib
+    h = _lib.Handle(packed[0], 0)
+    if packed[1] is not None:
+        h.init_fwd(packed[1], packed[2])
+    h.init_adj(packed[3], packed[4])
+    return h
+
+
+def _fwd(torch, h, f):
+    ft = torch.as_tensor(np.float32(f)).cuda()
+    R = torch.full((f.shape[0], h.Nproj, h.N0), float('nan'), device='cuda')
+    h.fwd(R.data_ptr(), ft.data_ptr(), f.shape[0], torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return R.cpu().numpy().astype(np.float64)
+
+
+def _adj(torch, h, R):
+    Rt = torch.as_tensor(np.float32(R)).cuda()
+    f = torch.full((R.shape[0], h.N0, h.N0), float('nan'), device='cuda')
+    h.adj(f.data_ptr(), Rt.data_ptr(), R.shape[0], torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return f.cpu().numpy().astype(np.float64)
+
+
+def _inputs(G, S, seed):
+    rng = np.random.default_rng(seed)
+    f = rng.random((S, G.N0, G.N0)).astype(np.float32).astype(np.float64)
+    R = rng.random((S, G.Nproj0, G.N0)).astype(np.float32).astype(np.float64)
+    return f, R
+
+
+@pytest.mark.parametrize("case", ["n64_cubic_ramp", "n48_cor_shepp", "n32_os2_linear_hann", "n64_cubic_none"])
+def test_reference_tables(torch_cuda, golden_dir, case):
+    """Reference-made tables: GPU fwd/adj == oracle fwd/adj."""
+    z = np.load(os.path.join(golden_dir, 'packed_%s.npz' % case))
+    packed = [z[n] for n in NAMES]
+    tr = O.Transform.from_packed(*packed)
+    h = _handle(packed)
+    f, R = _inputs(tr.G, 3, 0)
+    Rg = _fwd(torch_cuda, h, f)
+    fg = _adj(torch_cuda, h, R)
+    Ro = tr.fwd(f)
+    fo = tr.adj(R)
+    assert np.all(np.isfinite(Rg)) and np.all(np.isfinite(fg))
+    assert O.rel_l2(Rg, Ro) < TOL, O.rel_l2(Rg, Ro)
+    assert O.rel_l2(fg, fo) < TOL, O.rel_l2(fg, fo)
+
+
+@pytest.mark.parametrize("args", [(256, 384, 'cubic', 'ramp', 128), (96, 150, 'cubic', 'hamming', 45),
+                                  (128, 64, 'linear', 'none', 64), (80, 120, 'cubic', 'parzen', 40.5)])
+def test_own_tables_vs_fp64_oracle(torch_cuda, args):
+    """This library's fp64 precompute; the oracle runs with unrounded float64 tables."""
+    from lprec_gb300 import _lib
+    N0, Nproj, interp, filt, cor = args
+    packed = _lib.precompute(N0, Nproj, 2, cor, interp, filt, precision='fp64')
+    h = _handle(packed)
+    tr = O.Transform(N0, Nproj, 2, filt, cor, interp, mode='fp64', rounded=False)
+    f, R = _inputs(tr.G, 2, 1)
+    assert O.rel_l2(_fwd(torch_cuda, h, f), tr.fwd(f)) < TOL
+    assert O.rel_l2(_adj(torch_cuda, h, R), tr.adj(R)) < TOL
+
+
+def test_reference_pins_adj_many(torch_cuda, golden_dir):
+    """tests/test_adj_many.py pins on the GPU: 8 slices scaled by (8-k)."""
+    from lprec_gb300 import lpTransform
+    torch = torch_cuda
+    d = np.load(os.path.join(golden_dir, 'testdata.npz'))
+    S = 8
+    fa = np.stack([d['f'] * (S - k) for k in range(S)]).astype(np.float32)
+    Ra = np.stack([d['R'] * (S - k) for k in range(S)]).astype(np.float32)
+    lp = lpTransform(512, 384, S, 'None', 256, 'cubic')
+    lp.precompute(1)
+    lp.initcmem(1, 0)
+    fg, Rg = torch.as_tensor(fa).cuda(), torch.as_tensor(Ra).cuda()
+    Rfg = torch.zeros((S, 384, 512), device='cuda')
+    fRg = torch.zeros((S, 512, 512), device='cuda')
+    RfRg = torch.zeros((S, 384, 512), device='cuda')
+    lp.fwdp(Rfg, fg, 0)
+    lp.adjp(fRg, Rg, 0)
+    lp.fwdp(RfRg, fRg, 0)
+    Rf, fR, RfR = [x.cpu().double().numpy() for x in (Rfg, fRg, RfRg)]
+    s1 = np.sum(Rf * Ra)
+    s2 = np.sum(fR * fa)
+    err0 = abs(s1 - s2) / abs(s2)
+    err1 = np.linalg.norm(fR - fa) / np.linalg.norm(fa)
+    err2 = np.linalg.norm(RfR - Rf) / np.linalg.norm(Rf)
+    assert err0 < 5e-3 and err1 < 7e-3 and err2 < 7e-4, (err0, err1, err2)
+
+
+def test_batch_equals_single(torch_cuda):
+    from lprec_gb300 import _lib
+    packed = _lib.precompute(64, 96, 4, 32, 'cubic', 'shepp-logan')
+    h = _handle(packed)
+    G = O.create_geometry(64, 96, 4, 32, 'cubic')
+    f, R = _inputs(G, 4, 5)
+    Rb = _fwd(torch_cuda, h, f)
+    fb = _adj(torch_cuda, h, R)
+    for s in range(4):
+        assert np.array_equal(_fwd(torch_cuda, h, f[s:s + 1])[0], Rb[s])
+        assert np.array_equal(_adj(torch_cuda, h, R[s:s + 1])[0], fb[s])
+
+
+def test_deterministic(torch_cuda):
+    from lprec_gb300 import _lib
+    packed = _lib.precompute(128, 192, 2, 64, 'cubic', 'ramp')
+    h = _handle(packed)
+    G = O.create_geometry(128, 192, 2, 64, 'cubic')
+    f, R = _inputs(G, 2, 9)
+    assert np.array_equal(_fwd(torch_cuda, h, f), _fwd(torch_cuda, h, f))
+    assert np.array_equal(_adj(torch_cuda, h, R), _adj(torch_cuda, h, R))
