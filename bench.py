@@ -1,0 +1,385 @@
+"""Benchmark: batched fwd+adj slices/s of the log-polar Radon transform at N=2048.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one forward (Radon) transform plus one adjoint with the
+shepp-logan FBP filter over a batch of 128 slices of 2048x2048 images and
+3000x2048 sinograms (random-ellipse phantoms, 30 ellipses, seed 3, with
+Gaussian noise of 1% of the sinogram maximum on the adjoint's input),
+all resident in HBM.  `value` is slices/s over all ranks (replicas, weak
+scaling).  `e2e` repeats the step through the public lpTransform API from
+pinned host buffers with the host<->device copies inside the timed region.
+
+`--impl reference` times the CPU float64 restatement of the reference
+algorithm (the oracle; the reference itself has no CPU path and its CUDA code
+does not build with CUDA 13) on the host cores, one slice per process.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "fwd+adj slices/s (N=2048, Nproj=3000, batched)"
+UNIT = "slices/s"
+WORKLOAD = dict(N=2048, Nproj=3000, S=128, filter="shepp-logan", interp="cubic", ellipses=30, seed=3, noise=0.01)
+# algorithmic HBM bytes per slice of one fwd+adj step (N=2048, Nproj=3000, batch 128)
+ALGO_BYTES_PER_SLICE = 1.541e9
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if not self.path or not os.path.exists(self.path):
+            return out
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+def phantoms_gpu(torch, N, S, n_ell, seed, dev):
+    """Random-ellipse phantoms (the oracle's generator, vectorised on the GPU)."""
+    rng = np.random.default_rng(seed)
+    lin = torch.linspace(-1, 1, N, dtype=torch.float64, device=dev)
+    x2, x1 = torch.meshgrid(-lin, lin, indexing="ij")
+    out = torch.zeros((S, N, N), dtype=torch.float32, device=dev)
+    for s in range(S):
+        img = torch.zeros((N, N), dtype=torch.float64, device=dev)
+        for _ in range(n_ell):
+            r = 0.7 * np.sqrt(rng.uniform())
+            phi = 2 * np.pi * rng.uniform()
+            cx, cy = r * np.cos(phi), r * np.sin(phi)
+            a, b = rng.uniform(0.05, 0.35, size=2)
+            rot = rng.uniform(0, np.pi)
+            val = rng.uniform(-0.2, 1.0)
+            u = (x1 - cx) * np.cos(rot) + (x2 - cy) * np.sin(rot)
+            v = -(x1 - cx) * np.sin(rot) + (x2 - cy) * np.cos(rot)
+            img += val * (((u / a) ** 2 + (v / b) ** 2) <= 1)
+        out[s] = img.float()
+    return out
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: oracle (float64 NumPy restatement), one slice per process
+# ---------------------------------------------------------------------------
+def _cpu_slice(args):
+    path, N, seed = args
+    sys.path.insert(0, ROOT)
+    from oracle import lprec_oracle as O
+    z = np.load(path)
+    tr = O.Transform.from_packed(z["glpars"], z["fwdparsi"], z["fwdparamsf"], z["adjparsi"], z["adjparamsf"])
+    rng = np.random.default_rng(seed)
+    f = O.ellipse_phantom(N, WORKLOAD["ellipses"], rng)[None]
+    t0 = time.perf_counter()
+    R = tr.fwd(f)
+    tr.adj(R)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(packed, nslices, nproc):
+    import multiprocessing as mp
+    fd, path = tempfile.mkstemp(suffix=".npz")
+    os.close(fd)
+    np.savez(path, glpars=packed[0], fwdparsi=packed[1], fwdparamsf=packed[2], adjparsi=packed[3],
+             adjparamsf=packed[4])
+    try:
+        ctx = mp.get_context("spawn")
+        t0 = time.perf_counter()
+        with ctx.Pool(nproc) as pool:
+            per = pool.map(_cpu_slice, [(path, WORKLOAD["N"], 1000 + i) for i in range(nslices)])
+        wall = time.perf_counter() - t0
+    finally:
+        os.unlink(path)
+    return nslices / wall, wall, per
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    from lprec_gb300 import _lib
+    W = WORKLOAD
+    packed = _lib.precompute(W["N"], W["Nproj"], 1, W["N"] / 2, W["interp"], W["filter"], precision="fp64")
+    cores = len(os.sched_getaffinity(0))
+    nproc = max(1, min(cores, 8))
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, wall, _ = cpu_baseline(packed, nproc, nproc)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * nproc / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic random-ellipse phantoms",
+            "config": {"workload": "fwd+adj N=2048 Nproj=3000 shepp-logan cubic", "slices_per_step": nproc},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nproc, "kind": "port",
+                             "sample": "%d slices per step, one process per slice (oracle, float64)" % nproc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# GPU benchmark
+# ---------------------------------------------------------------------------
+def per_kernel_bytes(h, S, prof):
+    """Algorithmic HBM bytes per kernel kind for the launches recorded in `prof`."""
+    N, N0, Nk, Nth, Nrho = h.N, h.N0, h.Nrho // 2 + 1, h.Ntheta, h.Nrho
+    P, P0 = h.Nproj_int, h.Nproj
+    half = Nth // 2 + 8
+    b = {
+        "fwd_ingest": S * (N0 * N0 + N * N) * 4,
+        "col_prefilter": S * (2 * N * N + 2 * P * N) * 4 / 2,      # mean of the fwd and adj launches
+        "fwd_c2lp": S * (N * N * 4 + Nk * Nth * 8) + Nth * Nrho * 8 / 1,
+        "theta_conv": S * (Nk * Nth * 8 + Nk * half * 8) + Nk * Nth * 8,
+        "fwd_lp2polar": S * (Nk * half * 8 + P0 // 3 * N0 * 4),
+        "adj_ingest": S * (P0 * N0 + P * N) * 4,
+        "adj_polar2lp": S * (P // 3 * N * 4 + Nk * half * 8),
+        "adj_lpcols": S * (Nk * half * 8 + half * Nrho * 4),
+        "adj_lp2cart": S * (3 * half * Nrho * 4 + N0 * N0 * 4) + 3 * N0 * N0 * 8,
+    }
+    return b
+
+
+def run_ours(args):
+    import torch
+    from lprec_gb300 import lpTransform, _lib
+    ws, rank, local = dist_env()
+    dist = ws > 1
+    if dist:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dev = local
+    torch.cuda.set_device(dev)
+    W = WORKLOAD
+    N, Nproj, S = W["N"], W["Nproj"], W["S"]
+    if args.small:
+        N, Nproj, S = 256, 384, 8
+    lp = lpTransform(N, Nproj, S, W["filter"], N / 2, W["interp"])
+    t0 = time.perf_counter()
+    lp.precompute(1)
+    t_pre = time.perf_counter() - t0
+    lp.initcmem(1, dev)
+    h = lp.clphandle[dev]
+    f = phantoms_gpu(torch, N, S, W["ellipses"], W["seed"] + rank, dev)
+    R = torch.empty((S, Nproj, N), device=dev)
+    lp.fwdp(R, f, dev)
+    torch.cuda.synchronize()
+    gen = torch.Generator(device=dev).manual_seed(W["seed"])
+    Rn = R + W["noise"] * float(R.abs().max()) * torch.randn(R.shape, device=dev, generator=gen)
+    Rout = torch.empty_like(R)
+    fout = torch.empty_like(f)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        lp.fwdp(Rout, f, dev)
+        lp.adjp(fout, Rn, dev)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        tdist.barrier()
+    h.set_profiling(True)
+    h.profile()  # clear
+    n0 = _lib.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(dev) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = _lib.launch_count() - n0
+    prof = h.profile()
+    h.set_profiling(False)
+    ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = ws * S / (ms_step / 1000.0)
+
+    # plain drop-in: one slice per call
+    nplain = min(S, 16)
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for s in range(nplain):
+        lp.fwdp(Rout[s:s + 1], f[s:s + 1], dev)
+        lp.adjp(fout[s:s + 1], Rn[s:s + 1], dev)
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain = nplain / (p0.elapsed_time(p1) / 1000.0)
+
+    # e2e through the public API from pinned host buffers
+    fh = f.cpu().pin_memory()
+    Rh = Rn.cpu().pin_memory()
+    Rh_out = torch.empty(R.shape, dtype=torch.float32).pin_memory()
+    fh_out = torch.empty(f.shape, dtype=torch.float32).pin_memory()
+    fd = torch.empty_like(f)
+    Rd = torch.empty_like(R)
+
+    def e2e_step():
+        fd.copy_(fh, non_blocking=True)
+        lp.fwdp(Rout, fd, dev)
+        Rh_out.copy_(Rout, non_blocking=True)
+        Rd.copy_(Rh, non_blocking=True)
+        lp.adjp(fout, Rd, dev)
+        fh_out.copy_(fout, non_blocking=True)
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    torch.cuda.synchronize()
+    q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ke = max(2, args.steps // 2)
+    q0.record(stream)
+    for _ in range(ke):
+        e2e_step()
+    q1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = q0.elapsed_time(q1) / ke
+    if dist:
+        t = torch.tensor([e2e_ms], device=dev)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e = ws * S / (e2e_ms / 1000.0)
+    h2d = (f.numel() + R.numel()) * 4
+    d2h = h2d
+
+    # roofline of the dominant kernel
+    peak, peak_kind = peaks()
+    kb = per_kernel_bytes(h, S, prof)
+    top = max(prof.items(), key=lambda kv: kv[1][0])
+    name, (tms, nl) = top
+    per_launch_ms = tms / max(nl, 1)
+    per_launch_bytes = kb[name] if name != "theta_conv" else kb[name]
+    achieved = per_launch_bytes / (per_launch_ms / 1000.0) / 1e9
+    kernels = {k: {"ms_total": round(v[0], 3), "launches": v[1],
+                   "share": round(v[0] / max(sum(x[0] for x in prof.values()), 1e-9), 4)}
+               for k, v in prof.items() if v[1]}
+    step_gbs = ALGO_BYTES_PER_SLICE * S / (ms_step / 1000.0) / 1e9
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic random-ellipse phantoms (30 ellipses, seed 3), 1% Gaussian noise on the adjoint input",
+            "config": {"workload": "fwd+adj batch: %d slices N=%d Nproj=%d cubic %s" % (S, N, Nproj, W["filter"]),
+                       "slices": S, "N": N, "Nproj": Nproj, "parallelism": "replicas" if ws > 1 else "single",
+                       "l2": "inputs larger than L2 (%.1f GB per step)" % (S * (N * N + Nproj * N) * 4 / 1e9),
+                       "precompute_s": round(t_pre, 2)},
+            "plain_value": plain, "batched_over_plain": value / plain / ws,
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                         "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms},
+            "step_roofline": {"algorithmic_bytes_per_slice": ALGO_BYTES_PER_SLICE, "achieved": step_gbs,
+                              "peak": peak, "frac": step_gbs / peak},
+            "kernels": kernels,
+            "clocks": clk.summary()}
+    if rank == 0 and not args.no_cpu:
+        cores = len(os.sched_getaffinity(0))
+        nproc = max(1, min(cores, 4))
+        packed = (lp.glpars, lp.fwdparsi, lp.fwdparamsf, lp.adjparsi, lp.adjparamsf)
+        if args.small:
+            packed = _lib.precompute(N, Nproj, 1, N / 2, W["interp"], W["filter"], precision="fp64")
+        v, wall, per = cpu_baseline(packed, nproc, nproc)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nproc, "kind": "port",
+                                "sample": "%d slices fwd+adj N=%d, one process per slice, oracle float64, %.1f s"
+                                          % (nproc, N, wall)}
+    if dist:
+        tdist.barrier()
+        tdist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true", help="N=256 smoke-size workload")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -103,6 +103,23 @@ int lp_get_geometry(const lp_handle* h, int32_t out[10]);
 /* Bytes of device memory the handle holds. */
 int lp_device_bytes(const lp_handle* h, int64_t* bytes);
 
+/*
+ * Instrumentation (no counterpart in the reference, whose only timing is
+ * wall-clock tic/toc in tests/timing.py:2-11).
+ *   lp_launch_count   kernels this library has launched in the process
+ *   lp_kernel_count   number of kernel kinds; lp_kernel_name(id) their names
+ *   lp_set_profiling  bracket every launch of the handle with CUDA events on
+ *                     the launch stream
+ *   lp_profile_collect  wait for the recorded events and return, per kernel
+ *                     kind, total milliseconds and launches (arrays of
+ *                     lp_kernel_count() entries); clears the record
+ */
+long long lp_launch_count(void);
+int lp_kernel_count(void);
+const char* lp_kernel_name(int id);
+int lp_set_profiling(lp_handle* h, int enable);
+int lp_profile_collect(lp_handle* h, double* ms, int64_t* launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,7 +21,8 @@ PRECISION = {"reference": 0, "fp64": 1}
 
 # every symbol include/lprec_gb300.h declares
 EXPORTS = ("lp_last_error", "lp_version", "lp_precompute_sizes", "lp_precompute", "lp_create", "lp_init_fwd",
-           "lp_init_adj", "lp_destroy", "lp_fwd", "lp_adj", "lp_get_geometry", "lp_device_bytes")
+           "lp_init_adj", "lp_destroy", "lp_fwd", "lp_adj", "lp_get_geometry", "lp_device_bytes",
+           "lp_launch_count", "lp_kernel_count", "lp_kernel_name", "lp_set_profiling", "lp_profile_collect")
 
 
 class LprecError(RuntimeError):
@@ -59,6 +60,11 @@ def lib():
         "lp_adj": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
         "lp_get_geometry": (c_int, [c_void_p, P_i32]),
         "lp_device_bytes": (c_int, [c_void_p, P_i64]),
+        "lp_launch_count": (ctypes.c_longlong, []),
+        "lp_kernel_count": (c_int, []),
+        "lp_kernel_name": (c_char_p, [c_int]),
+        "lp_set_profiling": (c_int, [c_void_p, c_int]),
+        "lp_profile_collect": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_double), P_i64]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -75,6 +81,10 @@ def check(rc):
 
 def _ptr(a, ctype):
     return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+def launch_count():
+    return int(lib().lp_launch_count())
 
 
 def precompute(N0, Nproj, Nslices, cor, interp_type, filter_type, precision="reference", with_fwd=True,
@@ -138,6 +148,18 @@ class Handle:
         b = np.zeros(1, np.int64)
         check(lib().lp_device_bytes(self._h, _ptr(b, ctypes.c_int64)))
         return int(b[0])
+
+    def set_profiling(self, on):
+        check(lib().lp_set_profiling(self._h, 1 if on else 0))
+
+    def profile(self):
+        """{kernel name: (total ms, launches)} of the launches recorded since the last call."""
+        L = lib()
+        n = L.lp_kernel_count()
+        ms = np.zeros(n, np.float64)
+        cnt = np.zeros(n, np.int64)
+        check(L.lp_profile_collect(self._h, _ptr(ms, ctypes.c_double), _ptr(cnt, ctypes.c_int64)))
+        return {L.lp_kernel_name(i).decode(): (float(ms[i]), int(cnt[i])) for i in range(n)}
 
     def close(self):
         if self._h is not None and _lib is not None:

@@ -7,6 +7,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -112,8 +113,34 @@ struct AdjDev {
   DevBuf<float> G[3];      // [Nslices][W2][Nrho]
 };
 
+enum KernelId {
+  K_FWD_INGEST = 0,
+  K_COL_PREFILTER,
+  K_FWD_C2LP,
+  K_THETA_CONV,
+  K_FWD_LP2POLAR,
+  K_ADJ_INGEST,
+  K_ADJ_POLAR2LP,
+  K_ADJ_LPCOLS,
+  K_ADJ_LP2CART,
+  K_COUNT
+};
+static const char* kKernelNames[K_COUNT] = {"fwd_ingest", "col_prefilter", "fwd_c2lp", "theta_conv",
+                                             "fwd_lp2polar", "adj_ingest", "adj_polar2lp", "adj_lpcols",
+                                             "adj_lp2cart"};
+
+static std::atomic<long long> g_launches(0);
+
+struct ProfRec {
+  int kid;
+  cudaEvent_t a, b;
+};
+
 struct lp_handle {
   int device = 0;
+  bool profiling = false;
+  std::vector<ProfRec> prof;        // recorded launches not yet collected
+  std::vector<cudaEvent_t> evpool;  // reusable events
   int N = 0, N0 = 0, Nth = 0, Nrho = 0, Nk = 0, Nproj = 0, Nproj0 = 0, Nslices = 0, cor = 0, os = 1, cubic = 1;
   float cor_f = 0.f;
   std::vector<float> erho_h;
@@ -194,9 +221,70 @@ static bool finite_coord(float v, float lim) { return isfinite(v) && fabsf(v) < 
 // taps of one axis for coordinate t: first index and count
 static inline int first_tap(float t, int cubic) { return (int)floorf(t) - (cubic ? 1 : 0); }
 
+static cudaEvent_t take_event(lp_handle* h) {
+  if (!h->evpool.empty()) {
+    cudaEvent_t e = h->evpool.back();
+    h->evpool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Launch one kernel; with profiling on, bracket it with events on its stream.
+template <typename F>
+static cudaError_t launch(lp_handle* h, int kid, cudaStream_t st, F fn) {
+  ProfRec r{kid, nullptr, nullptr};
+  if (h->profiling) {
+    r.a = take_event(h);
+    r.b = take_event(h);
+    cudaEventRecord(r.a, st);
+  }
+  cudaError_t e = fn();
+  if (e == cudaSuccess) g_launches.fetch_add(1, std::memory_order_relaxed);
+  if (h->profiling) {
+    cudaEventRecord(r.b, st);
+    h->prof.push_back(r);
+  }
+  return e;
+}
+
 extern "C" {
 
 const char* lp_last_error(void) { return g_err.c_str(); }
+
+long long lp_launch_count(void) { return g_launches.load(); }
+
+int lp_kernel_count(void) { return K_COUNT; }
+
+const char* lp_kernel_name(int id) { return (id >= 0 && id < K_COUNT) ? kKernelNames[id] : ""; }
+
+int lp_set_profiling(lp_handle* h, int enable) {
+  if (!h) return set_err(LP_ERR_ARG, "lp_set_profiling: null handle");
+  h->profiling = enable != 0;
+  return LP_OK;
+}
+
+int lp_profile_collect(lp_handle* h, double* ms, int64_t* launches) {
+  if (!h || !ms || !launches) return set_err(LP_ERR_ARG, "lp_profile_collect: null pointer");
+  DeviceGuard g(h->device);
+  for (int k = 0; k < K_COUNT; ++k) {
+    ms[k] = 0.0;
+    launches[k] = 0;
+  }
+  for (const ProfRec& r : h->prof) {
+    float t = 0.f;
+    CUDA_TRY(cudaEventSynchronize(r.b));
+    CUDA_TRY(cudaEventElapsedTime(&t, r.a, r.b));
+    ms[r.kid] += t;
+    launches[r.kid] += 1;
+    h->evpool.push_back(r.a);
+    h->evpool.push_back(r.b);
+  }
+  h->prof.clear();
+  return LP_OK;
+}
 
 int lp_version(void) { return 100; }
 
@@ -508,6 +596,11 @@ int lp_destroy(lp_handle* h) {
   free_adj(h->adj);
   h->erho.free_();
   h->spec.free_();
+  for (const ProfRec& r : h->prof) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
   delete h;
   return LP_OK;
 }
@@ -546,21 +639,21 @@ int lp_fwd(lp_handle* h, float* R, const float* f, int S0, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   FwdDev* F = h->fwd;
   FwdIngestArgs ia{f, F->fbuf.p, h->N, h->N0, h->N / 2 - h->N0 / 2, h->cubic};
-  CUDA_TRY(launch_fwd_ingest(ia, S0, st));
+  CUDA_TRY(launch(h, K_FWD_INGEST, st, [&] { return launch_fwd_ingest(ia, S0, st); }));
   if (h->cubic) {
     ColPrefilterArgs ca{F->fbuf.p, h->N, h->N};
-    CUDA_TRY(launch_col_prefilter(ca, S0, st));
+    CUDA_TRY(launch(h, K_COL_PREFILTER, st, [&] { return launch_col_prefilter(ca, S0, st); }));
   }
   for (int k = 0; k < 3; ++k) {
     FwdC2LPArgs a1{F->fbuf.p, h->spec.p, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, h->cubic,
                    h->plan_rho};
-    CUDA_TRY(launch_fwd_c2lp(a1, S0, st));
+    CUDA_TRY(launch(h, K_FWD_C2LP, st, [&] { return launch_fwd_c2lp(a1, S0, st); }));
     ThetaConvArgs a2{h->spec.p, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), 0, h->Nth - 1,
                      F->lo, F->hi, 0, h->plan_th};
-    CUDA_TRY(launch_theta_conv(a2, S0, st));
+    CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
     FwdLP2PolarArgs a3{h->spec.p, R, F->thc.p, F->rhoc.p, F->rows[k].p, F->nrows[k], h->N, h->N0, h->Nth,
                        h->Nrho, h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho};
-    CUDA_TRY(launch_fwd_lp2polar(a3, S0, st));
+    CUDA_TRY(launch(h, K_FWD_LP2POLAR, st, [&] { return launch_fwd_lp2polar(a3, S0, st); }));
   }
   return LP_OK;
 }
@@ -576,10 +669,10 @@ int lp_adj(lp_handle* h, float* f, const float* R, int S0, void* stream) {
   AdjDev* A = h->adj;
   AdjIngestArgs ia{R, A->rbuf.p, A->filter ? A->H.p : nullptr, h->N, h->N0, h->Nproj, h->Nproj0, h->os,
                    h->N / 2 - h->cor, h->cubic, h->plan_filt};
-  CUDA_TRY(launch_adj_ingest(ia, S0, st));
+  CUDA_TRY(launch(h, K_ADJ_INGEST, st, [&] { return launch_adj_ingest(ia, S0, st); }));
   if (h->cubic) {
     ColPrefilterArgs ca{A->rbuf.p, h->Nproj, h->N};
-    CUDA_TRY(launch_col_prefilter(ca, S0, st));
+    CUDA_TRY(launch(h, K_COL_PREFILTER, st, [&] { return launch_col_prefilter(ca, S0, st); }));
   }
   for (int k = 0; k < 3; ++k) {
     if (A->chi[k] < A->clo[k]) {
@@ -588,16 +681,16 @@ int lp_adj(lp_handle* h, float* f, const float* R, int S0, void* stream) {
     }
     AdjPolar2LPArgs a1{A->rbuf.p, h->spec.p, A->ta[k].p, A->sx[k].p, A->woff[k].p, A->wpt[k].p, h->N, h->Nth,
                        h->Nrho, h->Nk, h->Nproj, h->cubic, A->clo[k], A->chi[k], h->plan_rho};
-    CUDA_TRY(launch_adj_polar2lp(a1, S0, st));
+    CUDA_TRY(launch(h, K_ADJ_POLAR2LP, st, [&] { return launch_adj_polar2lp(a1, S0, st); }));
     ThetaConvArgs a2{h->spec.p, A->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), A->clo[k],
                      A->chi[k], A->lo2, A->hi2, 0, h->plan_th};
-    CUDA_TRY(launch_theta_conv(a2, S0, st));
+    CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
     AdjLPColsArgs a3{h->spec.p, A->G[k].p, h->Nth, h->Nrho, h->Nk, A->lo2, A->hi2, A->W2, h->plan_rho};
-    CUDA_TRY(launch_adj_lpcols(a3, S0, st));
+    CUDA_TRY(launch(h, K_ADJ_LPCOLS, st, [&] { return launch_adj_lpcols(a3, S0, st); }));
   }
   AdjLP2CartArgs a4{A->G[0].p, A->G[1].p, A->G[2].p, A->c2lp[0].p, A->c2lp[1].p, A->c2lp[2].p, f,
                     h->N0, h->Nth, h->Nrho, A->lo2, A->W2, h->cubic, h->N0 * h->N0};
-  CUDA_TRY(launch_adj_lp2cart(a4, S0, st));
+  CUDA_TRY(launch(h, K_ADJ_LP2CART, st, [&] { return launch_adj_lp2cart(a4, S0, st); }));
   return LP_OK;
 }
 

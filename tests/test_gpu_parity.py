@@ -62,6 +62,8 @@ def test_reference_tables(torch_cuda, golden_dir, case):
     """Reference-made tables: GPU fwd/adj == oracle fwd/adj."""
     z = np.load(os.path.join(golden_dir, 'packed_%s.npz' % case))
     packed = [z[n] for n in NAMES]
+    packed[0] = packed[0].copy()
+    packed[0][6] = 3  # batch capacity (Nslices)
     tr = O.Transform.from_packed(*packed)
     h = _handle(packed)
     f, R = _inputs(tr.G, 3, 0)
@@ -76,15 +78,30 @@ def test_reference_tables(torch_cuda, golden_dir, case):
 
 @pytest.mark.parametrize("args", [(256, 384, 'cubic', 'ramp', 128), (96, 150, 'cubic', 'hamming', 45),
                                   (128, 64, 'linear', 'none', 64), (80, 120, 'cubic', 'parzen', 40.5)])
-def test_own_tables_vs_fp64_oracle(torch_cuda, args):
-    """This library's fp64 precompute; the oracle runs with unrounded float64 tables."""
+def test_own_tables(torch_cuda, args):
+    """This library's fp64 precompute, same float32 tables in the oracle, noise inputs."""
+    from lprec_gb300 import _lib
+    N0, Nproj, interp, filt, cor = args
+    packed = _lib.precompute(N0, Nproj, 2, cor, interp, filt, precision='fp64')
+    h = _handle(packed)
+    tr = O.Transform.from_packed(*packed)
+    f, R = _inputs(tr.G, 2, 1)
+    assert O.rel_l2(_fwd(torch_cuda, h, f), tr.fwd(f)) < TOL
+    assert O.rel_l2(_adj(torch_cuda, h, R), tr.adj(R)) < TOL
+
+
+@pytest.mark.parametrize("args", [(256, 384, 'cubic', 'shepp-logan', 128), (96, 150, 'cubic', 'ramp', 45)])
+def test_fp64_oracle_error_phantom(torch_cuda, args):
+    """Error against the float64 oracle (unrounded float64 tables) on phantom data."""
     from lprec_gb300 import _lib
     N0, Nproj, interp, filt, cor = args
     packed = _lib.precompute(N0, Nproj, 2, cor, interp, filt, precision='fp64')
     h = _handle(packed)
     tr = O.Transform(N0, Nproj, 2, filt, cor, interp, mode='fp64', rounded=False)
-    f, R = _inputs(tr.G, 2, 1)
-    assert O.rel_l2(_fwd(torch_cuda, h, f), tr.fwd(f)) < TOL
+    rng = np.random.default_rng(7)
+    f = np.stack([O.ellipse_phantom(N0, 10, rng) for _ in range(2)])
+    R = tr.fwd(f)
+    assert O.rel_l2(_fwd(torch_cuda, h, f), R) < TOL
     assert O.rel_l2(_adj(torch_cuda, h, R), tr.adj(R)) < TOL
 
 
