@@ -212,7 +212,8 @@ def per_kernel_bytes(h, S, prof):
 
 def run_ours(args):
     import torch
-    from lprec_gb300 import lpTransform, _lib
+    from lprec_gb300 import _lib
+    from lprec_gb300.lpTransform import lpTransform
     ws, rank, local = dist_env()
     dist = ws > 1
     if dist:

@@ -4,7 +4,7 @@ Drop-in for lprec's ``lpTransform`` (precompute / initcmem / fwdp / adjp) and
 the ``lpmethods`` solvers, backed by hand-written sm_103a CUDA kernels behind a
 C ABI (include/lprec_gb300.h).  PyTorch supplies device tensors and streams.
 """
-from .lpTransform import lpTransform  # noqa: F401
+from . import lpTransform  # noqa: F401  (module, as in lprec: lpTransform.lpTransform(...))
 from . import lpmethods  # noqa: F401
 
 __version__ = "0.1.0"

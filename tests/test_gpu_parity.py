@@ -107,7 +107,7 @@ def test_fp64_oracle_error_phantom(torch_cuda, args):
 
 def test_reference_pins_adj_many(torch_cuda, golden_dir):
     """tests/test_adj_many.py pins on the GPU: 8 slices scaled by (8-k)."""
-    from lprec_gb300 import lpTransform
+    from lprec_gb300.lpTransform import lpTransform
     torch = torch_cuda
     d = np.load(os.path.join(golden_dir, 'testdata.npz'))
     S = 8
