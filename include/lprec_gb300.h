@@ -114,6 +114,22 @@ int lp_device_bytes(const lp_handle* h, int64_t* bytes);
  *                     kind, total milliseconds and launches (arrays of
  *                     lp_kernel_count() entries); clears the record
  */
+/*
+ * Forward transform without device allocation (no counterpart in the
+ * reference).  Same result as lp_fwd, but its scratch -- the prefiltered
+ * image and the log-polar spectrum -- lives in one device array of
+ * LP_NOALLOC_SCRATCH_BYTES that the library declares at file scope, so the
+ * call allocates and frees nothing.  Meant for callers whose device memory is
+ * owned by another allocator or a fixed pool and that may not call cudaMalloc
+ * or cudaFree while processing.  Calls needing more scratch than the fixed
+ * size (lp_noalloc_scratch_bytes) fail with LP_ERR_UNSUPPORTED.  The first
+ * call on a device looks the array up (make it before any stream capture);
+ * all calls share the array, so calls that overlap on the GPU race.
+ */
+#define LP_NOALLOC_SCRATCH_BYTES (64LL * 1024 * 1024)
+int lp_fwd_noalloc(lp_handle* h, float* R, const float* f, int S0, void* stream);
+int lp_noalloc_scratch_bytes(const lp_handle* h, int S0, int64_t* bytes);
+
 long long lp_launch_count(void);
 int lp_kernel_count(void);
 const char* lp_kernel_name(int id);

@@ -695,3 +695,97 @@ int lp_adj(lp_handle* h, float* f, const float* R, int S0, void* stream) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Forward transform without device allocation.
+//
+// For callers that must not allocate or free device memory while they run:
+// applications whose device memory belongs to another allocator (a
+// framework's caching allocator or a fixed pool reserved at start-up), where
+// cudaMalloc can fail although the pool has room and where cudaMalloc and
+// cudaFree would synchronise the device in the middle of their pipeline.
+// lp_fwd_noalloc takes its scratch (the prefiltered image and the log-polar
+// spectrum) from one file-scope device array of LP_NOALLOC_SCRATCH_BYTES
+// instead of the handle's buffers; it calls no allocating routine.
+//
+// Every GPU that loads this library holds the array until the process exits.
+// Its device address is looked up with cudaGetSymbolAddress on the first call
+// on each device (with that device current); make that first call before any
+// stream capture.  All calls share the array and it keeps the last call's
+// contents: calls whose work overlaps on the GPU (other streams, other host
+// threads) race on it and must be serialised by the caller.  Nothing in it has
+// to start at zero: every scratch word this path reads was written earlier in
+// the same call.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[LP_NOALLOC_SCRATCH_BYTES];
+
+#define LP_NOALLOC_MAX_DEVICES 64
+static void* g_noalloc_ptr[LP_NOALLOC_MAX_DEVICES];
+static std::mutex g_noalloc_mu;
+
+static int noalloc_scratch(int device, void** out) {
+  if (device < 0 || device >= LP_NOALLOC_MAX_DEVICES)
+    return set_err(LP_ERR_UNSUPPORTED, "lp_fwd_noalloc: device id %d too large", device);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // device is current (DeviceGuard)
+    if (e != cudaSuccess)
+      return set_err(LP_ERR_CUDA, "lp_fwd_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    g_noalloc_ptr[device] = p;
+  }
+  *out = g_noalloc_ptr[device];
+  return LP_OK;
+}
+
+static inline size_t round256(size_t b) { return (b + 255) / 256 * 256; }
+
+extern "C" int lp_noalloc_scratch_bytes(const lp_handle* h, int S0, int64_t* bytes) {
+  if (!h || !bytes) return set_err(LP_ERR_ARG, "lp_noalloc_scratch_bytes: null pointer");
+  *bytes = (int64_t)(round256((size_t)S0 * h->N * h->N * sizeof(float)) +
+                     round256((size_t)S0 * h->Nk * h->Nth * sizeof(float2)));
+  return LP_OK;
+}
+
+extern "C" int lp_fwd_noalloc(lp_handle* h, float* R, const float* f, int S0, void* stream) {
+  if (!h) return set_err(LP_ERR_ARG, "lp_fwd_noalloc: null handle");
+  if (!h->fwd) return set_err(LP_ERR_STATE, "lp_fwd_noalloc: forward tables not initialised (lp_init_fwd)");
+  if (S0 < 0 || S0 > h->Nslices)
+    return set_err(LP_ERR_ARG, "lp_fwd_noalloc: S0=%d outside [0, %d]", S0, h->Nslices);
+  if (S0 == 0) return LP_OK;
+  if (!R || !f) return set_err(LP_ERR_ARG, "lp_fwd_noalloc: null data pointer");
+  const size_t fbytes = round256((size_t)S0 * h->N * h->N * sizeof(float));
+  const size_t sbytes = round256((size_t)S0 * h->Nk * h->Nth * sizeof(float2));
+  if (fbytes + sbytes > (size_t)LP_NOALLOC_SCRATCH_BYTES)
+    return set_err(LP_ERR_UNSUPPORTED,
+                   "lp_fwd_noalloc: %d slices of N=%d need %zu bytes of scratch, more than the fixed %lld; "
+                   "use fewer slices per call or lp_fwd",
+                   S0, h->N, fbytes + sbytes, (long long)LP_NOALLOC_SCRATCH_BYTES);
+  DeviceGuard g(h->device);
+  void* base = nullptr;
+  int rc = noalloc_scratch(h->device, &base);
+  if (rc != LP_OK) return rc;
+  float* fbuf = (float*)base;
+  float2* spec = (float2*)((unsigned char*)base + fbytes);
+  cudaStream_t st = (cudaStream_t)stream;
+  FwdDev* F = h->fwd;
+  FwdIngestArgs ia{f, fbuf, h->N, h->N0, h->N / 2 - h->N0 / 2, h->cubic};
+  CUDA_TRY(launch(h, K_FWD_INGEST, st, [&] { return launch_fwd_ingest(ia, S0, st); }));
+  if (h->cubic) {
+    ColPrefilterArgs ca{fbuf, h->N, h->N};
+    CUDA_TRY(launch(h, K_COL_PREFILTER, st, [&] { return launch_col_prefilter(ca, S0, st); }));
+  }
+  for (int k = 0; k < 3; ++k) {
+    FwdC2LPArgs a1{fbuf, spec, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, h->cubic, h->plan_rho};
+    CUDA_TRY(launch(h, K_FWD_C2LP, st, [&] { return launch_fwd_c2lp(a1, S0, st); }));
+    ThetaConvArgs a2{spec, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), 0, h->Nth - 1,
+                     F->lo, F->hi, 0, h->plan_th};
+    CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
+    FwdLP2PolarArgs a3{spec, R, F->thc.p, F->rhoc.p, F->rows[k].p, F->nrows[k], h->N, h->N0, h->Nth,
+                       h->Nrho, h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho};
+    CUDA_TRY(launch(h, K_FWD_LP2POLAR, st, [&] { return launch_fwd_lp2polar(a3, S0, st); }));
+  }
+  return LP_OK;
+}

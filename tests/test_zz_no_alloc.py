@@ -1,0 +1,67 @@
+"""lp_fwd_noalloc: the forward transform for callers that may not allocate device memory.
+
+Some callers run inside applications whose device memory belongs to another
+allocator (a framework's caching allocator, or a fixed pool reserved at
+start-up): they may not call cudaMalloc/cudaFree while processing.  The
+allocation-free entry point takes its scratch from a fixed device array inside
+the library.  This file is collected last so that a run stopping at the first
+failure has already run every other test.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_noalloc_matches_lp_fwd_twice(torch_cuda):
+    torch = torch_cuda
+    from lprec_gb300 import _lib
+    N, Nproj, S = 128, 192, 4
+    packed = _lib.precompute(N, Nproj, S, N / 2, 'cubic', 'ramp', precision='fp64')
+    h = _lib.Handle(packed[0], 0)
+    h.init_fwd(packed[1], packed[2])
+    h.init_adj(packed[3], packed[4])
+    stream = torch.cuda.current_stream().cuda_stream
+    rng = np.random.default_rng(11)
+    for call in range(2):  # two calls in a row, different inputs
+        f = torch.as_tensor(rng.random((S, N, N), dtype=np.float32)).cuda()
+        R_ref = torch.full((S, Nproj, N), float('nan'), device='cuda')
+        R_new = torch.full((S, Nproj, N), float('nan'), device='cuda')
+        h.fwd(R_ref.data_ptr(), f.data_ptr(), S, stream)
+        h.fwd_noalloc(R_new.data_ptr(), f.data_ptr(), S, stream)
+        torch.cuda.synchronize()
+        a, b = R_new.cpu().double().numpy(), R_ref.cpu().double().numpy()
+        assert np.all(np.isfinite(a)), call
+        assert _rel(a, b) <= TOL, (call, _rel(a, b))
+
+
+def test_noalloc_rejects_oversize(torch_cuda):
+    torch = torch_cuda
+    from lprec_gb300 import _lib
+    N, Nproj, S = 512, 768, 24
+    packed = _lib.precompute(N, Nproj, S, N / 2, 'cubic', 'none', precision='fp64')
+    h = _lib.Handle(packed[0], 0)
+    h.init_fwd(packed[1], packed[2])
+    limit = 64 * 1024 * 1024
+    assert h.noalloc_scratch_bytes(S) > limit
+    f = torch.zeros((S, N, N), device='cuda')
+    R = torch.zeros((S, Nproj, N), device='cuda')
+    with pytest.raises(_lib.LprecError) as ei:
+        h.fwd_noalloc(R.data_ptr(), f.data_ptr(), S, torch.cuda.current_stream().cuda_stream)
+    assert ei.value.code == _lib.LP_ERR_UNSUPPORTED
+    assert "scratch" in str(ei.value)
