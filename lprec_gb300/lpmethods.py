@@ -1,2 +1,188 @@
-def fbp(*a, **k):
-    raise NotImplementedError
+"""Reconstruction methods built on fwdp/adjp (drop-in for src/lprec/lpmethods.py).
+
+Every method has the reference's signature
+
+    method(lp, init_recon, tomo0, num_iter, reg_par, gpu) -> numpy.ndarray
+
+with `init_recon` [S, N, N] and `tomo0` [S, Nproj, N] host arrays (or CUDA
+tensors).  Vectors stay float32 on the GPU, as in the reference; inner
+products and norms are accumulated in float64 (the reference sums float32).
+Work is enqueued on the current torch stream of device `gpu`.
+"""
+import numpy as np
+
+C_TV = 0.35  # step of the primal-dual TV iterations (lpmethods.py:202)
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _dev(a, gpu):
+    torch = _torch()
+    if isinstance(a, torch.Tensor):
+        return a.to(device="cuda:%d" % gpu, dtype=torch.float32).contiguous().clone()
+    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float32)).to("cuda:%d" % gpu)
+
+
+def _dot(a, b):
+    """float64 inner product of two float32 device tensors."""
+    return (a.double() * b.double()).sum()
+
+
+def _dot_slices(a, b):
+    return (a.double() * b.double()).sum(dim=(1, 2))
+
+
+def _out(x):
+    return x.cpu().numpy()
+
+
+def fbp(lp, init_recon, tomo0, num_iter=0, reg_par=0, gpu=0):
+    """Filtered back-projection: one adjp (the filter is applied inside), lpmethods.py:7-19."""
+    torch = _torch()
+    with torch.cuda.device(gpu):
+        recon = _dev(init_recon, gpu)
+        tomo = _dev(tomo0, gpu)
+        lp.adjp(recon, tomo, gpu)
+        return _out(recon)
+
+
+def grad(lp, init_recon, tomo0, num_iter, reg_par, gpu=0):
+    """Gradient descent on 1/2||R f - g||^2; reg_par < 0 picks a Barzilai-Borwein step
+    per slice (lpmethods.py:22-59)."""
+    torch = _torch()
+    with torch.cuda.device(gpu):
+        recon = _dev(init_recon, gpu)
+        tomo = _dev(tomo0, gpu)
+        S = tomo.shape[0]
+        recon0 = recon.clone()
+        grad0 = torch.zeros_like(recon)
+        g = torch.zeros_like(tomo)
+        gr = torch.zeros_like(recon)
+        for i in range(num_iter):
+            lp.fwdp(g, recon, gpu)
+            g.sub_(tomo).mul_(2)
+            lp.adjp(gr, g, gpu)
+            if reg_par < 0:
+                if i == 0:
+                    lam = torch.full((S,), 1e-3, dtype=torch.float64, device=recon.device)
+                else:
+                    dg = gr - grad0
+                    lam = _dot_slices(recon - recon0, dg) / _dot_slices(dg, dg)
+            else:
+                lam = torch.full((S,), float(reg_par), dtype=torch.float64, device=recon.device)
+            recon0.copy_(recon)
+            grad0.copy_(gr)
+            recon.sub_(lam.float().view(S, 1, 1) * gr)
+        return _out(recon)
+
+
+def cg(lp, init_recon, tomo0, num_iter, reg_par=0, gpu=0):
+    """Conjugate gradients on the normal equations R*R f = R*g (lpmethods.py:62-97)."""
+    torch = _torch()
+    with torch.cuda.device(gpu):
+        recon = _dev(init_recon, gpu)
+        tomo = _dev(tomo0, gpu)
+        b = torch.zeros_like(recon)
+        f = torch.zeros_like(recon)
+        g = torch.zeros_like(tomo)
+        lp.adjp(b, tomo, gpu)
+        lp.fwdp(g, recon, gpu)
+        lp.adjp(f, g, gpu)
+        r = b - f
+        p = r.clone()
+        rsold = _dot(r, r)
+        for i in range(num_iter):
+            lp.fwdp(g, p, gpu)
+            lp.adjp(f, g, gpu)
+            alpha = (rsold / _dot(p, f)).float()
+            recon.add_(alpha * p)
+            r.sub_(alpha * f)
+            rsnew = _dot(r, r)
+            p.mul_((rsnew / rsold).float()).add_(r)
+            rsold = rsnew
+        return _out(recon)
+
+
+def em(lp, init_recon, tomo0, num_iter, reg_par, gpu=0):
+    """Expectation maximisation; reg_par keeps the division away from 0 (lpmethods.py:100-128)."""
+    torch = _torch()
+    with torch.cuda.device(gpu):
+        recon = _dev(init_recon, gpu)
+        tomo = _dev(tomo0, gpu)
+        xi = torch.zeros_like(recon)
+        upd = torch.zeros_like(recon)
+        g = torch.zeros_like(tomo)
+        lp.adjp(xi, torch.ones_like(tomo), gpu)
+        xi.add_(1e-5)
+        eps = float(np.float32(reg_par))
+        for i in range(num_iter):
+            lp.fwdp(g, recon, gpu)
+            lp.adjp(upd, tomo / (g + eps), gpu)
+            recon.mul_(upd / xi)
+        return _out(recon)
+
+
+def _tv_family(lp, init_recon, tomo0, num_iter, reg_par, gpu, prox):
+    """Chambolle-Pock iterations shared by tv, tve, tvl1 (lpmethods.py:131-288)."""
+    torch = _torch()
+    with torch.cuda.device(gpu):
+        recon = _dev(init_recon, gpu)
+        tomo = _dev(tomo0, gpu)
+        g = torch.zeros_like(tomo)
+        p = torch.zeros_like(recon)
+        recon0 = recon.clone()
+        prox0x = torch.zeros_like(recon)
+        prox0y = torch.zeros_like(recon)
+        div0 = torch.zeros_like(recon)
+        prox1 = torch.zeros_like(tomo)
+        lam = reg_par
+        c = C_TV
+        for i in range(num_iter):
+            prox0x[:, :, :-1] += c * (recon[:, :, 1:] - recon[:, :, :-1])
+            prox0y[:, :-1, :] += c * (recon[:, 1:, :] - recon[:, :-1, :])
+            nprox = torch.clamp(torch.sqrt(prox0x * prox0x + prox0y * prox0y) / lam, min=1)
+            prox0x = prox0x / nprox
+            prox0y = prox0y / nprox
+            lp.fwdp(g, recon, gpu)
+            prox1 = prox(prox1, g, tomo, c)
+            recon = recon0
+            div0[:, :, 1:] = prox0x[:, :, 1:] - prox0x[:, :, :-1]
+            div0[:, :, 0] = prox0x[:, :, 0]
+            div0[:, 1:, :] += prox0y[:, 1:, :] - prox0y[:, :-1, :]
+            div0[:, 0, :] += prox0y[:, 0, :]
+            lp.adjp(p, prox1, gpu)
+            recon0 = recon0 - c * p + c * div0
+            recon = 2 * recon0 - recon
+        return _out(recon)
+
+
+def tv(lp, init_recon, tomo0, num_iter, reg_par, gpu=0):
+    """1/2||R f - g||^2 + reg_par TV(f) (lpmethods.py:131-180)."""
+    return _tv_family(lp, init_recon, tomo0, num_iter, reg_par, gpu,
+                      lambda p1, g, tomo, c: (p1 + c * g - c * tomo) / (1 + c))
+
+
+def tve(lp, init_recon, tomo0, num_iter, reg_par, gpu=0):
+    """sum(R f - g log R f) + reg_par TV(f) (lpmethods.py:182-230)."""
+    torch = _torch()
+
+    def prox(p1, g, tomo, c):
+        t = p1 + c * g - 1
+        tmp = 0.5 * (t + torch.sqrt(t * t + 4 * c * tomo))
+        tmp = torch.clamp(tmp, min=0)
+        return p1 + c * g - tmp
+    return _tv_family(lp, init_recon, tomo0, num_iter, reg_par, gpu, prox)
+
+
+def tvl1(lp, init_recon, tomo0, num_iter, reg_par, gpu=0):
+    """||R f - g||_1 + reg_par TV(f) (lpmethods.py:232-288)."""
+    torch = _torch()
+
+    def prox(p1, g, tomo, c):
+        tmp = p1 + c * g - c * tomo
+        tmp2 = torch.clamp(tmp.abs() - 1, min=0)
+        return tmp - tmp2 * torch.sign(tmp)
+    return _tv_family(lp, init_recon, tomo0, num_iter, reg_par, gpu, prox)
