@@ -223,6 +223,8 @@ def run_ours(args):
     torch.cuda.set_device(dev)
     W = WORKLOAD
     N, Nproj, S = W["N"], W["Nproj"], W["S"]
+    if args.slices:
+        S = args.slices
     if args.small:
         N, Nproj, S = 256, 384, 8
     lp = lpTransform(N, Nproj, S, W["filter"], N / 2, W["interp"])
@@ -375,6 +377,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="N=256 smoke-size workload")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--slices", type=int, default=0, help="batch size (default 128); for profiling runs")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

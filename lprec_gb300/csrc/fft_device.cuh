@@ -1,14 +1,16 @@
 // Shared-memory complex FFT used by the log-polar convolution and the FBP filter.
 //
-// Stockham autosort formulation: every stage reads the whole signal with unit
-// stride (conflict-free), applies one radix-r butterfly per group of r points,
-// and writes in sorted order into the other buffer.  Radices 2, 3, 4, 5, 7 and
-// 8 have hand-written butterflies; any other prime factor uses a direct DFT.
-// Lengths are N = 16*m (log-polar grids) or 4N, 2N: any positive length works.
+// Stockham autosort formulation, ping-pong between two shared buffers.  Data is
+// planar (separate re / im float arrays) with one pad word after every 32, so
+// both the unit-stride reads and the stride-R writes of a stage hit distinct
+// banks.  Twiddles come from a table W[t] = exp(-2*pi*i*t/L) computed on the
+// host in float64.  Radix 16, 8, 4, 2, 3, 5 and 7 have hand-written
+// butterflies; other prime factors use a direct DFT from the same table, so
+// any length works (N = 16*m log-polar grids allow any m).
 //
-// Sign convention: dir = -1 is the forward transform exp(-2*pi*i*jk/L), dir =
-// +1 the unnormalised inverse, as cuFFT defines them (reference call sites
-// src/cuda/lpRgpu.cu:270,277,314,321,353,368).
+// Sign convention: DIR = -1 is the forward transform exp(-2*pi*i*jk/L),
+// DIR = +1 the unnormalised inverse, as cuFFT defines them (reference call
+// sites src/cuda/lpRgpu.cu:270,277,314,321,353,368).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -21,14 +23,17 @@ struct FFTPlan {
   int L;
   int nst;
   int radix[LP_FFT_MAX_STAGES];
+  const float2* tw;  // device table of L twiddles exp(-2*pi*i*t/L)
 };
 
 // Factor L into stages, largest fast radix first.
-inline FFTPlan make_fft_plan(int L) {
+inline FFTPlan make_fft_plan(int L, const float2* tw) {
   FFTPlan p;
   p.L = L;
   p.nst = 0;
+  p.tw = tw;
   int n = L;
+  while (n % 16 == 0) { p.radix[p.nst++] = 16; n /= 16; }
   while (n % 8 == 0) { p.radix[p.nst++] = 8; n /= 8; }
   while (n % 4 == 0) { p.radix[p.nst++] = 4; n /= 4; }
   while (n % 2 == 0) { p.radix[p.nst++] = 2; n /= 2; }
@@ -40,47 +45,79 @@ inline FFTPlan make_fft_plan(int L) {
   return p;
 }
 
+// padded planar index
+__device__ __forceinline__ int fpad(int p) { return p + (p >> 5); }
+// floats needed for one planar plane of length L
+__host__ __device__ inline int fft_plane_floats(int L) { return L + (L >> 5) + 1; }
+
+// A complex array in shared memory: two padded planes.
+struct CBuf {
+  float* re;
+  float* im;
+  __device__ __forceinline__ float2 get(int p) const {
+    const int q = fpad(p);
+    return make_float2(re[q], im[q]);
+  }
+  __device__ __forceinline__ void set(int p, float2 v) const {
+    const int q = fpad(p);
+    re[q] = v.x;
+    im[q] = v.y;
+  }
+  __device__ __forceinline__ CBuf offset(int n) const { return CBuf{re + n, im + n}; }
+};
+
+// floats of one complex buffer holding `nfft` signals of length L; signal f
+// starts fft_plane_floats(L) * f floats into each plane (the `stride`
+// argument of fft_block), so the padding of one signal never overlaps the next
+__host__ __device__ inline int fft_buf_floats(int L, int nfft) { return 2 * nfft * fft_plane_floats(L); }
+
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
-// multiply by dir*i
+// multiply by DIR*i
 template <int DIR>
 __device__ __forceinline__ float2 mul_i(float2 a) {
   return DIR < 0 ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);
 }
+// multiply by exp(DIR*i*pi*m/8) given c = cos(pi*m/8), s = sin(pi*m/8)
+template <int DIR>
+__device__ __forceinline__ float2 rot(float2 a, float c, float s) {
+  return make_float2(a.x * c - DIR * a.y * s, a.y * c + DIR * a.x * s);
+}
 
 template <int DIR>
 __device__ __forceinline__ void bfly2(float2* v) {
-  float2 a = v[0], b = v[1];
+  const float2 a = v[0], b = v[1];
   v[0] = cadd(a, b);
   v[1] = csub(a, b);
 }
 
 template <int DIR>
 __device__ __forceinline__ void bfly4(float2* v) {
-  float2 a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
-  float2 b0 = cadd(v[1], v[3]), b1 = mul_i<DIR>(csub(v[1], v[3]));
+  const float2 a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
+  const float2 b0 = cadd(v[1], v[3]), b1 = mul_i<DIR>(csub(v[1], v[3]));
   v[0] = cadd(a0, b0);
   v[2] = csub(a0, b0);
   v[1] = cadd(a1, b1);
   v[3] = csub(a1, b1);
 }
 
+#define LP_C8 0.92387953251128675613f  // cos(pi/8)
+#define LP_S8 0.38268343236508977173f  // sin(pi/8)
+#define LP_R2 0.70710678118654752440f  // cos(pi/4)
+
 template <int DIR>
 __device__ __forceinline__ void bfly8(float2* v) {
-  const float r = 0.70710678118654752440f;
   float2 e[4] = {v[0], v[2], v[4], v[6]};
   float2 o[4] = {v[1], v[3], v[5], v[7]};
   bfly4<DIR>(e);
   bfly4<DIR>(o);
-  // twiddles w8^k, k = 0..3, w8 = exp(dir*i*pi/4)
-  float2 t1 = make_float2(r * (o[1].x - DIR * o[1].y), r * (o[1].y + DIR * o[1].x));
-  float2 t2 = mul_i<DIR>(o[2]);
-  float2 t3 = make_float2(r * (-o[3].x - DIR * o[3].y), r * (-o[3].y + DIR * o[3].x));
+  const float2 t1 = rot<DIR>(o[1], LP_R2, LP_R2);
+  const float2 t2 = mul_i<DIR>(o[2]);
+  const float2 t3 = rot<DIR>(o[3], -LP_R2, LP_R2);
   v[0] = cadd(e[0], o[0]);
   v[4] = csub(e[0], o[0]);
   v[1] = cadd(e[1], t1);
@@ -91,13 +128,43 @@ __device__ __forceinline__ void bfly8(float2* v) {
   v[7] = csub(e[3], t3);
 }
 
+// 16 = 4 x 4: X[c + 4d] = sum_b w4^(bd) w16^(bc) sum_a v[b + 4a] w4^(ac)
+template <int DIR>
+__device__ __forceinline__ void bfly16(float2* v) {
+  float2 u[16];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    float2 t[4] = {v[b], v[b + 4], v[b + 8], v[b + 12]};
+    bfly4<DIR>(t);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) u[4 * b + c] = t[c];
+  }
+  // twiddles w16^(b*c): exponents 0,1,2,3 / 2,4,6 / 3,6,9
+  u[5] = rot<DIR>(u[5], LP_C8, LP_S8);
+  u[6] = rot<DIR>(u[6], LP_R2, LP_R2);
+  u[7] = rot<DIR>(u[7], LP_S8, LP_C8);
+  u[9] = rot<DIR>(u[9], LP_R2, LP_R2);
+  u[10] = mul_i<DIR>(u[10]);
+  u[11] = rot<DIR>(u[11], -LP_R2, LP_R2);
+  u[13] = rot<DIR>(u[13], LP_S8, LP_C8);
+  u[14] = rot<DIR>(u[14], -LP_R2, LP_R2);
+  u[15] = rot<DIR>(u[15], -LP_C8, -LP_S8);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    float2 t[4] = {u[c], u[4 + c], u[8 + c], u[12 + c]};
+    bfly4<DIR>(t);
+#pragma unroll
+    for (int d = 0; d < 4; ++d) v[c + 4 * d] = t[d];
+  }
+}
+
 template <int DIR>
 __device__ __forceinline__ void bfly3(float2* v) {
   const float c = -0.5f, s = DIR * 0.86602540378443864676f;
-  float2 t = cadd(v[1], v[2]);
-  float2 d = csub(v[1], v[2]);
-  float2 m = make_float2(v[0].x + c * t.x, v[0].y + c * t.y);
-  float2 r = make_float2(-s * d.y, s * d.x);
+  const float2 t = cadd(v[1], v[2]);
+  const float2 d = csub(v[1], v[2]);
+  const float2 m = make_float2(v[0].x + c * t.x, v[0].y + c * t.y);
+  const float2 r = make_float2(-s * d.y, s * d.x);
   v[0] = cadd(v[0], t);
   v[1] = cadd(m, r);
   v[2] = csub(m, r);
@@ -107,12 +174,12 @@ template <int DIR>
 __device__ __forceinline__ void bfly5(float2* v) {
   const float c1 = 0.30901699437494742410f, c2 = -0.80901699437494742410f;
   const float s1 = DIR * 0.95105651629515357212f, s2 = DIR * 0.58778525229247312917f;
-  float2 t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
-  float2 d1 = csub(v[1], v[4]), d2 = csub(v[2], v[3]);
-  float2 m1 = make_float2(v[0].x + c1 * t1.x + c2 * t2.x, v[0].y + c1 * t1.y + c2 * t2.y);
-  float2 m2 = make_float2(v[0].x + c2 * t1.x + c1 * t2.x, v[0].y + c2 * t1.y + c1 * t2.y);
-  float2 r1 = make_float2(-(s1 * d1.y + s2 * d2.y), s1 * d1.x + s2 * d2.x);
-  float2 r2 = make_float2(-(s2 * d1.y - s1 * d2.y), s2 * d1.x - s1 * d2.x);
+  const float2 t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+  const float2 d1 = csub(v[1], v[4]), d2 = csub(v[2], v[3]);
+  const float2 m1 = make_float2(v[0].x + c1 * t1.x + c2 * t2.x, v[0].y + c1 * t1.y + c2 * t2.y);
+  const float2 m2 = make_float2(v[0].x + c2 * t1.x + c1 * t2.x, v[0].y + c2 * t1.y + c1 * t2.y);
+  const float2 r1 = make_float2(-(s1 * d1.y + s2 * d2.y), s1 * d1.x + s2 * d2.x);
+  const float2 r2 = make_float2(-(s2 * d1.y - s1 * d2.y), s2 * d1.x - s1 * d2.x);
   v[0] = cadd(v[0], cadd(t1, t2));
   v[1] = cadd(m1, r1);
   v[4] = csub(m1, r1);
@@ -120,116 +187,107 @@ __device__ __forceinline__ void bfly5(float2* v) {
   v[3] = csub(m2, r2);
 }
 
-// Generic odd radix (7 and larger primes): direct DFT, O(r^2) per butterfly.
-template <int DIR, int R>
-__device__ __forceinline__ void bfly_direct(float2* v) {
-  float2 out[R];
-#pragma unroll
-  for (int k = 0; k < R; ++k) {
-    float2 acc = v[0];
-#pragma unroll
-    for (int j = 1; j < R; ++j) {
-      float sn, cs;
-      sincospif((float)(2 * DIR * ((j * k) % R)) / (float)R, &sn, &cs);
-      acc.x += v[j].x * cs - v[j].y * sn;
-      acc.y += v[j].x * sn + v[j].y * cs;
-    }
-    out[k] = acc;
-  }
-#pragma unroll
-  for (int k = 0; k < R; ++k) v[k] = out[k];
+// twiddle exp(DIR*2*pi*i*t/L) from the table
+template <int DIR>
+__device__ __forceinline__ float2 twid(const float2* __restrict__ tw, int t) {
+  float2 w = __ldg(tw + t);
+  if (DIR > 0) w.y = -w.y;
+  return w;
 }
 
-// One Stockham stage with a compile-time radix over `nfft` signals of length L
-// stored at `stride` apart.  Ns = product of the radices already applied.
+// Direct DFT of radix R with roots from the table (L/R * q steps).
+template <int DIR>
+__device__ __forceinline__ void bfly_direct(float2* v, int R, const float2* __restrict__ tw, int LoverR) {
+  float2 out[7];
+  for (int q = 0; q < R; ++q) {
+    float2 acc = v[0];
+    for (int i = 1; i < R; ++i) acc = cadd(acc, cmul(v[i], twid<DIR>(tw, ((i * q) % R) * LoverR)));
+    out[q] = acc;
+  }
+  for (int q = 0; q < R; ++q) v[q] = out[q];
+}
+
+// One Stockham stage with compile-time radix R over `nfft` signals of length L
+// whose planes start `stride` floats apart.  Ns = product of the radices already applied.
 template <int DIR, int R>
-__device__ __forceinline__ void fft_stage(const float2* __restrict__ in, float2* __restrict__ out, int L,
+__device__ __forceinline__ void fft_stage(const CBuf in, const CBuf out, const float2* __restrict__ tw, int L,
                                           int Ns, int nfft, int stride) {
   const int Lr = L / R;
   const int total = nfft * Lr;
+  const int tstep = L / (Ns * R);
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
     const int f = t / Lr;
     const int j = t - f * Lr;
-    const float2* src = in + f * stride;
-    float2* dst = out + f * stride;
     const int k = j % Ns;
+    const CBuf src = in.offset(f * stride);
+    const CBuf dst = out.offset(f * stride);
     float2 v[R];
 #pragma unroll
-    for (int i = 0; i < R; ++i) v[i] = src[j + i * Lr];
+    for (int i = 0; i < R; ++i) v[i] = src.get(j + i * Lr);
     if (Ns > 1) {
-      // twiddle exp(dir*2*pi*i*i*k/(Ns*R))
-      const float base = (float)(2 * DIR) * (float)k / (float)(Ns * R);
 #pragma unroll
-      for (int i = 1; i < R; ++i) {
-        float sn, cs;
-        sincospif(base * (float)i, &sn, &cs);
-        v[i] = cmul(v[i], make_float2(cs, sn));
-      }
+      for (int i = 1; i < R; ++i) v[i] = cmul(v[i], twid<DIR>(tw, i * k * tstep));
     }
     if (R == 2) bfly2<DIR>(v);
-    else if (R == 3) bfly3<DIR>(v);
     else if (R == 4) bfly4<DIR>(v);
-    else if (R == 5) bfly5<DIR>(v);
     else if (R == 8) bfly8<DIR>(v);
-    else bfly_direct<DIR, R>(v);
-    const int base_o = (j - k) * R + k;
+    else if (R == 16) bfly16<DIR>(v);
+    else if (R == 3) bfly3<DIR>(v);
+    else if (R == 5) bfly5<DIR>(v);
+    else if (R == 7) bfly_direct<DIR>(v, 7, tw, L / R);
+    const int base = (j - k) * R + k;
 #pragma unroll
-    for (int i = 0; i < R; ++i) dst[base_o + i * Ns] = v[i];
+    for (int i = 0; i < R; ++i) dst.set(base + i * Ns, v[i]);
   }
 }
 
-// Generic prime radix not known at compile time (rare: N with a prime factor > 7).
+// Any prime radix > 7: direct DFT per butterfly.
 template <int DIR>
-__device__ void fft_stage_dyn(const float2* __restrict__ in, float2* __restrict__ out, int L, int Ns, int R,
+__device__ void fft_stage_dyn(const CBuf in, const CBuf out, const float2* __restrict__ tw, int L, int Ns, int R,
                               int nfft, int stride) {
   const int Lr = L / R;
   const int total = nfft * Lr;
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
     const int f = t / Lr;
     const int j = t - f * Lr;
-    const float2* src = in + f * stride;
-    float2* dst = out + f * stride;
     const int k = j % Ns;
-    const int base_o = (j - k) * R + k;
+    const CBuf src = in.offset(f * stride);
+    const CBuf dst = out.offset(f * stride);
+    const int base = (j - k) * R + k;
     for (int q = 0; q < R; ++q) {
       float2 acc = make_float2(0.f, 0.f);
       for (int i = 0; i < R; ++i) {
-        // total phase: twiddle i*k/(Ns*R) + butterfly i*q/R
-        const long long num = (long long)i * k + (long long)((i * q) % R) * Ns;
-        const long long den = (long long)Ns * R;
-        float sn, cs;
-        sincospif((float)(2 * DIR) * (float)(num % den) / (float)den, &sn, &cs);
-        const float2 x = src[j + i * Lr];
-        acc.x += x.x * cs - x.y * sn;
-        acc.y += x.x * sn + x.y * cs;
+        // twiddle i*k/(Ns*R) and butterfly root i*q/R in units of 1/L
+        const long long e = (long long)i * k * (L / (Ns * R)) + (long long)((i * q) % R) * Lr;
+        acc = cadd(acc, cmul(src.get(j + i * Lr), twid<DIR>(tw, (int)(e % L))));
       }
-      dst[base_o + q * Ns] = acc;
+      dst.set(base + q * Ns, acc);
     }
   }
 }
 
-// Run the whole transform; data starts in `a`, `b` is scratch of the same
-// size.  Returns the buffer that holds the result (a or b).  All threads of
-// the block must call it; it ends with a __syncthreads().
+// Run the transform on `nfft` signals; data starts in `a`, `b` is scratch of
+// the same shape.  Returns the buffer holding the result.  All threads of the
+// block must call it; it ends with a __syncthreads().
 template <int DIR>
-__device__ float2* fft_block(float2* a, float2* b, const FFTPlan& p, int nfft, int stride) {
+__device__ CBuf fft_block(CBuf a, CBuf b, const FFTPlan& p, int nfft, int stride) {
   int Ns = 1;
-  float2* in = a;
-  float2* out = b;
+  CBuf in = a, out = b;
   for (int s = 0; s < p.nst; ++s) {
     const int R = p.radix[s];
     switch (R) {
-      case 2: fft_stage<DIR, 2>(in, out, p.L, Ns, nfft, stride); break;
-      case 3: fft_stage<DIR, 3>(in, out, p.L, Ns, nfft, stride); break;
-      case 4: fft_stage<DIR, 4>(in, out, p.L, Ns, nfft, stride); break;
-      case 5: fft_stage<DIR, 5>(in, out, p.L, Ns, nfft, stride); break;
-      case 7: fft_stage<DIR, 7>(in, out, p.L, Ns, nfft, stride); break;
-      case 8: fft_stage<DIR, 8>(in, out, p.L, Ns, nfft, stride); break;
-      default: fft_stage_dyn<DIR>(in, out, p.L, Ns, R, nfft, stride); break;
+      case 16: fft_stage<DIR, 16>(in, out, p.tw, p.L, Ns, nfft, stride); break;
+      case 8: fft_stage<DIR, 8>(in, out, p.tw, p.L, Ns, nfft, stride); break;
+      case 4: fft_stage<DIR, 4>(in, out, p.tw, p.L, Ns, nfft, stride); break;
+      case 2: fft_stage<DIR, 2>(in, out, p.tw, p.L, Ns, nfft, stride); break;
+      case 3: fft_stage<DIR, 3>(in, out, p.tw, p.L, Ns, nfft, stride); break;
+      case 5: fft_stage<DIR, 5>(in, out, p.tw, p.L, Ns, nfft, stride); break;
+      case 7: fft_stage<DIR, 7>(in, out, p.tw, p.L, Ns, nfft, stride); break;
+      default: fft_stage_dyn<DIR>(in, out, p.tw, p.L, Ns, R, nfft, stride); break;
     }
     __syncthreads();
     Ns *= R;
-    float2* t = in;
+    const CBuf t = in;
     in = out;
     out = t;
   }

@@ -1,0 +1,119 @@
+// Register-resident complex FFT for power-of-two lengths 256..8192.
+//
+// Each thread of a signal's T = L/16 threads holds 16 elements in registers,
+// thread t holding x[t + i*T], i = 0..15.  Every stage is a Stockham step:
+// the thread's elements form 16/R butterflies of radix R (elements m, m+NB,
+// m+2NB, ... with NB = 16/R), twiddled and transformed in registers, then
+// written to their sorted positions in one shared buffer; the next stage
+// reads the same natural positions t + i*T back.  The schedule is radix 16
+// followed by at most one radix 2/4/8 stage, so L = 4096 takes three stages.
+// Index arithmetic is resolved at compile time.  Shared positions carry one
+// pad element per 16 (`spad`), which keeps the radix-16 scatter of the first
+// stage and the unit-stride reads conflict-free for 64-bit accesses.
+//
+// Twiddles exp(DIR*2*pi*i*a*k/(Ns*R)) are built per butterfly from two
+// sincospif() calls (powers 1 and 4) and short products (depth <= 3), so no
+// table is gathered.  On return the transform is in shared memory in
+// natural order at spad(k); registers are free.
+//
+// DIR = -1 forward exp(-2*pi*i*jk/L), DIR = +1 unnormalised inverse.
+#pragma once
+#include "fft_device.cuh"
+
+namespace lpgb {
+
+__device__ __forceinline__ int spad(int p) { return p + (p >> 4); }
+// float2 slots of one padded signal buffer
+__host__ __device__ constexpr int reg_fft_slots(int L) { return L + (L >> 4); }
+
+template <int R, int DIR>
+__device__ __forceinline__ void reg_bfly(float2* x) {
+  if constexpr (R == 16) bfly16<DIR>(x);
+  else if constexpr (R == 8) bfly8<DIR>(x);
+  else if constexpr (R == 4) bfly4<DIR>(x);
+  else bfly2<DIR>(x);
+}
+
+// twiddle powers w^i, i < R, of w = exp(DIR*2*pi*i*f) with f = k/(Ns*R)
+template <int R, int DIR>
+__device__ __forceinline__ void twiddle_powers(float f, float2* w) {
+  float s1, c1;
+  sincospif(2.0f * f, &s1, &c1);
+  const float2 w1 = make_float2(c1, DIR * s1);
+  w[0] = make_float2(1.f, 0.f);
+  w[1] = w1;
+  if constexpr (R >= 4) {
+    w[2] = cmul(w1, w1);
+    w[3] = cmul(w[2], w1);
+  }
+  if constexpr (R >= 8) {
+    float s4, c4;
+    sincospif(8.0f * f, &s4, &c4);
+    const float2 w4 = make_float2(c4, DIR * s4);
+    w[4] = w4;
+    w[5] = cmul(w4, w1);
+    w[6] = cmul(w4, w[2]);
+    w[7] = cmul(w4, w[3]);
+    if constexpr (R == 16) {
+      const float2 w8 = cmul(w4, w4);
+      const float2 w12 = cmul(w8, w4);
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        w[8 + a] = a == 0 ? w8 : cmul(w8, w[a]);
+        w[12 + a] = a == 0 ? w12 : cmul(w12, w[a]);
+      }
+    }
+  }
+}
+
+template <int L, int DIR, int R, int NS, bool LAST>
+__device__ __forceinline__ void reg_stage(float2 (&v)[16], float2* sm, int t) {
+  constexpr int T = L / 16;
+  constexpr int NB = 16 / R;
+#pragma unroll
+  for (int m = 0; m < NB; ++m) {
+    const int jp = t + m * T;
+    const int k = jp & (NS - 1);
+    float2 x[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) x[i] = v[m + i * NB];
+    if constexpr (NS > 1) {
+      float2 w[R];
+      twiddle_powers<R, DIR>((float)k * (1.0f / (float)(NS * R)), w);
+#pragma unroll
+      for (int i = 1; i < R; ++i) x[i] = cmul(x[i], w[i]);
+    }
+    reg_bfly<R, DIR>(x);
+    const int base = (jp - k) * R + k;
+#pragma unroll
+    for (int i = 0; i < R; ++i) sm[spad(base + i * NS)] = x[i];
+  }
+  __syncthreads();
+  if constexpr (!LAST) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = sm[spad(t + i * T)];
+    __syncthreads();
+  }
+}
+
+// Transform one signal.  v: this thread's 16 elements x[t + i*T]; sm: the
+// signal's shared buffer of reg_fft_slots(L) float2.  All threads of the
+// block must call it (it synchronises the block).
+template <int L, int DIR>
+__device__ __forceinline__ void reg_fft(float2 (&v)[16], float2* sm, int t) {
+  static_assert(L == 256 || L == 512 || L == 1024 || L == 2048 || L == 4096 || L == 8192, "size");
+  reg_stage<L, DIR, 16, 1, false>(v, sm, t);
+  if constexpr (L == 256) {
+    reg_stage<L, DIR, 16, 16, true>(v, sm, t);
+  } else if constexpr (L == 8192) {
+    reg_stage<L, DIR, 16, 16, false>(v, sm, t);
+    reg_stage<L, DIR, 16, 256, false>(v, sm, t);
+    reg_stage<L, DIR, 2, 4096, true>(v, sm, t);
+  } else {
+    reg_stage<L, DIR, 16, 16, false>(v, sm, t);
+    constexpr int R3 = L / 256;
+    reg_stage<L, DIR, R3, 256, true>(v, sm, t);
+  }
+}
+
+}  // namespace lpgb

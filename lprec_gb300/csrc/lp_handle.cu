@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/lprec_gb300.h"
+#include "host_fft.h"
 #include "lp_kernels.cuh"
 
 using namespace lpgb;
@@ -146,6 +147,8 @@ struct lp_handle {
   std::vector<float> erho_h;
   DevBuf<float> erho;
   DevBuf<float2> spec;     // [Nslices][Nk][Nth]
+  DevBuf<float2> tw_rho;   // FFT twiddles for length Nrho (also the FBP filter's 2N)
+  DevBuf<float2> tw_th;    // FFT twiddles for length Nth
   FwdDev* fwd = nullptr;
   AdjDev* adj = nullptr;
   FFTPlan plan_rho, plan_th, plan_filt;
@@ -217,6 +220,42 @@ static std::vector<float2> extend_kernel(const float* v, int Nrho, int Nth) {
 }
 
 static bool finite_coord(float v, float lim) { return isfinite(v) && fabsf(v) < lim; }
+
+// W[t] = exp(-2 pi i t / L), evaluated in float64
+static std::vector<float2> twiddles(int L) {
+  std::vector<float2> w(L);
+  for (int t = 0; t < L; ++t) {
+    const double a = -2.0 * lpgb_host::kPi * (double)t / (double)L;
+    w[t] = make_float2((float)cos(a), (float)sin(a));
+  }
+  return w;
+}
+
+// The FBP filter of applyFilter (src/cuda/lpRgpu.cu:333-382) is a circular
+// convolution of length 4N of a zero-padded row with h = IFFT(filter shifted
+// by 2N).  Outputs and inputs both lie in one N-sample window, so only
+// h[d] for |d| < N matters and a circular convolution of length 2N with the
+// folded kernel gives the same result.  Returns its spectrum divided by 2N
+// (real: the filter is symmetric), or an empty vector if it is not symmetric.
+static std::vector<float> fbp_kernel_2n(const float* filt, int N) {
+  using lpgb_host::cd;
+  const int M = 4 * N, L2 = 2 * N;
+  std::vector<cd> H(M), tmp(M);
+  for (int k = 0; k < M; ++k) H[k] = cd((double)filt[(k + 2 * N) % M], 0.0);
+  for (int k = 1; k < M; ++k)
+    if (H[k].real() != H[M - k].real()) return {};
+  // h = IFFT(H) / M; H is real and symmetric, so IFFT = FFT
+  lpgb_host::HostFFT fM(M);
+  fM.run(H.data(), tmp.data());
+  std::vector<cd> h2(L2, cd(0, 0)), t2(L2);
+  for (int d = 0; d < N; ++d) h2[d] = cd(H[d].real() / M, 0.0);
+  for (int e = 1; e < N; ++e) h2[L2 - e] = cd(H[M - e].real() / M, 0.0);
+  lpgb_host::HostFFT f2(L2);
+  f2.run(h2.data(), t2.data());
+  std::vector<float> out(L2);
+  for (int k = 0; k < L2; ++k) out[k] = (float)(h2[k].real() / L2);
+  return out;
+}
 
 // taps of one axis for coordinate t: first index and count
 static inline int first_tap(float t, int cubic) { return (int)floorf(t) - (cubic ? 1 : 0); }
@@ -320,15 +359,19 @@ int lp_create(const float* glpars, int64_t n, int device, lp_handle** out) {
   lp_handle* h = new lp_handle(h0);
   h->erho_h.resize(h->Nrho);
   for (int r = 0; r < h->Nrho; ++r) h->erho_h[r] = glpars[10 + (size_t)r * h->Nth];
-  h->plan_rho = make_fft_plan(h->Nrho);
-  h->plan_th = make_fft_plan(h->Nth);
-  h->plan_filt = make_fft_plan(4 * h->N);
   DeviceGuard g(device);
   cudaError_t e = configure_kernels(h->N);
   if (e == cudaSuccess) e = dev_upload(h->erho, h->erho_h);
+  if (e == cudaSuccess) e = dev_upload(h->tw_rho, twiddles(h->Nrho));
+  if (e == cudaSuccess) e = dev_upload(h->tw_th, twiddles(h->Nth));
   if (e == cudaSuccess) e = dev_alloc(h->spec, (size_t)h->Nslices * h->Nk * h->Nth);
+  h->plan_rho = make_fft_plan(h->Nrho, h->tw_rho.p);
+  h->plan_th = make_fft_plan(h->Nth, h->tw_th.p);
+  h->plan_filt = h->plan_rho;
   if (e != cudaSuccess) {
     h->erho.free_();
+    h->tw_rho.free_();
+    h->tw_th.free_();
     h->spec.free_();
     delete h;
     return set_err(e == cudaErrorMemoryAllocation ? LP_ERR_OOM : LP_ERR_CUDA, "lp_create: %s",
@@ -575,9 +618,8 @@ int lp_init_adj(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
   A->W2 = hi2 - lo2 + 1;
   cudaError_t e = dev_upload(A->fz, extend_kernel(fzv, Nrho, Nth));
   if (e == cudaSuccess && flag == 1) {
-    if (h->N > 3200) return fail(LP_ERR_UNSUPPORTED, "FBP filter supports N <= 3200");
-    std::vector<float> Hh(4 * (size_t)N);
-    for (int kk = 0; kk < 4 * N; ++kk) Hh[kk] = filt[(kk + 2 * N) % (4 * N)];
+    std::vector<float> Hh = fbp_kernel_2n(filt, N);
+    if (Hh.empty()) return fail(LP_ERR_UNSUPPORTED, "FBP filter is not symmetric");
     e = dev_upload(A->H, Hh);
     A->filter = true;
   }
@@ -596,6 +638,8 @@ int lp_destroy(lp_handle* h) {
   free_adj(h->adj);
   h->erho.free_();
   h->spec.free_();
+  h->tw_rho.free_();
+  h->tw_th.free_();
   for (const ProfRec& r : h->prof) {
     cudaEventDestroy(r.a);
     cudaEventDestroy(r.b);
@@ -614,7 +658,7 @@ int lp_get_geometry(const lp_handle* h, int32_t out[10]) {
 
 int lp_device_bytes(const lp_handle* h, int64_t* bytes) {
   if (!h || !bytes) return set_err(LP_ERR_ARG, "lp_device_bytes: null pointer");
-  int64_t b = h->erho.n * 4 + h->spec.n * 8;
+  int64_t b = h->erho.n * 4 + h->spec.n * 8 + h->tw_rho.n * 8 + h->tw_th.n * 8;
   if (h->fwd) {
     for (int k = 0; k < 3; ++k) b += h->fwd->c2lp[k].n * 8 + h->fwd->rows[k].n * 4;
     b += h->fwd->thc.n * 4 + h->fwd->rhoc.n * 4 + h->fwd->fz.n * 8 + h->fwd->fbuf.n * 4;

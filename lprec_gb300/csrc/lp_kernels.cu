@@ -17,6 +17,7 @@
 // at index position (x, y), which is what sampling the reference's textures
 // at (x+0.5, y+0.5) means (src/include/main_kernels.cuh:21-84).
 #include "lp_kernels.cuh"
+#include "fft_reg.cuh"
 
 namespace lpgb {
 
@@ -61,6 +62,24 @@ __device__ __forceinline__ float interp2d(const float* __restrict__ img, int W, 
       for (int i = 0; i < 4; ++i) cx[i] = wrapi(ix - 1 + i, W);
     }
     float acc = 0.f;
+    const int b4 = (ix - 1) & ~3;
+    if ((W & 3) == 0 && ix >= 1 && b4 + 8 <= W) {
+      // the four taps lie in two aligned float4 of the row
+      const int o = ix - 1 - b4;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float* row = img + (size_t)wrapi(iy - 1 + j, H) * W + b4;
+        const float4 p = __ldg(reinterpret_cast<const float4*>(row));
+        const float4 q = __ldg(reinterpret_cast<const float4*>(row) + 1);
+        float t0, t1, t2, t3;
+        if (o == 0) { t0 = p.x; t1 = p.y; t2 = p.z; t3 = p.w; }
+        else if (o == 1) { t0 = p.y; t1 = p.z; t2 = p.w; t3 = q.x; }
+        else if (o == 2) { t0 = p.z; t1 = p.w; t2 = q.x; t3 = q.y; }
+        else { t0 = p.w; t1 = q.x; t2 = q.y; t3 = q.z; }
+        acc += wy[j] * (wx[0] * t0 + wx[1] * t1 + wx[2] * t2 + wx[3] * t3);
+      }
+      return acc;
+    }
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const float* row = img + (size_t)wrapi(iy - 1 + j, H) * W;
@@ -112,6 +131,15 @@ __device__ __forceinline__ int axis_weights(float t, int cubic, float* w) {
   w[2] = 0.f;
   w[3] = 0.f;
   return it;
+}
+
+// Two complex FFT buffers (nfft signals of length L each) at the start of
+// dynamic shared memory; returns the first float after them.
+__device__ __forceinline__ float* carve(float* sm, int L, int nfft, CBuf& a, CBuf& b) {
+  const int pf = nfft * fft_plane_floats(L);
+  a = CBuf{sm, sm + pf};
+  b = CBuf{sm + 2 * pf, sm + 3 * pf};
+  return sm + 4 * pf;
 }
 
 // ---------------------------------------------------------------------------
@@ -290,10 +318,10 @@ __global__ void k_col_prefilter(ColPrefilterArgs a) {
 // multiply by e^rho, FFT along rho (two real columns in one complex FFT).
 // Reference: interp mode 3 (lpRgpu.cu:263), mulexp (:267), R2C (:270).
 // ---------------------------------------------------------------------------
-__global__ void k_fwd_c2lp(FwdC2LPArgs a) {
-  extern __shared__ float2 sm2[];
-  float2* A = sm2;
-  float2* B = sm2 + a.Nrho;
+__global__ void __launch_bounds__(256, 2) k_fwd_c2lp(FwdC2LPArgs a) {
+  extern __shared__ float smf[];
+  CBuf A, B;
+  carve(smf, a.Nrho, 1, A, B);
   const int s = blockIdx.x;
   const int th = 2 * blockIdx.y;
   const int thb = th + 1 < a.Nth ? th + 1 : -1;
@@ -309,14 +337,14 @@ __global__ void k_fwd_c2lp(FwdC2LPArgs a) {
       const float2 pb = __ldg(cb + r);
       if (!isnan(pb.x)) vb = e * interp2d(img, a.N, a.N, pb.x, pb.y, a.cubic);
     }
-    A[r] = make_float2(va, vb);
+    A.set(r, make_float2(va, vb));
   }
   __syncthreads();
-  const float2* Z = fft_block<-1>(A, B, a.plan, 1, a.Nrho);
+  const CBuf Z = fft_block<-1>(A, B, a.plan, 1, 0);
   float2* out = a.spec + (size_t)s * a.Nk * a.Nth;
   for (int k = threadIdx.x; k < a.Nk; k += blockDim.x) {
-    const float2 z1 = Z[k];
-    const float2 z2 = Z[k == 0 ? 0 : a.Nrho - k];
+    const float2 z1 = Z.get(k);
+    const float2 z2 = Z.get(k == 0 ? 0 : a.Nrho - k);
     out[(size_t)k * a.Nth + th] = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
     if (thb >= 0) out[(size_t)k * a.Nth + thb] = make_float2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
   }
@@ -327,38 +355,49 @@ __global__ void k_fwd_c2lp(FwdC2LPArgs a) {
 // Reference: the theta half of cuFFT's 2-D R2C/C2R and `mul`
 // (lpRgpu.cu:270-277, simple_kernels.cuh:2-12).
 // ---------------------------------------------------------------------------
-__global__ void k_theta_conv(ThetaConvArgs a) {
-  extern __shared__ float2 sm2[];
-  float2* A = sm2;
-  float2* B = sm2 + a.Nth;
+__global__ void __launch_bounds__(256, 2) k_theta_conv(ThetaConvArgs a) {
+  extern __shared__ float smf[];
+  CBuf A, B;
+  carve(smf, a.Nth, 2, A, B);
   const int s = blockIdx.x;
-  const int k = blockIdx.y;
-  float2* row = a.spec + ((size_t)s * a.Nk + k) * a.Nth;
-  for (int t = threadIdx.x; t < a.Nth; t += blockDim.x)
-    A[t] = (t >= a.in_lo && t <= a.in_hi) ? row[t] : make_float2(0.f, 0.f);
-  __syncthreads();
-  float2* X = fft_block<-1>(A, B, a.plan, 1, a.Nth);
-  const float2* fz = a.fz + (size_t)k * a.Nth;
-  for (int t = threadIdx.x; t < a.Nth; t += blockDim.x) {
-    float2 w = __ldg(fz + t);
-    if (a.conj_fz) w.y = -w.y;
-    X[t] = cscale(cmul(X[t], w), a.scale);
+  const int k0 = 2 * blockIdx.y;
+  const int nrow = (k0 + 1 < a.Nk) ? 2 : 1;
+  float2* rows = a.spec + ((size_t)s * a.Nk + k0) * a.Nth;
+  const int ps = fft_plane_floats(a.Nth);  // plane stride between the two rows
+  for (int i = threadIdx.x; i < 2 * a.Nth; i += blockDim.x) {
+    const int r = i / a.Nth, t = i - r * a.Nth;
+    const bool in = r < nrow && t >= a.in_lo && t <= a.in_hi;
+    A.offset(r * ps).set(t, in ? rows[i] : make_float2(0.f, 0.f));
   }
   __syncthreads();
-  float2* Y = fft_block<1>(X, X == A ? B : A, a.plan, 1, a.Nth);
-  for (int t = a.out_lo + threadIdx.x; t <= a.out_hi; t += blockDim.x) row[t] = Y[t];
+  const CBuf X = fft_block<-1>(A, B, a.plan, 2, ps);
+  const float2* fz = a.fz + (size_t)k0 * a.Nth;
+  for (int i = threadIdx.x; i < nrow * a.Nth; i += blockDim.x) {
+    const int r = i / a.Nth, t = i - r * a.Nth;
+    float2 w = __ldg(fz + i);
+    if (a.conj_fz) w.y = -w.y;
+    const CBuf Xr = X.offset(r * ps);
+    Xr.set(t, cscale(cmul(Xr.get(t), w), a.scale));
+  }
+  __syncthreads();
+  const CBuf Y = fft_block<1>(X, X.re == A.re ? B : A, a.plan, 2, ps);
+  const int w = a.out_hi - a.out_lo + 1;
+  for (int i = threadIdx.x; i < nrow * w; i += blockDim.x) {
+    const int r = i / w, t = a.out_lo + (i - r * w);
+    rows[(size_t)r * a.Nth + t] = Y.offset(r * ps).get(t);
+  }
 }
 
 // Build the complex signal whose inverse FFT gives two real rho profiles
 // from their half spectra V0, V1 (kr = 0..Nrho/2); C2R semantics: the
 // imaginary parts at kr = 0 and kr = Nrho/2 are ignored.
-__device__ __forceinline__ void put_pair(float2* Z, int k, int Nrho, float2 v0, float2 v1) {
+__device__ __forceinline__ void put_pair(const CBuf& Z, int k, int Nrho, float2 v0, float2 v1) {
   const int half = Nrho / 2;
   if (k == 0 || k == half) {
-    Z[k] = make_float2(v0.x, v1.x);
+    Z.set(k, make_float2(v0.x, v1.x));
   } else {
-    Z[k] = make_float2(v0.x - v1.y, v0.y + v1.x);
-    Z[Nrho - k] = make_float2(v0.x + v1.y, v1.x - v0.y);
+    Z.set(k, make_float2(v0.x - v1.y, v0.y + v1.x));
+    Z.set(Nrho - k, make_float2(v0.x + v1.y, v1.x - v0.y));
   }
 }
 
@@ -369,10 +408,10 @@ __device__ __forceinline__ void put_pair(float2* Z, int k, int Nrho, float2 v0, 
 // into the caller's sinogram (stepangles + cor window, lpRgpu.cu:191-192).
 // Reference: C2R (:277), interp mode 5 (:284).
 // ---------------------------------------------------------------------------
-__global__ void k_fwd_lp2polar(FwdLP2PolarArgs a) {
-  extern __shared__ float2 sm2[];
-  float2* A = sm2;
-  float2* B = sm2 + a.Nrho;
+__global__ void __launch_bounds__(256, 2) k_fwd_lp2polar(FwdLP2PolarArgs a) {
+  extern __shared__ float smf[];
+  CBuf A, B;
+  carve(smf, a.Nrho, 1, A, B);
   const int s = blockIdx.x;
   const int i0 = 2 * blockIdx.y;
   const int r0 = a.rows[i0];
@@ -407,19 +446,19 @@ __global__ void k_fwd_lp2polar(FwdLP2PolarArgs a) {
     put_pair(A, k, a.Nrho, v0, v1);
   }
   __syncthreads();
-  const float2* zr = fft_block<1>(A, B, a.plan, 1, a.Nrho);
+  const CBuf zr = fft_block<1>(A, B, a.plan, 1, 0);
   const int Nrho = a.Nrho;
   for (int x = threadIdx.x; x < a.N; x += blockDim.x) {
     const int xo = x - a.cor_off;
     if (xo < 0 || xo >= a.N0) continue;
     if (r0 % a.os == 0) {
       const float t = __ldg(a.rhoc + (size_t)r0 * a.N + x);
-      const float v = interp1d([&](int i) { return zr[i].x; }, Nrho, t, a.cubic);
+      const float v = interp1d([&](int i) { return zr.re[fpad(i)]; }, Nrho, t, a.cubic);
       a.Rout[((size_t)s * a.Nproj0 + r0 / a.os) * a.N0 + xo] = v;
     }
     if (r1 >= 0 && r1 % a.os == 0) {
       const float t = __ldg(a.rhoc + (size_t)r1 * a.N + x);
-      const float v = interp1d([&](int i) { return zr[i].y; }, Nrho, t, a.cubic);
+      const float v = interp1d([&](int i) { return zr.im[fpad(i)]; }, Nrho, t, a.cubic);
       a.Rout[((size_t)s * a.Nproj0 + r1 / a.os) * a.N0 + xo] = v;
     }
   }
@@ -431,15 +470,14 @@ __global__ void k_fwd_lp2polar(FwdLP2PolarArgs a) {
 // lpRgpu.cu:333-382) as one complex FFT of length 4N for both rows, and the
 // row (s direction) prefilter.  Rows between angle steps are written as 0.
 // ---------------------------------------------------------------------------
-__global__ void k_adj_ingest(AdjIngestArgs a) {
-  extern __shared__ float2 sm2[];
+__global__ void __launch_bounds__(256, 2) k_adj_ingest(AdjIngestArgs a) {
+  extern __shared__ float smf[];
   const int N = a.N;
-  const int M = 4 * N;
+  const int M = 2 * N;  // the filter couples samples less than N apart: a 2N circular convolution is exact
   const bool filt = a.H != nullptr;
-  float2* F0 = sm2;
-  float2* F1 = sm2 + (filt ? M : 0);
-  float* lines = reinterpret_cast<float*>(sm2 + (filt ? 2 * M : 0));  // 2 rows
-  float* cp = lines + 2 * N;                                          // 2 rows scratch
+  CBuf F0, F1;
+  float* lines = filt ? carve(smf, M, 1, F0, F1) : smf;  // 2 rows
+  float* cp = lines + 2 * N;                             // 2 rows of scratch
   const int s = blockIdx.x;
   const int q0 = 2 * blockIdx.y;
   const int q1 = q0 + 1 < a.Nproj0 ? q0 + 1 : -1;
@@ -453,16 +491,16 @@ __global__ void k_adj_ingest(AdjIngestArgs a) {
   __syncthreads();
   if (filt) {
     for (int x = threadIdx.x; x < M; x += blockDim.x)
-      F0[x] = x < N ? make_float2(lines[x], lines[N + x]) : make_float2(0.f, 0.f);
+      F0.set(x, x < N ? make_float2(lines[x], lines[N + x]) : make_float2(0.f, 0.f));
     __syncthreads();
-    float2* X = fft_block<-1>(F0, F1, a.plan, 1, M);
-    const float sc = 1.0f / (float)M;
-    for (int k = threadIdx.x; k < M; k += blockDim.x) X[k] = cscale(X[k], __ldg(a.H + k) * sc);
+    const CBuf X = fft_block<-1>(F0, F1, a.plan, 1, 0);
+    for (int k = threadIdx.x; k < M; k += blockDim.x) X.set(k, cscale(X.get(k), __ldg(a.H + k)));
     __syncthreads();
-    float2* Y = fft_block<1>(X, X == F0 ? F1 : F0, a.plan, 1, M);
+    const CBuf Y = fft_block<1>(X, X.re == F0.re ? F1 : F0, a.plan, 1, 0);
     for (int x = threadIdx.x; x < N; x += blockDim.x) {
-      lines[x] = Y[x].x;
-      lines[N + x] = Y[x].y;
+      const float2 y = Y.get(x);
+      lines[x] = y.x;
+      lines[N + x] = y.y;
     }
     __syncthreads();
   }
@@ -491,11 +529,10 @@ __global__ void k_adj_ingest(AdjIngestArgs a) {
 // points add a direct 2-D sample.  Then FFT along rho.
 // Reference: interp mode 4 for lpids and wids (lpRgpu.cu:307, :311), R2C (:314).
 // ---------------------------------------------------------------------------
-__global__ void k_adj_polar2lp(AdjPolar2LPArgs a) {
-  extern __shared__ float2 sm2[];
-  float2* A = sm2;
-  float2* B = sm2 + a.Nrho;
-  float* prof = reinterpret_cast<float*>(sm2 + 2 * a.Nrho);  // 2 x N
+__global__ void __launch_bounds__(256, 2) k_adj_polar2lp(AdjPolar2LPArgs a) {
+  extern __shared__ float smf[];
+  CBuf A, B;
+  float* prof = carve(smf, a.Nrho, 1, A, B);  // 2 x N
   const int s = blockIdx.x;
   const int th0 = a.clo + 2 * blockIdx.y;
   const int th1 = th0 + 1 <= a.chi ? th0 + 1 : -1;
@@ -535,7 +572,7 @@ __global__ void k_adj_polar2lp(AdjPolar2LPArgs a) {
       const float x1 = __ldg(sx1 + r);
       if (!isnan(x1)) v1 = interp1d([&](int i) { return prof[a.N + i]; }, a.N, x1, a.cubic);
     }
-    A[r] = make_float2(v0, v1);
+    A.set(r, make_float2(v0, v1));
   }
   __syncthreads();
   // wrap points (distinct rho within a column)
@@ -547,16 +584,16 @@ __global__ void k_adj_polar2lp(AdjPolar2LPArgs a) {
       const float4 p = __ldg(a.wpt + w);
       const int r = (int)p.x;
       const float v = interp2d(img, a.N, a.Nproj, p.y, p.z, a.cubic);
-      if (c == 0) A[r].x += v;
-      else A[r].y += v;
+      if (c == 0) A.re[fpad(r)] += v;
+      else A.im[fpad(r)] += v;
     }
     __syncthreads();
   }
-  const float2* Z = fft_block<-1>(A, B, a.plan, 1, a.Nrho);
+  const CBuf Z = fft_block<-1>(A, B, a.plan, 1, 0);
   float2* out = a.spec + (size_t)s * a.Nk * a.Nth;
   for (int k = threadIdx.x; k < a.Nk; k += blockDim.x) {
-    const float2 z1 = Z[k];
-    const float2 z2 = Z[k == 0 ? 0 : a.Nrho - k];
+    const float2 z1 = Z.get(k);
+    const float2 z2 = Z.get(k == 0 ? 0 : a.Nrho - k);
     out[(size_t)k * a.Nth + th0] = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
     if (th1 >= 0) out[(size_t)k * a.Nth + th1] = make_float2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
   }
@@ -566,10 +603,10 @@ __global__ void k_adj_polar2lp(AdjPolar2LPArgs a) {
 // adjoint, per span: inverse FFT along rho for two theta columns, store the
 // real log-polar columns [theta][rho] for the Cartesian gather (C2R :321).
 // ---------------------------------------------------------------------------
-__global__ void k_adj_lpcols(AdjLPColsArgs a) {
-  extern __shared__ float2 sm2[];
-  float2* A = sm2;
-  float2* B = sm2 + a.Nrho;
+__global__ void __launch_bounds__(256, 2) k_adj_lpcols(AdjLPColsArgs a) {
+  extern __shared__ float smf[];
+  CBuf A, B;
+  carve(smf, a.Nrho, 1, A, B);
   const int s = blockIdx.x;
   const int th0 = a.lo2 + 2 * blockIdx.y;
   const int th1 = th0 + 1 <= a.hi2 ? th0 + 1 : -1;
@@ -580,11 +617,12 @@ __global__ void k_adj_lpcols(AdjLPColsArgs a) {
     put_pair(A, k, a.Nrho, v0, v1);
   }
   __syncthreads();
-  const float2* z = fft_block<1>(A, B, a.plan, 1, a.Nrho);
+  const CBuf z = fft_block<1>(A, B, a.plan, 1, 0);
   float* g0 = a.G + ((size_t)s * a.W2 + (th0 - a.lo2)) * a.Nrho;
   for (int r = threadIdx.x; r < a.Nrho; r += blockDim.x) {
-    g0[r] = z[r].x;
-    if (th1 >= 0) g0[a.Nrho + r] = z[r].y;
+    const float2 v = z.get(r);
+    g0[r] = v.x;
+    if (th1 >= 0) g0[a.Nrho + r] = v.y;
   }
 }
 
@@ -599,6 +637,8 @@ __device__ __forceinline__ float interp_cols(const float* __restrict__ G, int Nr
   const int ct = axis_weights(t.x, cubic, wt);
   const int cr = axis_weights(t.y, cubic, wr);
   const int nt = cubic ? 4 : 2;
+  const int b4 = cr & ~3;
+  const bool vec = cubic && (Nrho & 3) == 0 && cr >= 0 && b4 + 8 <= Nrho;
   int rr[4];
   const bool inner = (cr >= 0 && cr + 3 < Nrho);
 #pragma unroll
@@ -609,9 +649,22 @@ __device__ __forceinline__ float interp_cols(const float* __restrict__ G, int Nr
     if (col < 0 || col >= W2) continue;  // outside the stored band: zero weight by construction
     const float* g = G + (size_t)col * Nrho;
     float v = 0.f;
+    if (vec) {
+      // the four rho taps lie in two aligned float4 of the column
+      const float4 p = __ldg(reinterpret_cast<const float4*>(g + b4));
+      const float4 q = __ldg(reinterpret_cast<const float4*>(g + b4) + 1);
+      const int o = cr - b4;
+      float t0, t1, t2, t3;
+      if (o == 0) { t0 = p.x; t1 = p.y; t2 = p.z; t3 = p.w; }
+      else if (o == 1) { t0 = p.y; t1 = p.z; t2 = p.w; t3 = q.x; }
+      else if (o == 2) { t0 = p.z; t1 = p.w; t2 = q.x; t3 = q.y; }
+      else { t0 = p.w; t1 = q.x; t2 = q.y; t3 = q.z; }
+      v = wr[0] * t0 + wr[1] * t1 + wr[2] * t2 + wr[3] * t3;
+    } else {
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
-      if (i < nt) v += wr[i] * __ldg(g + rr[i]);
+      for (int i = 0; i < 4; ++i)
+        if (i < nt) v += wr[i] * __ldg(g + rr[i]);
+    }
     acc += wt[j] * v;
   }
   return acc;
@@ -637,14 +690,25 @@ __global__ void k_adj_lp2cart(AdjLP2CartArgs a) {
 // ---------------------------------------------------------------------------
 static const int kFFTThreads = 256;
 
-static size_t smem_c2lp(int Nrho) { return 2 * (size_t)Nrho * sizeof(float2); }
-static size_t smem_theta(int Nth) { return 2 * (size_t)Nth * sizeof(float2); }
+static size_t fft_bytes(int L, int nfft) { return 4 * (size_t)nfft * fft_plane_floats(L) * sizeof(float); }
+static size_t smem_c2lp(int Nrho) { return fft_bytes(Nrho, 1); }
+static size_t smem_theta(int Nth) { return fft_bytes(Nth, 2); }
 static size_t smem_adj_ingest(int N, bool filt) {
-  return (filt ? 2 * (size_t)4 * N * sizeof(float2) : 0) + 4 * (size_t)N * sizeof(float);
+  return (filt ? fft_bytes(2 * N, 1) : 0) + 4 * (size_t)N * sizeof(float);
 }
-static size_t smem_polar2lp(int Nrho, int N) { return 2 * (size_t)Nrho * sizeof(float2) + 2 * (size_t)N * sizeof(float); }
+static size_t smem_polar2lp(int Nrho, int N) { return fft_bytes(Nrho, 1) + 2 * (size_t)N * sizeof(float); }
 
 static int g_smem_optin = 48 * 1024;
+static cudaError_t smem_ok(size_t need);
+cudaError_t configure_p2_kernels(int optin);
+bool p2_fwd_c2lp(const FwdC2LPArgs& a, int S, cudaStream_t st, cudaError_t* err);
+bool p2_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st, cudaError_t* err);
+bool p2_fwd_lp2polar(const FwdLP2PolarArgs& a, int S, cudaStream_t st, cudaError_t* err);
+bool p2_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st, cudaError_t* err);
+bool p2_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st, cudaError_t* err);
+bool p2_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st, cudaError_t* err);
+// generic (any N) kernels are used when g_use_p2 is false or the size is not a power of two
+static bool g_use_p2 = true;
 
 // Allow every kernel the device's opt-in shared memory; launches check their
 // own need against it.
@@ -663,8 +727,10 @@ cudaError_t configure_kernels(int N) {
     e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     if (e != cudaSuccess) return e;
   }
-  return cudaSuccess;
+  return configure_p2_kernels(optin);
 }
+
+void set_use_p2(bool on) { g_use_p2 = on; }
 
 static cudaError_t smem_ok(size_t need) {
   return need <= (size_t)g_smem_optin ? cudaSuccess : cudaErrorInvalidConfiguration;
@@ -688,6 +754,8 @@ cudaError_t launch_col_prefilter(const ColPrefilterArgs& a, int S, cudaStream_t 
 }
 
 cudaError_t launch_fwd_c2lp(const FwdC2LPArgs& a, int S, cudaStream_t st) {
+  cudaError_t pe;
+  if (g_use_p2 && p2_fwd_c2lp(a, S, st, &pe)) return pe;
   if (smem_ok(smem_c2lp(a.Nrho)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.Nth + 1) / 2);
   k_fwd_c2lp<<<grid, kFFTThreads, smem_c2lp(a.Nrho), st>>>(a);
@@ -695,13 +763,17 @@ cudaError_t launch_fwd_c2lp(const FwdC2LPArgs& a, int S, cudaStream_t st) {
 }
 
 cudaError_t launch_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st) {
+  cudaError_t pe;
+  if (g_use_p2 && p2_theta_conv(a, S, st, &pe)) return pe;
   if (smem_ok(smem_theta(a.Nth)) != cudaSuccess) return cudaErrorInvalidConfiguration;
-  dim3 grid(S, a.Nk);
+  dim3 grid(S, (a.Nk + 1) / 2);
   k_theta_conv<<<grid, kFFTThreads, smem_theta(a.Nth), st>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_fwd_lp2polar(const FwdLP2PolarArgs& a, int S, cudaStream_t st) {
+  cudaError_t pe;
+  if (g_use_p2 && p2_fwd_lp2polar(a, S, st, &pe)) return pe;
   if (a.nrows <= 0) return cudaSuccess;
   if (smem_ok(smem_c2lp(a.Nrho)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.nrows + 1) / 2);
@@ -710,6 +782,8 @@ cudaError_t launch_fwd_lp2polar(const FwdLP2PolarArgs& a, int S, cudaStream_t st
 }
 
 cudaError_t launch_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st) {
+  cudaError_t pe;
+  if (g_use_p2 && p2_adj_ingest(a, S, st, &pe)) return pe;
   if (smem_ok(smem_adj_ingest(a.N, a.H != nullptr)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.Nproj0 + 1) / 2);
   k_adj_ingest<<<grid, kFFTThreads, smem_adj_ingest(a.N, a.H != nullptr), st>>>(a);
@@ -717,6 +791,8 @@ cudaError_t launch_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st) {
 }
 
 cudaError_t launch_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st) {
+  cudaError_t pe;
+  if (g_use_p2 && p2_adj_polar2lp(a, S, st, &pe)) return pe;
   if (a.chi < a.clo) return cudaSuccess;
   if (smem_ok(smem_polar2lp(a.Nrho, a.N)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.chi - a.clo + 2) / 2);
@@ -725,6 +801,8 @@ cudaError_t launch_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st
 }
 
 cudaError_t launch_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st) {
+  cudaError_t pe;
+  if (g_use_p2 && p2_adj_lpcols(a, S, st, &pe)) return pe;
   if (smem_ok(smem_c2lp(a.Nrho)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.hi2 - a.lo2 + 2) / 2);
   k_adj_lpcols<<<grid, kFFTThreads, smem_c2lp(a.Nrho), st>>>(a);
@@ -735,6 +813,520 @@ cudaError_t launch_adj_lp2cart(const AdjLP2CartArgs& a, int S, cudaStream_t st) 
   dim3 grid(S, (a.npix + 255) / 256);
   k_adj_lp2cart<<<grid, 256, 0, st>>>(a);
   return cudaGetLastError();
+}
+
+}  // namespace lpgb
+
+// ===========================================================================
+// Power-of-two sizes (N = 256 .. 4096): the same kernels on the register FFT
+// of fft_reg.cuh.  A signal is transformed by T = L/16 threads; blocks of 256
+// threads carry 256/T signals when L < 4096.
+// ===========================================================================
+namespace lpgb {
+
+template <int L>
+struct P2 {
+  static constexpr int T = L / 16;                  // threads per signal
+  static constexpr int NSIG = T >= 256 ? 1 : 256 / T;
+  static constexpr int BLOCK = T * NSIG;
+  static constexpr int SLOTS = reg_fft_slots(L);
+};
+
+// forward, per span: Cartesian -> log-polar gather for column pairs, e^rho, FFT along rho
+template <int L>
+__global__ void __launch_bounds__(256, 2) k_fwd_c2lp_p2(FwdC2LPArgs a) {
+  extern __shared__ float2 sm2[];
+  constexpr int T = P2<L>::T;
+  const int sig = threadIdx.x / T, t = threadIdx.x % T;
+  float2* sm = sm2 + sig * P2<L>::SLOTS;
+  const int s = blockIdx.x;
+  const int th = 2 * (blockIdx.y * P2<L>::NSIG + sig);
+  const bool live = th < a.Nth;
+  const int thb = (live && th + 1 < a.Nth) ? th + 1 : -1;
+  const float* img = a.fbuf + (size_t)s * a.N * a.N;
+  const float2* ca = a.c2lp + (size_t)(live ? th : 0) * L;
+  const float2* cb = a.c2lp + (size_t)max(thb, 0) * L;
+  float2 v[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const int r = t + i * T;
+    float va = 0.f, vb = 0.f;
+    if (live) {
+      const float e = __ldg(a.erho + r);
+      const float2 pa = __ldg(ca + r);
+      if (!isnan(pa.x)) va = e * interp2d(img, a.N, a.N, pa.x, pa.y, a.cubic);
+      if (thb >= 0) {
+        const float2 pb = __ldg(cb + r);
+        if (!isnan(pb.x)) vb = e * interp2d(img, a.N, a.N, pb.x, pb.y, a.cubic);
+      }
+    }
+    v[i] = make_float2(va, vb);
+  }
+  reg_fft<L, -1>(v, sm, t);
+  if (!live) return;
+  float2* out = a.spec + (size_t)s * a.Nk * a.Nth;
+  for (int k = t; k < a.Nk; k += T) {
+    const float2 z1 = sm[spad(k)];
+    const float2 z2 = sm[spad((L - k) & (L - 1))];
+    const float4 pr = make_float4(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y), 0.5f * (z1.y + z2.y),
+                                  0.5f * (z2.x - z1.x));
+    if (thb >= 0) *reinterpret_cast<float4*>(out + (size_t)k * a.Nth + th) = pr;
+    else out[(size_t)k * a.Nth + th] = make_float2(pr.x, pr.y);
+  }
+}
+
+// per rho frequency: FFT along theta, multiply by the kernel, inverse; NSIG rows per block
+template <int L>
+__global__ void __launch_bounds__(256, 2) k_theta_conv_p2(ThetaConvArgs a) {
+  extern __shared__ float2 sm2[];
+  constexpr int T = P2<L>::T;
+  const int sig = threadIdx.x / T, t = threadIdx.x % T;
+  float2* sm = sm2 + sig * P2<L>::SLOTS;
+  const int s = blockIdx.x;
+  const int k = blockIdx.y * P2<L>::NSIG + sig;
+  const bool live = k < a.Nk;
+  float2* row = a.spec + ((size_t)s * a.Nk + (live ? k : 0)) * L;
+  float2 v[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const int c = t + i * T;
+    v[i] = (live && c >= a.in_lo && c <= a.in_hi) ? row[c] : make_float2(0.f, 0.f);
+  }
+  reg_fft<L, -1>(v, sm, t);
+  const float2* fz = a.fz + (size_t)(live ? k : 0) * L;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const int c = t + i * T;
+    float2 w = __ldg(fz + c);
+    if (a.conj_fz) w.y = -w.y;
+    v[i] = cscale(cmul(sm[spad(c)], w), a.scale);
+  }
+  __syncthreads();
+  reg_fft<L, 1>(v, sm, t);
+  if (!live) return;
+  for (int c = a.out_lo + t; c <= a.out_hi; c += T) row[c] = sm[spad(c)];
+}
+
+// element p of the complex signal whose inverse FFT gives two real profiles
+// with half spectra V0, V1 (C2R semantics: imaginary parts at 0 and L/2 ignored)
+__device__ __forceinline__ float2 pair_elem(int p, int L, float2 v0, float2 v1) {
+  const int half = L / 2;
+  if (p == 0 || p == half) return make_float2(v0.x, v1.x);
+  if (p < half) return make_float2(v0.x - v1.y, v0.y + v1.x);
+  return make_float2(v0.x + v1.y, v1.x - v0.y);  // conj(V0) + i conj(V1) at L - p
+}
+
+// forward, per span: two angle rows per signal, theta taps combined in frequency,
+// inverse FFT along rho, rho interpolation into the caller's sinogram
+template <int L>
+__global__ void __launch_bounds__(256, 2) k_fwd_lp2polar_p2(FwdLP2PolarArgs a) {
+  extern __shared__ float2 sm2[];
+  constexpr int T = P2<L>::T;
+  const int sig = threadIdx.x / T, t = threadIdx.x % T;
+  float2* sm = sm2 + sig * P2<L>::SLOTS;
+  const int s = blockIdx.x;
+  const int i0 = 2 * (blockIdx.y * P2<L>::NSIG + sig);
+  const bool live = i0 < a.nrows;
+  const int r0 = live ? a.rows[i0] : 0;
+  const int r1 = (live && i0 + 1 < a.nrows) ? a.rows[i0 + 1] : -1;
+  float w0[4], w1[4];
+  const int c0 = axis_weights(__ldg(a.thc + r0), a.cubic, w0);
+  int c1 = 0;
+  if (r1 >= 0) {
+    c1 = axis_weights(__ldg(a.thc + r1), a.cubic, w1);
+  } else {
+    w1[0] = w1[1] = w1[2] = w1[3] = 0.f;
+  }
+  if (!live) w0[0] = w0[1] = w0[2] = w0[3] = 0.f;
+  int t0[4], t1[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    t0[j] = wrapi(c0 + j, a.Nth);
+    t1[j] = wrapi(c1 + j, a.Nth);
+  }
+  const int ntap = a.cubic ? 4 : 2;
+  const float2* sp = a.spec + (size_t)s * a.Nk * a.Nth;
+  // both rows' taps as offsets into one run of consecutive columns starting at cu
+  const int cu = min(c0, r1 >= 0 ? c1 : c0);
+  const int nu = max(c0, r1 >= 0 ? c1 : c0) - cu + ntap;
+  const bool run = nu <= 8 && cu >= 0 && cu + nu <= a.Nth;
+  float u0[8], u1[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int j0 = cu + q - c0, j1 = cu + q - c1;
+    u0[q] = (j0 >= 0 && j0 < ntap) ? w0[j0] : 0.f;
+    u1[q] = (r1 >= 0 && j1 >= 0 && j1 < ntap) ? w1[j1] : 0.f;
+  }
+  for (int kk = t; kk <= L / 2; kk += T) {
+    const float2* row = sp + (size_t)kk * a.Nth;
+    float2 v0 = make_float2(0.f, 0.f), v1 = make_float2(0.f, 0.f);
+    if (run) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        if (q < nu) {
+          const float2 z = row[cu + q];
+          v0.x += u0[q] * z.x;
+          v0.y += u0[q] * z.y;
+          v1.x += u1[q] * z.x;
+          v1.y += u1[q] * z.y;
+        }
+      }
+    } else {
+      for (int j = 0; j < ntap; ++j) {
+        const float2 q0 = row[t0[j]];
+        v0.x += w0[j] * q0.x;
+        v0.y += w0[j] * q0.y;
+        const float2 q1 = row[t1[j]];
+        v1.x += w1[j] * q1.x;
+        v1.y += w1[j] * q1.y;
+      }
+    }
+    sm[spad(kk)] = pair_elem(kk, L, v0, v1);
+    if (kk > 0 && kk < L / 2) sm[spad(L - kk)] = pair_elem(L - kk, L, v0, v1);
+  }
+  __syncthreads();
+  float2 v[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = sm[spad(t + i * T)];
+  __syncthreads();
+  reg_fft<L, 1>(v, sm, t);
+  if (!live) return;
+  for (int x = t; x < a.N; x += T) {
+    const int xo = x - a.cor_off;
+    if (xo < 0 || xo >= a.N0) continue;
+    if (r0 % a.os == 0) {
+      const float tr = __ldg(a.rhoc + (size_t)r0 * a.N + x);
+      const float val = interp1d([&](int i) { return sm[spad(i)].x; }, L, tr, a.cubic);
+      a.Rout[((size_t)s * a.Nproj0 + r0 / a.os) * a.N0 + xo] = val;
+    }
+    if (r1 >= 0 && r1 % a.os == 0) {
+      const float tr = __ldg(a.rhoc + (size_t)r1 * a.N + x);
+      const float val = interp1d([&](int i) { return sm[spad(i)].y; }, L, tr, a.cubic);
+      a.Rout[((size_t)s * a.Nproj0 + r1 / a.os) * a.N0 + xo] = val;
+    }
+  }
+}
+
+// adjoint ingest for N = L/2: one pair of input rows per block of T threads
+template <int L>
+__global__ void __launch_bounds__(256, 2) k_adj_ingest_p2(AdjIngestArgs a) {
+  extern __shared__ float2 sm2[];
+  constexpr int T = P2<L>::T;
+  const int N = L / 2;
+  const bool filt = a.H != nullptr;
+  float2* sm = sm2;
+  float* lines = reinterpret_cast<float*>(sm2 + (filt ? P2<L>::SLOTS : 0));  // 2 rows
+  float* cp = lines + 2 * N;
+  const int t = threadIdx.x;
+  const int s = blockIdx.x;
+  const int q0 = 2 * blockIdx.y;
+  const int q1 = q0 + 1 < a.Nproj0 ? q0 + 1 : -1;
+  const float* in0 = a.Rin + ((size_t)s * a.Nproj0 + q0) * a.N0;
+  const float* in1 = a.Rin + ((size_t)s * a.Nproj0 + max(q1, 0)) * a.N0;
+  if (filt) {
+    float2 v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int x = t + i * T;
+      const int xi = min(max(x - a.cor_off, 0), a.N0 - 1);
+      v[i] = x < N ? make_float2(__ldg(in0 + xi), q1 >= 0 ? __ldg(in1 + xi) : 0.f) : make_float2(0.f, 0.f);
+    }
+    reg_fft<L, -1>(v, sm, t);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int k = t + i * T;
+      v[i] = cscale(sm[spad(k)], __ldg(a.H + k));
+    }
+    __syncthreads();
+    reg_fft<L, 1>(v, sm, t);
+    for (int x = t; x < N; x += T) {
+      const float2 y = sm[spad(x)];
+      lines[x] = y.x;
+      lines[N + x] = y.y;
+    }
+  } else {
+    for (int x = t; x < N; x += T) {
+      const int xi = min(max(x - a.cor_off, 0), a.N0 - 1);
+      lines[x] = __ldg(in0 + xi);
+      lines[N + x] = q1 >= 0 ? __ldg(in1 + xi) : 0.f;
+    }
+  }
+  __syncthreads();
+  if (a.cubic) {
+    const int half = T / 2;
+    const int which = t >= half;
+    prefilter_line(lines + which * N, cp + which * N, N, t - which * half, half);
+  }
+  for (int rr = 0; rr < 2; ++rr) {
+    const int q = rr == 0 ? q0 : q1;
+    if (q < 0) break;
+    for (int j = 0; j < a.os; ++j) {
+      float* dst = a.rbuf + ((size_t)s * a.Nproj + (size_t)q * a.os + j) * N;
+      for (int x = t; x < N; x += T) dst[x] = j == 0 ? lines[rr * N + x] : 0.f;
+    }
+  }
+}
+
+// adjoint, per span: polar -> log-polar for a column pair per signal, FFT along rho
+template <int L>
+__global__ void __launch_bounds__(256, 2) k_adj_polar2lp_p2(AdjPolar2LPArgs a) {
+  extern __shared__ float2 sm2[];
+  constexpr int T = P2<L>::T;
+  const int N = L / 2;
+  const int sig = threadIdx.x / T, t = threadIdx.x % T;
+  float2* sm = sm2 + sig * P2<L>::SLOTS;
+  float* prof = reinterpret_cast<float*>(sm2 + P2<L>::NSIG * P2<L>::SLOTS) + sig * 2 * N;
+  const int s = blockIdx.x;
+  const int th0 = a.clo + 2 * (blockIdx.y * P2<L>::NSIG + sig);
+  const bool live = th0 <= a.chi;
+  const int th1 = (live && th0 + 1 <= a.chi) ? th0 + 1 : -1;
+  const float* img = a.rbuf + (size_t)s * a.Nproj * N;
+  const float nanv = __int_as_float(0x7fc00000);
+  const float ta0 = live ? __ldg(a.ta + th0) : nanv;
+  const float ta1 = th1 >= 0 ? __ldg(a.ta + th1) : nanv;
+  float w0[4], w1[4];
+  int rw0[4], rw1[4];
+  const bool has0 = !isnan(ta0), has1 = !isnan(ta1);
+  const int ntap = a.cubic ? 4 : 2;
+  {
+    const int c0 = has0 ? axis_weights(ta0, a.cubic, w0) : 0;
+    const int c1 = has1 ? axis_weights(ta1, a.cubic, w1) : 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      rw0[j] = wrapi(c0 + j, a.Nproj);
+      rw1[j] = wrapi(c1 + j, a.Nproj);
+    }
+  }
+  for (int x = t; x < N; x += T) {
+    float p0 = 0.f, p1 = 0.f;
+    for (int j = 0; j < ntap; ++j) {
+      if (has0) p0 += w0[j] * __ldg(img + (size_t)rw0[j] * N + x);
+      if (has1) p1 += w1[j] * __ldg(img + (size_t)rw1[j] * N + x);
+    }
+    prof[x] = p0;
+    prof[N + x] = p1;
+  }
+  __syncthreads();
+  const float* sx0 = a.sx + (size_t)(live ? th0 : 0) * L;
+  const float* sx1 = a.sx + (size_t)max(th1, 0) * L;
+  for (int r = t; r < L; r += T) {
+    float v0 = 0.f, v1 = 0.f;
+    if (live) {
+      const float x0 = __ldg(sx0 + r);
+      if (!isnan(x0)) v0 = interp1d([&](int i) { return prof[i]; }, N, x0, a.cubic);
+    }
+    if (th1 >= 0) {
+      const float x1 = __ldg(sx1 + r);
+      if (!isnan(x1)) v1 = interp1d([&](int i) { return prof[N + i]; }, N, x1, a.cubic);
+    }
+    sm[spad(r)] = make_float2(v0, v1);
+  }
+  __syncthreads();
+  // wrap points (distinct rho within a column) add a direct 2-D sample
+  for (int c = 0; c < 2; ++c) {
+    const int th = c == 0 ? th0 : th1;
+    if (!live || th < 0) continue;
+    const int wb = __ldg(a.woff + th), we = __ldg(a.woff + th + 1);
+    for (int w = wb + t; w < we; w += T) {
+      const float4 p = __ldg(a.wpt + w);
+      const int r = (int)p.x;
+      const float val = interp2d(img, N, a.Nproj, p.y, p.z, a.cubic);
+      if (c == 0) sm[spad(r)].x += val;
+      else sm[spad(r)].y += val;
+    }
+  }
+  __syncthreads();
+  float2 v[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = sm[spad(t + i * T)];
+  __syncthreads();
+  reg_fft<L, -1>(v, sm, t);
+  if (!live) return;
+  float2* out = a.spec + (size_t)s * a.Nk * a.Nth;
+  const bool al = ((th0 & 1) == 0) && th1 >= 0;  // 16-byte aligned pair
+  for (int k = t; k < a.Nk; k += T) {
+    const float2 z1 = sm[spad(k)];
+    const float2 z2 = sm[spad((L - k) & (L - 1))];
+    const float4 pr = make_float4(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y), 0.5f * (z1.y + z2.y),
+                                  0.5f * (z2.x - z1.x));
+    if (al) {
+      *reinterpret_cast<float4*>(out + (size_t)k * a.Nth + th0) = pr;
+    } else {
+      out[(size_t)k * a.Nth + th0] = make_float2(pr.x, pr.y);
+      if (th1 >= 0) out[(size_t)k * a.Nth + th1] = make_float2(pr.z, pr.w);
+    }
+  }
+}
+
+// adjoint, per span: inverse FFT along rho for a column pair per signal
+template <int L>
+__global__ void __launch_bounds__(256, 2) k_adj_lpcols_p2(AdjLPColsArgs a) {
+  extern __shared__ float2 sm2[];
+  constexpr int T = P2<L>::T;
+  const int sig = threadIdx.x / T, t = threadIdx.x % T;
+  float2* sm = sm2 + sig * P2<L>::SLOTS;
+  const int s = blockIdx.x;
+  const int th0 = a.lo2 + 2 * (blockIdx.y * P2<L>::NSIG + sig);
+  const bool live = th0 <= a.hi2;
+  const int th1 = (live && th0 + 1 <= a.hi2) ? th0 + 1 : -1;
+  const float2* sp = a.spec + (size_t)s * a.Nk * a.Nth;
+  const bool al = ((th0 & 1) == 0) && th1 >= 0;
+  for (int kk = t; kk <= L / 2; kk += T) {
+    float2 v0 = make_float2(0.f, 0.f), v1 = make_float2(0.f, 0.f);
+    if (al) {
+      const float4 q = *reinterpret_cast<const float4*>(sp + (size_t)kk * a.Nth + th0);
+      v0 = make_float2(q.x, q.y);
+      v1 = make_float2(q.z, q.w);
+    } else if (live) {
+      v0 = sp[(size_t)kk * a.Nth + th0];
+      if (th1 >= 0) v1 = sp[(size_t)kk * a.Nth + th1];
+    }
+    sm[spad(kk)] = pair_elem(kk, L, v0, v1);
+    if (kk > 0 && kk < L / 2) sm[spad(L - kk)] = pair_elem(L - kk, L, v0, v1);
+  }
+  __syncthreads();
+  float2 v[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = sm[spad(t + i * T)];
+  __syncthreads();
+  reg_fft<L, 1>(v, sm, t);
+  if (!live) return;
+  float* g0 = a.G + ((size_t)s * a.W2 + (th0 - a.lo2)) * L;
+  for (int r = t; r < L; r += T) {
+    const float2 z = sm[spad(r)];
+    g0[r] = z.x;
+    if (th1 >= 0) g0[L + r] = z.y;
+  }
+}
+
+// ---- dispatch ----------------------------------------------------------------
+static bool p2_ok(int L) { return L >= 256 && L <= 8192 && (L & (L - 1)) == 0; }
+
+template <int L>
+static void set_p2_attrs(int optin) {
+  cudaFuncSetAttribute(k_fwd_c2lp_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  cudaFuncSetAttribute(k_theta_conv_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  cudaFuncSetAttribute(k_fwd_lp2polar_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  cudaFuncSetAttribute(k_adj_ingest_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  cudaFuncSetAttribute(k_adj_polar2lp_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  cudaFuncSetAttribute(k_adj_lpcols_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+}
+
+cudaError_t configure_p2_kernels(int optin) {
+  set_p2_attrs<256>(optin);
+  set_p2_attrs<512>(optin);
+  set_p2_attrs<1024>(optin);
+  set_p2_attrs<2048>(optin);
+  set_p2_attrs<4096>(optin);
+  set_p2_attrs<8192>(optin);
+  return cudaGetLastError();
+}
+
+bool p2_fwd_c2lp(const FwdC2LPArgs& a, int S, cudaStream_t st, cudaError_t* err) {
+  const int L = a.Nrho;
+  if (!p2_ok(L)) return false;
+#define CALL(LL)                                                                              \
+  {                                                                                           \
+    const size_t sm = (size_t)P2<LL>::NSIG * P2<LL>::SLOTS * sizeof(float2);                 \
+    if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; }   \
+    dim3 grid(S, (a.Nth / 2 + P2<LL>::NSIG - 1) / P2<LL>::NSIG);                               \
+    k_fwd_c2lp_p2<LL><<<grid, P2<LL>::BLOCK, sm, st>>>(a);                                    \
+  }
+  switch (L) { case 256: CALL(256) break; case 512: CALL(512) break; case 1024: CALL(1024) break;
+               case 2048: CALL(2048) break; case 4096: CALL(4096) break; case 8192: CALL(8192) break; }
+#undef CALL
+  *err = cudaGetLastError();
+  return true;
+}
+
+bool p2_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st, cudaError_t* err) {
+  const int L = a.Nth;
+  if (!p2_ok(L)) return false;
+#define CALL(LL)                                                                              \
+  {                                                                                           \
+    const size_t sm = (size_t)P2<LL>::NSIG * P2<LL>::SLOTS * sizeof(float2);                 \
+    if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; }   \
+    dim3 grid(S, (a.Nk + P2<LL>::NSIG - 1) / P2<LL>::NSIG);                                    \
+    k_theta_conv_p2<LL><<<grid, P2<LL>::BLOCK, sm, st>>>(a);                                  \
+  }
+  switch (L) { case 256: CALL(256) break; case 512: CALL(512) break; case 1024: CALL(1024) break;
+               case 2048: CALL(2048) break; case 4096: CALL(4096) break; case 8192: CALL(8192) break; }
+#undef CALL
+  *err = cudaGetLastError();
+  return true;
+}
+
+bool p2_fwd_lp2polar(const FwdLP2PolarArgs& a, int S, cudaStream_t st, cudaError_t* err) {
+  const int L = a.Nrho;
+  if (!p2_ok(L)) return false;
+  if (a.nrows <= 0) { *err = cudaSuccess; return true; }
+#define CALL(LL)                                                                              \
+  {                                                                                           \
+    const size_t sm = (size_t)P2<LL>::NSIG * P2<LL>::SLOTS * sizeof(float2);                 \
+    if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; }   \
+    const int pairs = (a.nrows + 1) / 2;                                                      \
+    dim3 grid(S, (pairs + P2<LL>::NSIG - 1) / P2<LL>::NSIG);                                   \
+    k_fwd_lp2polar_p2<LL><<<grid, P2<LL>::BLOCK, sm, st>>>(a);                                \
+  }
+  switch (L) { case 256: CALL(256) break; case 512: CALL(512) break; case 1024: CALL(1024) break;
+               case 2048: CALL(2048) break; case 4096: CALL(4096) break; case 8192: CALL(8192) break; }
+#undef CALL
+  *err = cudaGetLastError();
+  return true;
+}
+
+bool p2_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st, cudaError_t* err) {
+  const int L = 2 * a.N;
+  if (!p2_ok(L) || L < 1024) return false;  // needs T = L/16 >= 64 threads per row pair
+#define CALL(LL)                                                                              \
+  {                                                                                           \
+    const size_t sm = (a.H ? (size_t)P2<LL>::SLOTS * sizeof(float2) : 0) + 4 * (size_t)(LL / 2) * sizeof(float); \
+    if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; }   \
+    dim3 grid(S, (a.Nproj0 + 1) / 2);                                                         \
+    k_adj_ingest_p2<LL><<<grid, P2<LL>::T, sm, st>>>(a);                                      \
+  }
+  switch (L) { case 1024: CALL(1024) break; case 2048: CALL(2048) break; case 4096: CALL(4096) break;
+               case 8192: CALL(8192) break; default: return false; }
+#undef CALL
+  *err = cudaGetLastError();
+  return true;
+}
+
+bool p2_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st, cudaError_t* err) {
+  const int L = a.Nrho;
+  if (!p2_ok(L)) return false;
+  if (a.chi < a.clo) { *err = cudaSuccess; return true; }
+#define CALL(LL)                                                                              \
+  {                                                                                           \
+    const size_t sm = (size_t)P2<LL>::NSIG * (P2<LL>::SLOTS * sizeof(float2) + (size_t)LL * sizeof(float)); \
+    if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; }   \
+    const int pairs = (a.chi - a.clo + 2) / 2;                                                \
+    dim3 grid(S, (pairs + P2<LL>::NSIG - 1) / P2<LL>::NSIG);                                   \
+    k_adj_polar2lp_p2<LL><<<grid, P2<LL>::BLOCK, sm, st>>>(a);                                \
+  }
+  switch (L) { case 256: CALL(256) break; case 512: CALL(512) break; case 1024: CALL(1024) break;
+               case 2048: CALL(2048) break; case 4096: CALL(4096) break; case 8192: CALL(8192) break; }
+#undef CALL
+  *err = cudaGetLastError();
+  return true;
+}
+
+bool p2_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st, cudaError_t* err) {
+  const int L = a.Nrho;
+  if (!p2_ok(L)) return false;
+#define CALL(LL)                                                                              \
+  {                                                                                           \
+    const size_t sm = (size_t)P2<LL>::NSIG * P2<LL>::SLOTS * sizeof(float2);                 \
+    if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; }   \
+    const int pairs = (a.hi2 - a.lo2 + 2) / 2;                                                \
+    dim3 grid(S, (pairs + P2<LL>::NSIG - 1) / P2<LL>::NSIG);                                   \
+    k_adj_lpcols_p2<LL><<<grid, P2<LL>::BLOCK, sm, st>>>(a);                                  \
+  }
+  switch (L) { case 256: CALL(256) break; case 512: CALL(512) break; case 1024: CALL(1024) break;
+               case 2048: CALL(2048) break; case 4096: CALL(4096) break; case 8192: CALL(8192) break; }
+#undef CALL
+  *err = cudaGetLastError();
+  return true;
 }
 
 }  // namespace lpgb

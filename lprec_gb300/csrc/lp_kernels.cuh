@@ -54,9 +54,9 @@ struct FwdLP2PolarArgs {      // inverse FFT along rho of theta-combined columns
 struct AdjIngestArgs {        // cor shift, angle step, edge padding, FBP filter, row prefilter
   const float* Rin;           // [S][Nproj0][N0]
   float* rbuf;                // [S][Nproj][N]
-  const float* H;             // [4N] filter in FFT order, or null
+  const float* H;             // [2N] real filter spectrum for a 2N circular convolution, / 2N; or null
   int N, N0, Nproj, Nproj0, os, cor_off, cubic;
-  FFTPlan plan;               // length 4N (filter)
+  FFTPlan plan;               // length 2N (filter)
 };
 
 struct AdjPolar2LPArgs {      // polar -> log-polar gather (+ wrap points), FFT along rho
@@ -101,5 +101,7 @@ cudaError_t launch_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st
 cudaError_t launch_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st);
 cudaError_t launch_adj_lp2cart(const AdjLP2CartArgs& a, int S, cudaStream_t st);
 cudaError_t configure_kernels(int N);
+// false: always use the generic (any-size) FFT kernels
+void set_use_p2(bool on);
 
 }  // namespace lpgb

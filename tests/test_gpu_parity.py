@@ -153,3 +153,20 @@ def test_deterministic(torch_cuda):
     f, R = _inputs(G, 2, 9)
     assert np.array_equal(_fwd(torch_cuda, h, f), _fwd(torch_cuda, h, f))
     assert np.array_equal(_adj(torch_cuda, h, R), _adj(torch_cuda, h, R))
+
+
+@pytest.mark.parametrize("args", [(512, 768, 'cubic', 'shepp-logan', 256, 2), (1024, 1536, 'linear', 'hann', 512, 1),
+                                  (2048, 3000, 'cubic', 'shepp-logan', 1024, 1)])
+def test_large_sizes(torch_cuda, args):
+    """Power-of-two sizes served by the register-FFT kernels, including N=2048."""
+    from lprec_gb300 import _lib
+    N0, Nproj, interp, filt, cor, S = args
+    packed = _lib.precompute(N0, Nproj, S, cor, interp, filt, precision='fp64')
+    h = _handle(packed)
+    tr = O.Transform.from_packed(*packed)
+    rng = np.random.default_rng(21)
+    f = np.stack([O.ellipse_phantom(N0, 10, rng) for _ in range(S)])
+    Rg = _fwd(torch_cuda, h, f)
+    assert O.rel_l2(Rg, tr.fwd(f)) < TOL
+    Rn = Rg + 0.01 * np.abs(Rg).max() * rng.standard_normal(Rg.shape)
+    assert O.rel_l2(_adj(torch_cuda, h, Rn), tr.adj(Rn)) < TOL
