@@ -97,6 +97,13 @@ struct FwdDev {
   DevBuf<float2> fz;       // [Nk][Nth]
   int lo = 0, hi = 0;      // theta columns the polar gather reads
   DevBuf<float> fbuf;      // [Nslices][N][N]
+  // cubic mode: the prefiltered image of each slice as a 2-D CUDA array that
+  // the Cartesian -> log-polar gather reads with texture gathers
+  std::vector<cudaArray_t> arr;
+  std::vector<cudaTextureObject_t> tex_h;
+  std::vector<cudaSurfaceObject_t> surf_h;
+  DevBuf<cudaTextureObject_t> tex;
+  DevBuf<cudaSurfaceObject_t> surf;
 };
 
 struct AdjDev {
@@ -164,6 +171,11 @@ static void free_fwd(FwdDev* f) {
   f->rhoc.free_();
   f->fz.free_();
   f->fbuf.free_();
+  for (cudaTextureObject_t t : f->tex_h) cudaDestroyTextureObject(t);
+  for (cudaSurfaceObject_t t : f->surf_h) cudaDestroySurfaceObject(t);
+  for (cudaArray_t a : f->arr) cudaFreeArray(a);
+  f->tex.free_();
+  f->surf.free_();
   delete f;
 }
 
@@ -220,6 +232,46 @@ static std::vector<float2> extend_kernel(const float* v, int Nrho, int Nth) {
 }
 
 static bool finite_coord(float v, float lim) { return isfinite(v) && fabsf(v) < lim; }
+
+// One N x N float array per slice, written through a surface by the column
+// prefilter and read through a gather texture (normalised, wrap on both axes)
+// by the Cartesian -> log-polar gather.  Skipped (left empty) when the device
+// cannot gather from textures that large.
+static cudaError_t make_slice_textures(FwdDev* F, int S, int N, int device) {
+  int gw = 0, gh = 0;
+  cudaDeviceGetAttribute(&gw, cudaDevAttrMaxTexture2DGatherWidth, device);
+  cudaDeviceGetAttribute(&gh, cudaDevAttrMaxTexture2DGatherHeight, device);
+  if (N > gw || N > gh) return cudaSuccess;
+  cudaChannelFormatDesc fd = cudaCreateChannelDesc<float>();
+  for (int s = 0; s < S; ++s) {
+    cudaArray_t a = nullptr;
+    cudaError_t e = cudaMallocArray(&a, &fd, N, N, cudaArrayTextureGather | cudaArraySurfaceLoadStore);
+    if (e != cudaSuccess) return e;
+    F->arr.push_back(a);
+    cudaResourceDesc rd;
+    memset(&rd, 0, sizeof(rd));
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = a;
+    cudaTextureDesc td;
+    memset(&td, 0, sizeof(td));
+    td.addressMode[0] = cudaAddressModeWrap;
+    td.addressMode[1] = cudaAddressModeWrap;
+    td.filterMode = cudaFilterModePoint;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 1;
+    cudaTextureObject_t t = 0;
+    e = cudaCreateTextureObject(&t, &rd, &td, nullptr);
+    if (e != cudaSuccess) return e;
+    F->tex_h.push_back(t);
+    cudaSurfaceObject_t so = 0;
+    e = cudaCreateSurfaceObject(&so, &rd);
+    if (e != cudaSuccess) return e;
+    F->surf_h.push_back(so);
+  }
+  cudaError_t e = dev_upload(F->tex, F->tex_h);
+  if (e == cudaSuccess) e = dev_upload(F->surf, F->surf_h);
+  return e;
+}
 
 // W[t] = exp(-2 pi i t / L), evaluated in float64
 static std::vector<float2> twiddles(int L) {
@@ -495,6 +547,7 @@ int lp_init_fwd(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
     }
     if (e == cudaSuccess) e = dev_upload(F->fz, extend_kernel(fzv, Nrho, Nth));
     if (e == cudaSuccess) e = dev_alloc(F->fbuf, (size_t)h->Nslices * N * N);
+    if (e == cudaSuccess && h->cubic) e = make_slice_textures(F, h->Nslices, N, h->device);
     if (e != cudaSuccess) {
       free_fwd(F);
       return set_err(e == cudaErrorMemoryAllocation ? LP_ERR_OOM : LP_ERR_CUDA, "lp_init_fwd: %s",
@@ -682,15 +735,16 @@ int lp_fwd(lp_handle* h, float* R, const float* f, int S0, void* stream) {
   DeviceGuard g(h->device);
   cudaStream_t st = (cudaStream_t)stream;
   FwdDev* F = h->fwd;
+  const bool tex = !F->tex_h.empty();
   FwdIngestArgs ia{f, F->fbuf.p, h->N, h->N0, h->N / 2 - h->N0 / 2, h->cubic};
   CUDA_TRY(launch(h, K_FWD_INGEST, st, [&] { return launch_fwd_ingest(ia, S0, st); }));
   if (h->cubic) {
-    ColPrefilterArgs ca{F->fbuf.p, h->N, h->N};
+    ColPrefilterArgs ca{F->fbuf.p, h->N, h->N, tex ? F->surf.p : nullptr};
     CUDA_TRY(launch(h, K_COL_PREFILTER, st, [&] { return launch_col_prefilter(ca, S0, st); }));
   }
   for (int k = 0; k < 3; ++k) {
     FwdC2LPArgs a1{F->fbuf.p, h->spec.p, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, h->cubic,
-                   h->plan_rho};
+                   h->plan_rho, tex ? F->tex.p : nullptr};
     CUDA_TRY(launch(h, K_FWD_C2LP, st, [&] { return launch_fwd_c2lp(a1, S0, st); }));
     ThetaConvArgs a2{h->spec.p, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), 0, h->Nth - 1,
                      F->lo, F->hi, 0, h->plan_th};

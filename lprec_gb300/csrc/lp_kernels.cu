@@ -62,24 +62,6 @@ __device__ __forceinline__ float interp2d(const float* __restrict__ img, int W, 
       for (int i = 0; i < 4; ++i) cx[i] = wrapi(ix - 1 + i, W);
     }
     float acc = 0.f;
-    const int b4 = (ix - 1) & ~3;
-    if ((W & 3) == 0 && ix >= 1 && b4 + 8 <= W) {
-      // the four taps lie in two aligned float4 of the row
-      const int o = ix - 1 - b4;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const float* row = img + (size_t)wrapi(iy - 1 + j, H) * W + b4;
-        const float4 p = __ldg(reinterpret_cast<const float4*>(row));
-        const float4 q = __ldg(reinterpret_cast<const float4*>(row) + 1);
-        float t0, t1, t2, t3;
-        if (o == 0) { t0 = p.x; t1 = p.y; t2 = p.z; t3 = p.w; }
-        else if (o == 1) { t0 = p.y; t1 = p.z; t2 = p.w; t3 = q.x; }
-        else if (o == 2) { t0 = p.z; t1 = p.w; t2 = q.x; t3 = q.y; }
-        else { t0 = p.w; t1 = q.x; t2 = q.y; t3 = q.z; }
-        acc += wy[j] * (wx[0] * t0 + wx[1] * t1 + wx[2] * t2 + wx[3] * t3);
-      }
-      return acc;
-    }
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const float* row = img + (size_t)wrapi(iy - 1 + j, H) * W;
@@ -94,6 +76,32 @@ __device__ __forceinline__ float interp2d(const float* __restrict__ img, int W, 
   const float* r1 = img + (size_t)wrapi(iy + 1, H) * W;
   return (1.f - ay) * ((1.f - ax) * __ldg(r0 + x0) + ax * __ldg(r0 + x1)) +
          ay * ((1.f - ax) * __ldg(r1 + x0) + ax * __ldg(r1 + x1));
+}
+
+// Cubic B-spline sample of a 2-D texture (N x N texels, normalised
+// coordinates, wrap addressing) at index position (x, y) from four 2x2
+// texel gathers.  A gather at integer texel coordinate (i, j) returns the
+// raw texels of columns i-1, i and rows j-1, j -- no filtering weights are
+// involved, the B-spline weights are applied here in float32.  The 0.5-texel
+// margin of the integer position makes the quad selection insensitive to
+// coordinate rounding.  Gather component order: w (i-1, j-1), z (i, j-1),
+// x (i-1, j), y (i, j).
+__device__ __forceinline__ float interp_tex_cubic(cudaTextureObject_t tx, float invN, float x, float y) {
+  const float fx = floorf(x), fy = floorf(y);
+  float wx[4], wy[4];
+  bspline_w(x - fx, wx);
+  bspline_w(y - fy, wy);
+  const float u0 = fx * invN, u1 = (fx + 2.0f) * invN;
+  const float v0 = fy * invN, v1 = (fy + 2.0f) * invN;
+  const float4 q00 = tex2Dgather<float4>(tx, u0, v0, 0);
+  const float4 q10 = tex2Dgather<float4>(tx, u1, v0, 0);
+  const float4 q01 = tex2Dgather<float4>(tx, u0, v1, 0);
+  const float4 q11 = tex2Dgather<float4>(tx, u1, v1, 0);
+  const float r0 = wx[0] * q00.w + wx[1] * q00.z + wx[2] * q10.w + wx[3] * q10.z;
+  const float r1 = wx[0] * q00.x + wx[1] * q00.y + wx[2] * q10.x + wx[3] * q10.y;
+  const float r2 = wx[0] * q01.w + wx[1] * q01.z + wx[2] * q11.w + wx[3] * q11.z;
+  const float r3 = wx[0] * q01.x + wx[1] * q01.y + wx[2] * q11.x + wx[3] * q11.y;
+  return wy[0] * r0 + wy[1] * r1 + wy[2] * r2 + wy[3] * r3;
 }
 
 // 1-D interpolation along a shared-memory line of length L (wrap).
@@ -290,12 +298,14 @@ __global__ void k_col_prefilter(ColPrefilterArgs a) {
   if (active) {
     float c;
     int n;
+    const cudaSurfaceObject_t so = a.surf ? a.surf[s] : 0;
     if (e + nw >= H) {
       // exact anticausal initialisation at H-1
       float last = (nw > 0) ? wu[nw - 1] : col[(size_t)(H - 1) * W];
       c = (z / (z - 1.0f)) * last;
       if (nw == 0) {
-        col[(size_t)(H - 1) * W] = c;
+        if (a.surf) surf2Dwrite(c, so, x * (int)sizeof(float), H - 1);
+        else col[(size_t)(H - 1) * W] = c;
         n = H - 2;
       } else {
         for (int i = nw - 2; i >= 0; --i) c = z * (c - wu[i]);
@@ -308,7 +318,8 @@ __global__ void k_col_prefilter(ColPrefilterArgs a) {
     }
     for (; n >= b; --n) {
       c = z * (c - col[(size_t)n * W]);
-      col[(size_t)n * W] = c;
+      if (a.surf) surf2Dwrite(c, so, x * (int)sizeof(float), n);
+      else col[(size_t)n * W] = c;
     }
   }
 }
@@ -328,14 +339,19 @@ __global__ void __launch_bounds__(256, 2) k_fwd_c2lp(FwdC2LPArgs a) {
   const float* img = a.fbuf + (size_t)s * a.N * a.N;
   const float2* ca = a.c2lp + (size_t)th * a.Nrho;
   const float2* cb = a.c2lp + (size_t)max(thb, 0) * a.Nrho;
+  const bool use_tex = a.tex != nullptr;
+  const cudaTextureObject_t tx = use_tex ? a.tex[s] : 0;
+  const float invN = 1.0f / (float)a.N;
   for (int r = threadIdx.x; r < a.Nrho; r += blockDim.x) {
     const float e = __ldg(a.erho + r);
     const float2 pa = __ldg(ca + r);
     float va = 0.f, vb = 0.f;
-    if (!isnan(pa.x)) va = e * interp2d(img, a.N, a.N, pa.x, pa.y, a.cubic);
+    if (!isnan(pa.x))
+      va = e * (use_tex ? interp_tex_cubic(tx, invN, pa.x, pa.y) : interp2d(img, a.N, a.N, pa.x, pa.y, a.cubic));
     if (thb >= 0) {
       const float2 pb = __ldg(cb + r);
-      if (!isnan(pb.x)) vb = e * interp2d(img, a.N, a.N, pb.x, pb.y, a.cubic);
+      if (!isnan(pb.x))
+        vb = e * (use_tex ? interp_tex_cubic(tx, invN, pb.x, pb.y) : interp2d(img, a.N, a.N, pb.x, pb.y, a.cubic));
     }
     A.set(r, make_float2(va, vb));
   }
@@ -637,8 +653,6 @@ __device__ __forceinline__ float interp_cols(const float* __restrict__ G, int Nr
   const int ct = axis_weights(t.x, cubic, wt);
   const int cr = axis_weights(t.y, cubic, wr);
   const int nt = cubic ? 4 : 2;
-  const int b4 = cr & ~3;
-  const bool vec = cubic && (Nrho & 3) == 0 && cr >= 0 && b4 + 8 <= Nrho;
   int rr[4];
   const bool inner = (cr >= 0 && cr + 3 < Nrho);
 #pragma unroll
@@ -649,22 +663,9 @@ __device__ __forceinline__ float interp_cols(const float* __restrict__ G, int Nr
     if (col < 0 || col >= W2) continue;  // outside the stored band: zero weight by construction
     const float* g = G + (size_t)col * Nrho;
     float v = 0.f;
-    if (vec) {
-      // the four rho taps lie in two aligned float4 of the column
-      const float4 p = __ldg(reinterpret_cast<const float4*>(g + b4));
-      const float4 q = __ldg(reinterpret_cast<const float4*>(g + b4) + 1);
-      const int o = cr - b4;
-      float t0, t1, t2, t3;
-      if (o == 0) { t0 = p.x; t1 = p.y; t2 = p.z; t3 = p.w; }
-      else if (o == 1) { t0 = p.y; t1 = p.z; t2 = p.w; t3 = q.x; }
-      else if (o == 2) { t0 = p.z; t1 = p.w; t2 = q.x; t3 = q.y; }
-      else { t0 = p.w; t1 = q.x; t2 = q.y; t3 = q.z; }
-      v = wr[0] * t0 + wr[1] * t1 + wr[2] * t2 + wr[3] * t3;
-    } else {
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
-        if (i < nt) v += wr[i] * __ldg(g + rr[i]);
-    }
+    for (int i = 0; i < 4; ++i)
+      if (i < nt) v += wr[i] * __ldg(g + rr[i]);
     acc += wt[j] * v;
   }
   return acc;
@@ -846,6 +847,9 @@ __global__ void __launch_bounds__(256, 2) k_fwd_c2lp_p2(FwdC2LPArgs a) {
   const float* img = a.fbuf + (size_t)s * a.N * a.N;
   const float2* ca = a.c2lp + (size_t)(live ? th : 0) * L;
   const float2* cb = a.c2lp + (size_t)max(thb, 0) * L;
+  const bool use_tex = a.tex != nullptr;
+  const cudaTextureObject_t tx = use_tex ? a.tex[s] : 0;
+  const float invN = 1.0f / (float)a.N;
   float2 v[16];
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
@@ -854,10 +858,13 @@ __global__ void __launch_bounds__(256, 2) k_fwd_c2lp_p2(FwdC2LPArgs a) {
     if (live) {
       const float e = __ldg(a.erho + r);
       const float2 pa = __ldg(ca + r);
-      if (!isnan(pa.x)) va = e * interp2d(img, a.N, a.N, pa.x, pa.y, a.cubic);
+      if (!isnan(pa.x))
+        va = e * (use_tex ? interp_tex_cubic(tx, invN, pa.x, pa.y) : interp2d(img, a.N, a.N, pa.x, pa.y, a.cubic));
       if (thb >= 0) {
         const float2 pb = __ldg(cb + r);
-        if (!isnan(pb.x)) vb = e * interp2d(img, a.N, a.N, pb.x, pb.y, a.cubic);
+        if (!isnan(pb.x))
+          vb = e * (use_tex ? interp_tex_cubic(tx, invN, pb.x, pb.y)
+                            : interp2d(img, a.N, a.N, pb.x, pb.y, a.cubic));
       }
     }
     v[i] = make_float2(va, vb);

@@ -17,6 +17,7 @@ struct FwdIngestArgs {        // centre f into the padded grid, prefilter rows
 struct ColPrefilterArgs {     // prefilter along the slow axis, in place
   float* img;                 // [S][H][W]
   int H, W;
+  const cudaSurfaceObject_t* surf;  // if set: final coefficients go to these per-slice 2-D arrays instead
 };
 
 struct FwdC2LPArgs {          // Cartesian -> log-polar gather, e^rho, FFT along rho
@@ -26,6 +27,7 @@ struct FwdC2LPArgs {          // Cartesian -> log-polar gather, e^rho, FFT along
   const float* erho;          // [Nrho]
   int N, Nth, Nrho, Nk, cubic;
   FFTPlan plan;               // length Nrho
+  const cudaTextureObject_t* tex;  // if set: the prefiltered image per slice as a gather texture (cubic)
 };
 
 struct ThetaConvArgs {        // FFT along theta, multiply by the kernel, inverse
