@@ -158,6 +158,17 @@ __device__ __forceinline__ float* carve(float* sm, int L, int nfft, CBuf& a, CBu
 // exact to |pole|^16 ~ 7e-10; the first and last chunk use the reference's
 // boundary initialisations.  `cp` is scratch of L floats.
 // ---------------------------------------------------------------------------
+// Shared-memory position of sample p of a line processed in chunks of C:
+// one pad word per chunk makes the chunk stride odd, so the threads walking
+// their chunks in lockstep hit distinct banks.
+// (an odd chunk stride is conflict-free already and gets no pad)
+__device__ __forceinline__ int lpos(int p, int C) { return (C & 1) ? p : p + p / C; }
+// floats a line of L samples occupies when split over nth threads
+__host__ __device__ inline int line_floats(int L, int nth) {
+  const int C = (L + nth - 1) / nth;
+  return (C & 1) ? L : L + (L - 1) / C + 1;
+}
+
 __device__ void prefilter_line(float* line, float* cp, int L, int tid, int nth) {
   const float z = LP_POLE;
   const int C = (L + nth - 1) / nth;
@@ -169,22 +180,22 @@ __device__ void prefilter_line(float* line, float* cp, int L, int tid, int nth) 
     int n = 0;
     if (n0 <= 0) {
       const int hor = min(12, L);
-      float sum = line[0];
+      float sum = line[lpos(0, C)];
       float zn = z;
       for (int i = 0; i < hor; ++i) {
-        sum += zn * line[i];
+        sum += zn * line[lpos(i, C)];
         zn *= z;
       }
       prev = LP_LAMBDA * sum;
-      if (b == 0) cp[0] = prev;
+      if (b == 0) cp[lpos(0, C)] = prev;
       n = 1;
     } else {
-      prev = LP_LAMBDA * line[n0];
+      prev = LP_LAMBDA * line[lpos(n0, C)];
       n = n0 + 1;
     }
     for (; n < e; ++n) {
-      prev = LP_LAMBDA * line[n] + z * prev;
-      if (n >= b) cp[n] = prev;
+      prev = LP_LAMBDA * line[lpos(n, C)] + z * prev;
+      if (n >= b) cp[lpos(n, C)] = prev;
     }
   }
   __syncthreads();
@@ -193,16 +204,16 @@ __device__ void prefilter_line(float* line, float* cp, int L, int tid, int nth) 
     float c;
     int n;
     if (n1 >= L - 1) {
-      c = (z / (z - 1.0f)) * cp[L - 1];
-      if (L - 1 < e) line[L - 1] = c;
+      c = (z / (z - 1.0f)) * cp[lpos(L - 1, C)];
+      if (L - 1 < e) line[lpos(L - 1, C)] = c;
       n = L - 2;
     } else {
-      c = -z * cp[n1];
+      c = -z * cp[lpos(n1, C)];
       n = n1 - 1;
     }
     for (; n >= b; --n) {
-      c = z * (c - cp[n]);
-      if (n < e) line[n] = c;
+      c = z * (c - cp[lpos(n, C)]);
+      if (n < e) line[lpos(n, C)] = c;
     }
   }
   __syncthreads();
@@ -214,20 +225,21 @@ __device__ void prefilter_line(float* line, float* cp, int L, int tid, int nth) 
 // ---------------------------------------------------------------------------
 __global__ void k_fwd_ingest(FwdIngestArgs a) {
   extern __shared__ float smf[];
+  const int C = (a.N + blockDim.x - 1) / blockDim.x;
   float* line = smf;
-  float* cp = smf + a.N;
+  float* cp = smf + line_floats(a.N, blockDim.x);
   const int s = blockIdx.x;
   const int y = blockIdx.y;
   const int Y = y - a.off;
   const float* src = a.fin + ((size_t)s * a.N0 + (size_t)max(Y, 0)) * a.N0;
   for (int x = threadIdx.x; x < a.N; x += blockDim.x) {
     const int X = x - a.off;
-    line[x] = (Y >= 0 && Y < a.N0 && X >= 0 && X < a.N0) ? __ldg(src + X) : 0.f;
+    line[lpos(x, C)] = (Y >= 0 && Y < a.N0 && X >= 0 && X < a.N0) ? __ldg(src + X) : 0.f;
   }
   __syncthreads();
   if (a.cubic) prefilter_line(line, cp, a.N, threadIdx.x, blockDim.x);
   float* dst = a.fbuf + ((size_t)s * a.N + y) * a.N;
-  for (int x = threadIdx.x; x < a.N; x += blockDim.x) dst[x] = line[x];
+  for (int x = threadIdx.x; x < a.N; x += blockDim.x) dst[x] = line[lpos(x, C)];
 }
 
 // ---------------------------------------------------------------------------
@@ -492,8 +504,11 @@ __global__ void __launch_bounds__(256, 2) k_adj_ingest(AdjIngestArgs a) {
   const int M = 2 * N;  // the filter couples samples less than N apart: a 2N circular convolution is exact
   const bool filt = a.H != nullptr;
   CBuf F0, F1;
-  float* lines = filt ? carve(smf, M, 1, F0, F1) : smf;  // 2 rows
-  float* cp = lines + 2 * N;                             // 2 rows of scratch
+  float* lines = filt ? carve(smf, M, 1, F0, F1) : smf;  // 2 rows, chunked layout
+  const int half = blockDim.x / 2;
+  const int C = (N + half - 1) / half;
+  const int LF = line_floats(N, half);
+  float* cp = lines + 2 * LF;                            // 2 rows of scratch
   const int s = blockIdx.x;
   const int q0 = 2 * blockIdx.y;
   const int q1 = q0 + 1 < a.Nproj0 ? q0 + 1 : -1;
@@ -501,13 +516,13 @@ __global__ void __launch_bounds__(256, 2) k_adj_ingest(AdjIngestArgs a) {
   const float* in1 = a.Rin + ((size_t)s * a.Nproj0 + max(q1, 0)) * a.N0;
   for (int x = threadIdx.x; x < N; x += blockDim.x) {
     const int xi = min(max(x - a.cor_off, 0), a.N0 - 1);
-    lines[x] = __ldg(in0 + xi);
-    lines[N + x] = q1 >= 0 ? __ldg(in1 + xi) : 0.f;
+    lines[lpos(x, C)] = __ldg(in0 + xi);
+    lines[LF + lpos(x, C)] = q1 >= 0 ? __ldg(in1 + xi) : 0.f;
   }
   __syncthreads();
   if (filt) {
     for (int x = threadIdx.x; x < M; x += blockDim.x)
-      F0.set(x, x < N ? make_float2(lines[x], lines[N + x]) : make_float2(0.f, 0.f));
+      F0.set(x, x < N ? make_float2(lines[lpos(x, C)], lines[LF + lpos(x, C)]) : make_float2(0.f, 0.f));
     __syncthreads();
     const CBuf X = fft_block<-1>(F0, F1, a.plan, 1, 0);
     for (int k = threadIdx.x; k < M; k += blockDim.x) X.set(k, cscale(X.get(k), __ldg(a.H + k)));
@@ -515,25 +530,24 @@ __global__ void __launch_bounds__(256, 2) k_adj_ingest(AdjIngestArgs a) {
     const CBuf Y = fft_block<1>(X, X.re == F0.re ? F1 : F0, a.plan, 1, 0);
     for (int x = threadIdx.x; x < N; x += blockDim.x) {
       const float2 y = Y.get(x);
-      lines[x] = y.x;
-      lines[N + x] = y.y;
+      lines[lpos(x, C)] = y.x;
+      lines[LF + lpos(x, C)] = y.y;
     }
     __syncthreads();
   }
   if (a.cubic) {
     // two lines at once: half of the block each
-    const int half = blockDim.x / 2;
     const int which = threadIdx.x >= half;
     const int tid = threadIdx.x - which * half;
     // prefilter_line synchronises the whole block; both halves call it together
-    prefilter_line(lines + which * N, cp + which * N, N, tid, half);
+    prefilter_line(lines + which * LF, cp + which * LF, N, tid, half);
   }
   for (int rr = 0; rr < 2; ++rr) {
     const int q = rr == 0 ? q0 : q1;
     if (q < 0) break;
     for (int j = 0; j < a.os; ++j) {
       float* dst = a.rbuf + ((size_t)s * a.Nproj + (size_t)q * a.os + j) * N;
-      for (int x = threadIdx.x; x < N; x += blockDim.x) dst[x] = j == 0 ? lines[rr * N + x] : 0.f;
+      for (int x = threadIdx.x; x < N; x += blockDim.x) dst[x] = j == 0 ? lines[rr * LF + lpos(x, C)] : 0.f;
     }
   }
 }
@@ -657,9 +671,10 @@ __device__ __forceinline__ float interp_cols(const float* __restrict__ G, int Nr
   const bool inner = (cr >= 0 && cr + 3 < Nrho);
 #pragma unroll
   for (int i = 0; i < 4; ++i) rr[i] = inner ? cr + i : wrapi(cr + i, Nrho);
+  const bool tin = ct >= 0 && ct + 3 < Nth;
   float acc = 0.f;
   for (int j = 0; j < nt; ++j) {
-    const int col = wrapi(ct + j, Nth) - lo2;
+    const int col = (tin ? ct + j : wrapi(ct + j, Nth)) - lo2;
     if (col < 0 || col >= W2) continue;  // outside the stored band: zero weight by construction
     const float* g = G + (size_t)col * Nrho;
     float v = 0.f;
@@ -695,7 +710,7 @@ static size_t fft_bytes(int L, int nfft) { return 4 * (size_t)nfft * fft_plane_f
 static size_t smem_c2lp(int Nrho) { return fft_bytes(Nrho, 1); }
 static size_t smem_theta(int Nth) { return fft_bytes(Nth, 2); }
 static size_t smem_adj_ingest(int N, bool filt) {
-  return (filt ? fft_bytes(2 * N, 1) : 0) + 4 * (size_t)N * sizeof(float);
+  return (filt ? fft_bytes(2 * N, 1) : 0) + 4 * (size_t)line_floats(N, 128) * sizeof(float);
 }
 static size_t smem_polar2lp(int Nrho, int N) { return fft_bytes(Nrho, 1) + 2 * (size_t)N * sizeof(float); }
 
@@ -738,9 +753,10 @@ static cudaError_t smem_ok(size_t need) {
 }
 
 cudaError_t launch_fwd_ingest(const FwdIngestArgs& a, int S, cudaStream_t st) {
-  if (smem_ok(2 * (size_t)a.N * sizeof(float)) != cudaSuccess) return cudaErrorInvalidConfiguration;
+  const size_t sm = 2 * (size_t)line_floats(a.N, 128) * sizeof(float);
+  if (smem_ok(sm) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, a.N);
-  k_fwd_ingest<<<grid, 128, 2 * (size_t)a.N * sizeof(float), st>>>(a);
+  k_fwd_ingest<<<grid, 128, sm, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -835,7 +851,7 @@ struct P2 {
 
 // forward, per span: Cartesian -> log-polar gather for column pairs, e^rho, FFT along rho
 template <int L>
-__global__ void __launch_bounds__(256, 2) k_fwd_c2lp_p2(FwdC2LPArgs a) {
+__global__ void __launch_bounds__(256, 3) k_fwd_c2lp_p2(FwdC2LPArgs a) {
   extern __shared__ float2 sm2[];
   constexpr int T = P2<L>::T;
   const int sig = threadIdx.x / T, t = threadIdx.x % T;
@@ -926,7 +942,7 @@ __device__ __forceinline__ float2 pair_elem(int p, int L, float2 v0, float2 v1) 
 // forward, per span: two angle rows per signal, theta taps combined in frequency,
 // inverse FFT along rho, rho interpolation into the caller's sinogram
 template <int L>
-__global__ void __launch_bounds__(256, 2) k_fwd_lp2polar_p2(FwdLP2PolarArgs a) {
+__global__ void __launch_bounds__(256, 3) k_fwd_lp2polar_p2(FwdLP2PolarArgs a) {
   extern __shared__ float2 sm2[];
   constexpr int T = P2<L>::T;
   const int sig = threadIdx.x / T, t = threadIdx.x % T;
@@ -1022,8 +1038,11 @@ __global__ void __launch_bounds__(256, 2) k_adj_ingest_p2(AdjIngestArgs a) {
   const int N = L / 2;
   const bool filt = a.H != nullptr;
   float2* sm = sm2;
-  float* lines = reinterpret_cast<float*>(sm2 + (filt ? P2<L>::SLOTS : 0));  // 2 rows
-  float* cp = lines + 2 * N;
+  const int half = T / 2;
+  const int C = (N + half - 1) / half;
+  const int LF = line_floats(N, half);
+  float* lines = reinterpret_cast<float*>(sm2 + (filt ? P2<L>::SLOTS : 0));  // 2 rows, chunked layout
+  float* cp = lines + 2 * LF;
   const int t = threadIdx.x;
   const int s = blockIdx.x;
   const int q0 = 2 * blockIdx.y;
@@ -1048,35 +1067,34 @@ __global__ void __launch_bounds__(256, 2) k_adj_ingest_p2(AdjIngestArgs a) {
     reg_fft<L, 1>(v, sm, t);
     for (int x = t; x < N; x += T) {
       const float2 y = sm[spad(x)];
-      lines[x] = y.x;
-      lines[N + x] = y.y;
+      lines[lpos(x, C)] = y.x;
+      lines[LF + lpos(x, C)] = y.y;
     }
   } else {
     for (int x = t; x < N; x += T) {
       const int xi = min(max(x - a.cor_off, 0), a.N0 - 1);
-      lines[x] = __ldg(in0 + xi);
-      lines[N + x] = q1 >= 0 ? __ldg(in1 + xi) : 0.f;
+      lines[lpos(x, C)] = __ldg(in0 + xi);
+      lines[LF + lpos(x, C)] = q1 >= 0 ? __ldg(in1 + xi) : 0.f;
     }
   }
   __syncthreads();
   if (a.cubic) {
-    const int half = T / 2;
     const int which = t >= half;
-    prefilter_line(lines + which * N, cp + which * N, N, t - which * half, half);
+    prefilter_line(lines + which * LF, cp + which * LF, N, t - which * half, half);
   }
   for (int rr = 0; rr < 2; ++rr) {
     const int q = rr == 0 ? q0 : q1;
     if (q < 0) break;
     for (int j = 0; j < a.os; ++j) {
       float* dst = a.rbuf + ((size_t)s * a.Nproj + (size_t)q * a.os + j) * N;
-      for (int x = t; x < N; x += T) dst[x] = j == 0 ? lines[rr * N + x] : 0.f;
+      for (int x = t; x < N; x += T) dst[x] = j == 0 ? lines[rr * LF + lpos(x, C)] : 0.f;
     }
   }
 }
 
 // adjoint, per span: polar -> log-polar for a column pair per signal, FFT along rho
 template <int L>
-__global__ void __launch_bounds__(256, 2) k_adj_polar2lp_p2(AdjPolar2LPArgs a) {
+__global__ void __launch_bounds__(256, 3) k_adj_polar2lp_p2(AdjPolar2LPArgs a) {
   extern __shared__ float2 sm2[];
   constexpr int T = P2<L>::T;
   const int N = L / 2;
@@ -1167,7 +1185,7 @@ __global__ void __launch_bounds__(256, 2) k_adj_polar2lp_p2(AdjPolar2LPArgs a) {
 
 // adjoint, per span: inverse FFT along rho for a column pair per signal
 template <int L>
-__global__ void __launch_bounds__(256, 2) k_adj_lpcols_p2(AdjLPColsArgs a) {
+__global__ void __launch_bounds__(256, 3) k_adj_lpcols_p2(AdjLPColsArgs a) {
   extern __shared__ float2 sm2[];
   constexpr int T = P2<L>::T;
   const int sig = threadIdx.x / T, t = threadIdx.x % T;
@@ -1287,7 +1305,7 @@ bool p2_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st, cudaError_t* 
   if (!p2_ok(L) || L < 1024) return false;  // needs T = L/16 >= 64 threads per row pair
 #define CALL(LL)                                                                              \
   {                                                                                           \
-    const size_t sm = (a.H ? (size_t)P2<LL>::SLOTS * sizeof(float2) : 0) + 4 * (size_t)(LL / 2) * sizeof(float); \
+    const size_t sm = (a.H ? (size_t)P2<LL>::SLOTS * sizeof(float2) : 0) + 4 * (size_t)line_floats(LL / 2, P2<LL>::T / 2) * sizeof(float); \
     if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; }   \
     dim3 grid(S, (a.Nproj0 + 1) / 2);                                                         \
     k_adj_ingest_p2<LL><<<grid, P2<LL>::T, sm, st>>>(a);                                      \

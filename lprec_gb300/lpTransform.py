@@ -136,22 +136,84 @@ class lpTransform:
                 raise ValueError("adjp: arrays live on cuda:%d, handle on cuda:%d" % (d, gpu))
         h.adj(fp, Rp, S0, _stream(gpu))
 
-    # ---- host-array conveniences -------------------------------------------
-    def fwd(self, f, gpu=0):
+    # ---- host arrays, pipelined ---------------------------------------------
+    def _host_op(self, op, x, out, gpu, chunk):
+        """Run fwdp/adjp over host arrays in slice chunks, overlapping the
+        host->device copy of chunk i+1 and the device->host copy of chunk i-1
+        with the transform of chunk i (three streams, events between them)."""
         import torch
         h = self._handle(gpu)
-        ft = torch.as_tensor(np.ascontiguousarray(f, dtype=np.float32)).cuda(gpu)
-        R = torch.empty((ft.shape[0], h.Nproj, h.N0), dtype=torch.float32, device=ft.device)
-        self.fwdp(R, ft, gpu)
-        return R.cpu().numpy()
+        dev = torch.device("cuda", gpu)
+        as_numpy = not isinstance(x, torch.Tensor)
+        xt = torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)) if as_numpy else x
+        if xt.dtype != torch.float32 or xt.device.type != "cpu":
+            raise ValueError("expected a float32 host array")
+        xt = xt.contiguous()
+        S = xt.shape[0]
+        oshape = (S, h.Nproj, h.N0) if op == "fwd" else (S, h.N0, h.N0)
+        if out is None:
+            out = torch.empty(oshape, dtype=torch.float32, pin_memory=torch.cuda.is_available())
+        elif not isinstance(out, torch.Tensor):
+            raise TypeError("out must be a torch CPU tensor")
+        if tuple(out.shape) != oshape:
+            raise ValueError("out has shape %s, expected %s" % (tuple(out.shape), oshape))
+        c = max(1, min(int(chunk or 16), h.Nslices, S))
+        key = (op, gpu, c) + tuple(xt.shape[1:])
+        bufs = self._pipe_bufs.get(key) if hasattr(self, "_pipe_bufs") else None
+        if bufs is None:
+            if not hasattr(self, "_pipe_bufs"):
+                self._pipe_bufs = {}
+            bufs = ([torch.empty((c,) + tuple(xt.shape[1:]), dtype=torch.float32, device=dev) for _ in range(2)],
+                    [torch.empty((c,) + oshape[1:], dtype=torch.float32, device=dev) for _ in range(2)],
+                    torch.cuda.Stream(dev), torch.cuda.Stream(dev))
+            self._pipe_bufs[key] = bufs
+        ins, outs, s_in, s_out = bufs
+        comp = torch.cuda.current_stream(dev)
+        done_comp = [None, None]
+        done_out = [None, None]
+        n = (S + c - 1) // c
+        for i in range(n):
+            a, b = i * c, min(S, (i + 1) * c)
+            k = i % 2
+            with torch.cuda.stream(s_in):
+                if done_comp[k] is not None:
+                    s_in.wait_event(done_comp[k])       # buffer's previous chunk consumed
+                ins[k][:b - a].copy_(xt[a:b], non_blocking=True)
+                ev_in = torch.cuda.Event()
+                ev_in.record(s_in)
+            comp.wait_event(ev_in)
+            if done_out[k] is not None:
+                comp.wait_event(done_out[k])            # output buffer drained
+            if op == "fwd":
+                self.fwdp(outs[k][:b - a], ins[k][:b - a], gpu)
+            else:
+                self.adjp(outs[k][:b - a], ins[k][:b - a], gpu)
+            ev_c = torch.cuda.Event()
+            ev_c.record(comp)
+            done_comp[k] = ev_c
+            with torch.cuda.stream(s_out):
+                s_out.wait_event(ev_c)
+                out[a:b].copy_(outs[k][:b - a], non_blocking=True)
+                ev_o = torch.cuda.Event()
+                ev_o.record(s_out)
+            done_out[k] = ev_o
+        for e in done_out:
+            if e is not None:
+                comp.wait_event(e)
+        if as_numpy:
+            torch.cuda.current_stream(dev).synchronize()
+            return out.numpy()
+        return out
 
-    def adj(self, R, gpu=0):
-        import torch
-        h = self._handle(gpu)
-        Rt = torch.as_tensor(np.ascontiguousarray(R, dtype=np.float32)).cuda(gpu)
-        f = torch.empty((Rt.shape[0], h.N0, h.N0), dtype=torch.float32, device=Rt.device)
-        self.adjp(f, Rt, gpu)
-        return f.cpu().numpy()
+    def fwd(self, f, gpu=0, out=None, chunk=None):
+        """Forward transform of host images f[S,N0,N0] -> host sinograms.  With torch
+        CPU tensors the result is enqueued on the current stream (synchronise before
+        reading it); NumPy input returns a NumPy array after synchronising."""
+        return self._host_op("fwd", f, out, gpu, chunk)
+
+    def adj(self, R, gpu=0, out=None, chunk=None):
+        """Adjoint / FBP of host sinograms R[S,Nproj,N0] -> host images (see fwd)."""
+        return self._host_op("adj", R, out, gpu, chunk)
 
     def close(self):
         for i, h in enumerate(self.clphandle):

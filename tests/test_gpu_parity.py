@@ -170,3 +170,27 @@ def test_large_sizes(torch_cuda, args):
     assert O.rel_l2(Rg, tr.fwd(f)) < TOL
     Rn = Rg + 0.01 * np.abs(Rg).max() * rng.standard_normal(Rg.shape)
     assert O.rel_l2(_adj(torch_cuda, h, Rn), tr.adj(Rn)) < TOL
+
+
+def test_host_array_pipeline(torch_cuda):
+    """lpTransform.fwd/adj on host arrays (chunked, overlapped copies) == fwdp/adjp."""
+    torch = torch_cuda
+    from lprec_gb300.lpTransform import lpTransform
+    S, N, Nproj = 7, 128, 192
+    lp = lpTransform(N, Nproj, 4, 'ramp', N / 2, 'cubic')
+    lp.precompute(1)
+    lp.initcmem(1, 0)
+    rng = np.random.default_rng(3)
+    f = rng.random((S, N, N), dtype=np.float32)
+    R = rng.random((S, Nproj, N), dtype=np.float32)
+    Rh = lp.fwd(f, 0, chunk=3)                      # numpy in, numpy out
+    fh = lp.adj(torch.from_numpy(R).pin_memory(), 0, chunk=4)
+    torch.cuda.synchronize()
+    fh = fh.numpy()
+    for s in range(S):
+        Rd = torch.zeros((1, Nproj, N), device='cuda')
+        fd = torch.zeros((1, N, N), device='cuda')
+        lp.fwdp(Rd, torch.as_tensor(f[s:s + 1]).cuda(), 0)
+        lp.adjp(fd, torch.as_tensor(R[s:s + 1]).cuda(), 0)
+        assert np.array_equal(Rh[s], Rd.cpu().numpy()[0])
+        assert np.array_equal(fh[s], fd.cpu().numpy()[0])
