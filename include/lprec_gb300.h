@@ -95,6 +95,15 @@ int lp_fwd(lp_handle* h, float* R, const float* f, int S0, void* stream);
 int lp_adj(lp_handle* h, float* f, const float* R, int S0, void* stream);
 
 /*
+ * Exact transpose of lp_fwd: f = Radon^T(R), the gradient of <lp_fwd(f), R>
+ * with respect to f (used as the autograd backward).  No counterpart in the
+ * reference, whose adjoint execAdjManyPtr is a different discretisation
+ * (its own kernel fZadj and grids, src/lprec/initsadj.py) and only
+ * approximately the transpose.  R is read only.
+ */
+int lp_fwd_transpose(lp_handle* h, float* f, const float* R, int S0, void* stream);
+
+/*
  * Geometry of a handle: out[0..9] = N, N0, Ntheta, Nrho, Nproj (internal),
  * Nproj (caller), Nslices, cor, osangles, cubic.
  */

@@ -23,7 +23,7 @@ PRECISION = {"reference": 0, "fp64": 1}
 EXPORTS = ("lp_last_error", "lp_version", "lp_precompute_sizes", "lp_precompute", "lp_create", "lp_init_fwd",
            "lp_init_adj", "lp_destroy", "lp_fwd", "lp_adj", "lp_get_geometry", "lp_device_bytes",
            "lp_launch_count", "lp_kernel_count", "lp_kernel_name", "lp_set_profiling", "lp_profile_collect",
-           "lp_fwd_noalloc", "lp_noalloc_scratch_bytes")
+           "lp_fwd_noalloc", "lp_noalloc_scratch_bytes", "lp_fwd_transpose")
 
 
 class LprecError(RuntimeError):
@@ -62,6 +62,7 @@ def lib():
         "lp_get_geometry": (c_int, [c_void_p, P_i32]),
         "lp_device_bytes": (c_int, [c_void_p, P_i64]),
         "lp_fwd_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+        "lp_fwd_transpose": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
         "lp_noalloc_scratch_bytes": (c_int, [c_void_p, c_int, P_i64]),
         "lp_launch_count": (ctypes.c_longlong, []),
         "lp_kernel_count": (c_int, []),
@@ -146,6 +147,9 @@ class Handle:
 
     def adj(self, f_ptr, R_ptr, S0, stream):
         check(lib().lp_adj(self._h, c_void_p(f_ptr), c_void_p(R_ptr), int(S0), c_void_p(stream)))
+
+    def fwd_transpose(self, f_ptr, R_ptr, S0, stream):
+        check(lib().lp_fwd_transpose(self._h, c_void_p(f_ptr), c_void_p(R_ptr), int(S0), c_void_p(stream)))
 
     def fwd_noalloc(self, R_ptr, f_ptr, S0, stream):
         check(lib().lp_fwd_noalloc(self._h, c_void_p(R_ptr), c_void_p(f_ptr), int(S0), c_void_p(stream)))

@@ -104,7 +104,13 @@ struct FwdDev {
   std::vector<cudaSurfaceObject_t> surf_h;
   DevBuf<cudaTextureObject_t> tex;
   DevBuf<cudaSurfaceObject_t> surf;
+  // exact transpose: per span, column blocks of kTransposeCW columns with the
+  // range of sinogram rows whose theta taps touch them; columns holding disk points
+  DevBuf<int2> blk[3];
+  int nblk[3] = {0, 0, 0};
+  int dlo = 0, dhi = -1;
 };
+static const int kTransposeCW = 8;
 
 struct AdjDev {
   DevBuf<float> ta[3];     // [Nth]
@@ -131,11 +137,16 @@ enum KernelId {
   K_ADJ_POLAR2LP,
   K_ADJ_LPCOLS,
   K_ADJ_LP2CART,
+  K_FWDT_POLAR,
+  K_FWDT_CART,
+  K_PREFILTER_T,
+  K_CROP,
   K_COUNT
 };
-static const char* kKernelNames[K_COUNT] = {"fwd_ingest", "col_prefilter", "fwd_c2lp", "theta_conv",
-                                             "fwd_lp2polar", "adj_ingest", "adj_polar2lp", "adj_lpcols",
-                                             "adj_lp2cart"};
+static const char* kKernelNames[K_COUNT] = {"fwd_ingest",   "col_prefilter", "fwd_c2lp",   "theta_conv",
+                                             "fwd_lp2polar", "adj_ingest",    "adj_polar2lp", "adj_lpcols",
+                                             "adj_lp2cart",  "fwdT_polar",    "fwdT_cart",  "prefilter_T",
+                                             "crop"};
 
 static std::atomic<long long> g_launches(0);
 
@@ -166,6 +177,7 @@ static void free_fwd(FwdDev* f) {
   for (int k = 0; k < 3; ++k) {
     f->c2lp[k].free_();
     f->rows[k].free_();
+    f->blk[k].free_();
   }
   f->thc.free_();
   f->rhoc.free_();
@@ -480,6 +492,13 @@ int lp_init_fwd(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
       }
       const int r = idx / Nth, t = idx % Nth;
       c2lp[(size_t)t * Nrho + r] = make_float2(x, y);
+      if (F->dhi < F->dlo) {
+        F->dlo = t;
+        F->dhi = t;
+      } else {
+        F->dlo = std::min(F->dlo, t);
+        F->dhi = std::max(F->dhi, t);
+      }
     }
     DeviceGuard g(h->device);
     cudaError_t e = dev_upload(F->c2lp[k], c2lp);
@@ -537,6 +556,32 @@ int lp_init_fwd(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
   }
   F->lo = lo;
   F->hi = hi;
+  // column blocks for the transpose
+  std::vector<int2> blk[3];
+  {
+    const int ntap = h->cubic ? 4 : 2;
+    const int nb = (hi - lo + kTransposeCW) / kTransposeCW;
+    for (int k = 0; k < 3; ++k) {
+      for (int b = 0; b < nb; ++b) {
+        const int c0 = lo + b * kTransposeCW, c1 = std::min(c0 + kTransposeCW, hi + 1);
+        int first = -1, last = -1;
+        for (int i = 0; i < (int)rows[k].size(); ++i) {
+          const int c = first_tap(thc[rows[k][i]], h->cubic);
+          bool touch = false;
+          for (int j = 0; j < ntap && !touch; ++j) {
+            int cc = (c + j) % Nth;
+            if (cc < 0) cc += Nth;
+            touch = cc >= c0 && cc < c1;
+          }
+          if (touch) {
+            if (first < 0) first = i;
+            last = i;
+          }
+        }
+        blk[k].push_back(first < 0 ? make_int2(0, 0) : make_int2(first, last + 1));
+      }
+    }
+  }
   {
     DeviceGuard g(h->device);
     cudaError_t e = dev_upload(F->thc, thc);
@@ -544,6 +589,8 @@ int lp_init_fwd(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
       F->nrows[k] = (int)rows[k].size();
       e = dev_upload(F->rows[k], rows[k]);
+      if (e == cudaSuccess) e = dev_upload(F->blk[k], blk[k]);
+      F->nblk[k] = (int)blk[k].size();
     }
     if (e == cudaSuccess) e = dev_upload(F->fz, extend_kernel(fzv, Nrho, Nth));
     if (e == cudaSuccess) e = dev_alloc(F->fbuf, (size_t)h->Nslices * N * N);
@@ -753,6 +800,42 @@ int lp_fwd(lp_handle* h, float* R, const float* f, int S0, void* stream) {
                        h->Nrho, h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho};
     CUDA_TRY(launch(h, K_FWD_LP2POLAR, st, [&] { return launch_fwd_lp2polar(a3, S0, st); }));
   }
+  return LP_OK;
+}
+
+int lp_fwd_transpose(lp_handle* h, float* f, const float* R, int S0, void* stream) {
+  if (!h) return set_err(LP_ERR_ARG, "lp_fwd_transpose: null handle");
+  if (!h->fwd) return set_err(LP_ERR_STATE, "lp_fwd_transpose: forward tables not initialised (lp_init_fwd)");
+  if (S0 < 0 || S0 > h->Nslices)
+    return set_err(LP_ERR_ARG, "lp_fwd_transpose: S0=%d outside [0, %d]", S0, h->Nslices);
+  if (S0 == 0) return LP_OK;
+  if (!R || !f) return set_err(LP_ERR_ARG, "lp_fwd_transpose: null data pointer");
+  DeviceGuard g(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  FwdDev* F = h->fwd;
+  float* acc = F->fbuf.p;
+  CUDA_TRY(cudaMemsetAsync(acc, 0, (size_t)S0 * h->N * h->N * sizeof(float), st));
+  for (int k = 0; k < 3; ++k) {
+    CUDA_TRY(cudaMemsetAsync(h->spec.p, 0, (size_t)S0 * h->Nk * h->Nth * sizeof(float2), st));
+    FwdTPolarArgs a1{R, h->spec.p, F->thc.p, F->rhoc.p, F->rows[k].p, F->blk[k].p, h->N, h->N0, h->Nth, h->Nrho,
+                     h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, F->lo, kTransposeCW, h->plan_rho};
+    CUDA_TRY(launch(h, K_FWDT_POLAR, st, [&] { return launch_fwdT_polar(a1, S0, F->nblk[k], st); }));
+    ThetaConvArgs a2{h->spec.p, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), F->lo, F->hi,
+                     F->dlo, F->dhi, 1, h->plan_th};
+    if (F->dhi >= F->dlo)
+      CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
+    FwdTCartArgs a3{h->spec.p, acc, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, F->dlo, F->dhi,
+                    h->cubic, h->plan_rho};
+    CUDA_TRY(launch(h, K_FWDT_CART, st, [&] { return launch_fwdT_cart(a3, S0, st); }));
+  }
+  if (h->cubic) {
+    PrefilterTArgs pc{acc, h->N, h->N, 0};
+    CUDA_TRY(launch(h, K_PREFILTER_T, st, [&] { return launch_prefilter_T(pc, S0, st); }));
+    PrefilterTArgs pr{acc, h->N, h->N, 1};
+    CUDA_TRY(launch(h, K_PREFILTER_T, st, [&] { return launch_prefilter_T(pr, S0, st); }));
+  }
+  CropArgs cr{acc, f, h->N, h->N0, h->N / 2 - h->N0 / 2};
+  CUDA_TRY(launch(h, K_CROP, st, [&] { return launch_crop(cr, S0, st); }));
   return LP_OK;
 }
 

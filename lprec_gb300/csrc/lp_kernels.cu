@@ -1355,3 +1355,218 @@ bool p2_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st, cudaError_t* 
 }
 
 }  // namespace lpgb
+
+// ===========================================================================
+// Exact transpose of the forward operator (gradient of <fwd(f), g> in f).
+// Stage by stage: transposed rho interpolation of every sinogram row, the
+// transpose of C2R (a_k * R2C), the theta-tap combination scattered back to
+// the columns, the theta convolution with conj(fZ), the transpose of R2C
+// (C2R of b_k * Y), e^rho, the transposed Cartesian interpolation (scatter),
+// and the transposed prefilter recursions.
+// ===========================================================================
+namespace lpgb {
+
+__global__ void __launch_bounds__(256) k_fwdT_polar(FwdTPolarArgs a) {
+  extern __shared__ float smf[];
+  CBuf A, B;
+  float* u = carve(smf, a.Nrho, 1, A, B);  // 2 x Nrho transposed-interpolation accumulators
+  const int s = blockIdx.x;
+  const int b = blockIdx.y;
+  const int c0 = a.lo + b * a.CW;
+  const int2 rr = __ldg(a.blk + b);
+  const int ntap = a.cubic ? 4 : 2;
+  float2* sp = a.spec + (size_t)s * a.Nk * a.Nth;
+  const int L = a.Nrho;
+  for (int i0 = rr.x; i0 < rr.y; i0 += 2) {
+    const int r0 = a.rows[i0];
+    const int r1 = (i0 + 1 < rr.y) ? a.rows[i0 + 1] : -1;
+    for (int i = threadIdx.x; i < 2 * L; i += blockDim.x) u[i] = 0.f;
+    __syncthreads();
+    // transposed 1-D interpolation along rho of the two rows
+    for (int q = 0; q < 2; ++q) {
+      const int r = q == 0 ? r0 : r1;
+      if (r < 0) continue;
+      const float* row = a.Rin + ((size_t)s * a.Nproj0 + r / a.os) * a.N0;
+      for (int x = threadIdx.x; x < a.N; x += blockDim.x) {
+        const int xo = x - a.cor_off;
+        if (xo < 0 || xo >= a.N0) continue;
+        const float val = __ldg(row + xo);
+        float w[4];
+        const int c = axis_weights(__ldg(a.rhoc + (size_t)r * a.N + x), a.cubic, w);
+        for (int j = 0; j < ntap; ++j) atomicAdd(u + q * L + wrapi(c + j, L), w[j] * val);
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < L; i += blockDim.x) A.set(i, make_float2(u[i], u[L + i]));
+    __syncthreads();
+    const CBuf Z = fft_block<-1>(A, B, a.plan, 1, 0);
+    float w0[4], w1[4];
+    const int t0 = axis_weights(__ldg(a.thc + r0), a.cubic, w0);
+    int t1 = 0;
+    if (r1 >= 0) t1 = axis_weights(__ldg(a.thc + r1), a.cubic, w1);
+    for (int k = threadIdx.x; k < a.Nk; k += blockDim.x) {
+      const float2 z1 = Z.get(k);
+      const float2 z2 = Z.get(k == 0 ? 0 : L - k);
+      const float ak = (k == 0 || k == L / 2) ? 1.f : 2.f;
+      float2 va = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+      float2 vb = make_float2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
+      if (ak == 1.f) {
+        va.y = 0.f;
+        vb.y = 0.f;
+      }
+      va = cscale(va, ak);
+      vb = cscale(vb, ak);
+      float2* rowk = sp + (size_t)k * a.Nth;
+      for (int j = 0; j < ntap; ++j) {
+        const int ca = wrapi(t0 + j, a.Nth);
+        if (ca >= c0 && ca < c0 + a.CW) {
+          float2 o = rowk[ca];
+          o.x += w0[j] * va.x;
+          o.y += w0[j] * va.y;
+          rowk[ca] = o;
+        }
+        if (r1 >= 0) {
+          const int cb = wrapi(t1 + j, a.Nth);
+          if (cb >= c0 && cb < c0 + a.CW) {
+            float2 o = rowk[cb];
+            o.x += w1[j] * vb.x;
+            o.y += w1[j] * vb.y;
+            rowk[cb] = o;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ void scatter2d(float* img, int W, int H, float x, float y, float val, int cubic) {
+  const float fx = floorf(x), fy = floorf(y);
+  const int ix = (int)fx, iy = (int)fy;
+  float wx[4], wy[4];
+  int nt;
+  if (cubic) {
+    bspline_w(x - fx, wx);
+    bspline_w(y - fy, wy);
+    nt = 4;
+  } else {
+    wx[0] = 1.f - (x - fx);
+    wx[1] = x - fx;
+    wy[0] = 1.f - (y - fy);
+    wy[1] = y - fy;
+    nt = 2;
+  }
+  const int ox = cubic ? 1 : 0;
+  for (int j = 0; j < nt; ++j) {
+    float* row = img + (size_t)wrapi(iy - ox + j, H) * W;
+    for (int i = 0; i < nt; ++i) atomicAdd(row + wrapi(ix - ox + i, W), wy[j] * wx[i] * val);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_fwdT_cart(FwdTCartArgs a) {
+  extern __shared__ float smf[];
+  CBuf A, B;
+  carve(smf, a.Nrho, 1, A, B);
+  const int s = blockIdx.x;
+  const int th0 = a.dlo + 2 * blockIdx.y;
+  const int th1 = th0 + 1 <= a.dhi ? th0 + 1 : -1;
+  const float2* sp = a.spec + (size_t)s * a.Nk * a.Nth;
+  const int L = a.Nrho;
+  for (int k = threadIdx.x; k < a.Nk; k += blockDim.x) {
+    const float bk = (k == 0 || k == L / 2) ? 1.f : 0.5f;
+    const float2 v0 = cscale(sp[(size_t)k * a.Nth + th0], bk);
+    const float2 v1 = th1 >= 0 ? cscale(sp[(size_t)k * a.Nth + th1], bk) : make_float2(0.f, 0.f);
+    put_pair(A, k, L, v0, v1);
+  }
+  __syncthreads();
+  const CBuf z = fft_block<1>(A, B, a.plan, 1, 0);
+  float* img = a.acc + (size_t)s * a.N * a.N;
+  for (int q = 0; q < 2; ++q) {
+    const int th = q == 0 ? th0 : th1;
+    if (th < 0) break;
+    const float2* cc = a.c2lp + (size_t)th * L;
+    for (int r = threadIdx.x; r < L; r += blockDim.x) {
+      const float2 p = __ldg(cc + r);
+      if (isnan(p.x)) continue;
+      const float2 zv = z.get(r);
+      const float val = __ldg(a.erho + r) * (q == 0 ? zv.x : zv.y);
+      scatter2d(img, a.N, a.N, p.x, p.y, val, a.cubic);
+    }
+  }
+}
+
+// one thread per line: y -> A^T (causal sum, boundary scaling) -> anticausal sum -> K^T
+__global__ void k_prefilter_T(PrefilterTArgs a) {
+  const int s = blockIdx.y;
+  const int line = blockIdx.x * blockDim.x + threadIdx.x;
+  const int L = a.along_rows ? a.W : a.H;
+  const int nl = a.along_rows ? a.H : a.W;
+  if (line >= nl) return;
+  const size_t stride = a.along_rows ? 1 : (size_t)a.W;
+  float* p = a.img + (size_t)s * a.H * a.W + (a.along_rows ? (size_t)line * a.W : (size_t)line);
+  const float z = LP_POLE, q = LP_POLE / (LP_POLE - 1.0f);
+  float t = 0.f;
+  for (int m = 0; m < L; ++m) {
+    t = p[m * stride] + z * t;
+    p[m * stride] = (m < L - 1) ? -z * t : q * t;
+  }
+  float w = p[(size_t)(L - 1) * stride];
+  for (int m = L - 2; m >= 0; --m) {
+    w = p[m * stride] + z * w;
+    p[m * stride] = w;
+  }
+  const float w0 = p[0];
+  const int hor = min(12, L);
+  float zn = z;
+  for (int m = 0; m < L; ++m) {
+    float v = LP_LAMBDA * p[m * stride];
+    if (m < hor) {
+      v += LP_LAMBDA * zn * w0;
+      zn *= z;
+    }
+    p[m * stride] = v;
+  }
+}
+
+__global__ void k_crop(CropArgs a) {
+  const int s = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.N0 * a.N0) return;
+  const int y = i / a.N0, x = i - y * a.N0;
+  a.dst[(size_t)s * a.N0 * a.N0 + i] = a.src[((size_t)s * a.N + y + a.off) * a.N + x + a.off];
+}
+
+cudaError_t launch_fwdT_polar(const FwdTPolarArgs& a, int S, int nblk, cudaStream_t st) {
+  if (nblk <= 0) return cudaSuccess;
+  const size_t sm = fft_bytes(a.Nrho, 1) + 2 * (size_t)a.Nrho * sizeof(float);
+  if (smem_ok(sm) != cudaSuccess) return cudaErrorInvalidConfiguration;
+  cudaFuncSetAttribute(k_fwdT_polar, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+  dim3 grid(S, nblk);
+  k_fwdT_polar<<<grid, 256, sm, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fwdT_cart(const FwdTCartArgs& a, int S, cudaStream_t st) {
+  if (a.dhi < a.dlo) return cudaSuccess;
+  const size_t sm = fft_bytes(a.Nrho, 1);
+  if (smem_ok(sm) != cudaSuccess) return cudaErrorInvalidConfiguration;
+  cudaFuncSetAttribute(k_fwdT_cart, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+  dim3 grid(S, (a.dhi - a.dlo + 2) / 2);
+  k_fwdT_cart<<<grid, 256, sm, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prefilter_T(const PrefilterTArgs& a, int S, cudaStream_t st) {
+  const int nl = a.along_rows ? a.H : a.W;
+  dim3 grid((nl + 127) / 128, S);
+  k_prefilter_T<<<grid, 128, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_crop(const CropArgs& a, int S, cudaStream_t st) {
+  dim3 grid((a.N0 * a.N0 + 255) / 256, S);
+  k_crop<<<grid, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace lpgb

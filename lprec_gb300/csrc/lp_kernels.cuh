@@ -107,3 +107,42 @@ cudaError_t configure_kernels(int N);
 void set_use_p2(bool on);
 
 }  // namespace lpgb
+
+namespace lpgb {
+// ---- exact transpose of the forward (autograd backward) --------------------
+struct FwdTPolarArgs {        // sinogram rows -> log-polar spectrum columns (transposed lp2polar)
+  const float* Rin;           // [S][Nproj0][N0] caller's gradient
+  float2* spec;               // [S][Nk][Nth], zeroed; block owns columns [c0, c0+CW)
+  const float* thc;           // [Nproj] theta coordinate per internal row
+  const float* rhoc;          // [Nproj][N] rho coordinate per polar point
+  const int* rows;            // rows of the span (multiples of os), sorted
+  const int2* blk;            // per column block: [first, last) into rows
+  int N, N0, Nth, Nrho, Nk, Nproj0, os, cor_off, cubic, lo, CW;
+  FFTPlan plan;               // length Nrho
+};
+
+struct FwdTCartArgs {         // spectrum columns -> real log-polar columns -> scatter to the image
+  const float2* spec;         // [S][Nk][Nth]
+  float* acc;                 // [S][N][N] accumulator (atomic adds)
+  const float2* c2lp;         // [Nth][Nrho] this span
+  const float* erho;          // [Nrho]
+  int N, Nth, Nrho, Nk, dlo, dhi, cubic;
+  FFTPlan plan;
+};
+
+struct PrefilterTArgs {       // transposed prefilter along lines of length L, in place
+  float* img;                 // [S][H][W]
+  int H, W, along_rows;       // along_rows: lines are rows (length W); else columns (length H)
+};
+
+struct CropArgs {
+  const float* src;           // [S][N][N]
+  float* dst;                 // [S][N0][N0]
+  int N, N0, off;
+};
+
+cudaError_t launch_fwdT_polar(const FwdTPolarArgs& a, int S, int nblk, cudaStream_t st);
+cudaError_t launch_fwdT_cart(const FwdTCartArgs& a, int S, cudaStream_t st);
+cudaError_t launch_prefilter_T(const PrefilterTArgs& a, int S, cudaStream_t st);
+cudaError_t launch_crop(const CropArgs& a, int S, cudaStream_t st);
+}  // namespace lpgb

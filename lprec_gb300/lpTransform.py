@@ -136,6 +136,17 @@ class lpTransform:
                 raise ValueError("adjp: arrays live on cuda:%d, handle on cuda:%d" % (d, gpu))
         h.adj(fp, Rp, S0, _stream(gpu))
 
+    def fwdp_T(self, f, R, gpu):
+        """Exact transpose of fwdp: f[S0,N0,N0] <- Radon^T(R[S0,Nproj,N0]) (autograd backward)."""
+        h = self._handle(gpu)
+        fp, fs, fd = _dev_ptr(f)
+        Rp, Rs, Rd = _dev_ptr(R)
+        S0 = Rs[0]
+        if Rs[1:] != (h.Nproj, h.N0) or fs != (S0, h.N0, h.N0):
+            raise ValueError("fwdp_T: R must be [S0,%d,%d] and f [S0,%d,%d]; got %s, %s"
+                             % (h.Nproj, h.N0, h.N0, h.N0, Rs, fs))
+        h.fwd_transpose(fp, Rp, S0, _stream(gpu))
+
     # ---- host arrays, pipelined ---------------------------------------------
     def _host_op(self, op, x, out, gpu, chunk):
         """Run fwdp/adjp over host arrays in slice chunks, overlapping the

@@ -747,6 +747,90 @@ class Transform:
     def adj(self, R):
         return adj(self.G, self.Ta, np.asarray(R, dtype=np.float64))
 
+    def fwd_T(self, R):
+        """Exact transpose of fwd (gradient of <fwd(f), R> with respect to f)."""
+        return fwd_T(self.G, self.Tf, np.asarray(R, dtype=np.float64), self.erho)
+
+
+# --------------------------------------------------------------------------
+# exact transpose of the forward operator (for the autograd backward); this
+# is NOT the reference's adjoint, which is a different discretisation
+# --------------------------------------------------------------------------
+def prefilter_lines_T(y, axis):
+    """Transpose of prefilter_lines along `axis` (main_kernels.cuh:97-142 as a matrix)."""
+    c = np.moveaxis(np.array(y, dtype=np.float64), axis, 0).copy()
+    L = c.shape[0]
+    z = POLE
+    q = z / (z - 1.0)
+    # A^T: causal sum t[m] = y[m] + z t[m-1]; a[m] = -z t[m], a[L-1] = q t[L-1]
+    t = c[0].copy()
+    a = np.empty_like(c)
+    for m in range(L):
+        if m > 0:
+            t = c[m] + z * t
+        a[m] = -z * t if m < L - 1 else q * t
+    # anticausal sum w[m] = a[m] + z w[m+1]
+    w = np.empty_like(c)
+    w[L - 1] = a[L - 1]
+    for m in range(L - 2, -1, -1):
+        w[m] = a[m] + z * w[m + 1]
+    # K^T: Lambda (w[m] + [m < H] z^(m+1) w[0])
+    hor = min(12, L)
+    out = LAMBDA * w
+    for m in range(hor):
+        out[m] += LAMBDA * z ** (m + 1) * w[0]
+    return np.moveaxis(out, 0, axis)
+
+
+def prefilter2d_T(y):
+    return prefilter_lines_T(prefilter_lines_T(y, -2), -1)
+
+
+def interp2d_T(shape, vals, x, y, cubic):
+    """Transpose of interp2d: scatter vals[S, Np] into an image of `shape` = (S, H, W)."""
+    S, H, W = shape
+    vals = np.asarray(vals, dtype=np.float64)
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    ix = np.floor(x)
+    iy = np.floor(y)
+    fx = x - ix
+    fy = y - iy
+    ix = ix.astype(np.int64)
+    iy = iy.astype(np.int64)
+    out = np.zeros((S, H * W))
+    if cubic:
+        wx = bspline_weights(fx)
+        wy = bspline_weights(fy)
+        taps = [(j - 1, i - 1, wy[j] * wx[i]) for j in range(4) for i in range(4)]
+    else:
+        taps = [(0, 0, (1 - fy) * (1 - fx)), (0, 1, (1 - fy) * fx), (1, 0, fy * (1 - fx)), (1, 1, fy * fx)]
+    for dj, di, wgt in taps:
+        idx = np.mod(iy + dj, H) * W + np.mod(ix + di, W)
+        for s in range(S):
+            out[s] += np.bincount(idx, weights=wgt * vals[s], minlength=H * W)
+    return out.reshape(S, H, W)
+
+
+def fwd_T(G, T, R_out, erho):
+    """Exact transpose of fwd(): R_out[S0, Nproj0, N0] -> f[S0, N0, N0]."""
+    S = R_out.shape[0]
+    N, N0 = G.N, G.N0
+    c0 = N // 2 - G.cor
+    R = np.zeros((S, G.Nproj, N))
+    R[:, ::G.osangles, c0:c0 + N0] = R_out
+    Rf = R.reshape(S, -1)
+    f = np.zeros((S, N, N))
+    for k in range(NSPAN):
+        H = interp2d_T((S, G.Nrho, G.Ntheta), Rf[:, T['pids'][k]], T['p2lp1'][k], T['p2lp2'][k], G.cubic)
+        X = np.fft.rfft2(H, axes=(-2, -1)) * np.conj(T['fZ'])[None]
+        H = np.fft.irfft2(X, s=(G.Nrho, G.Ntheta), axes=(-2, -1)) * erho[None, :, None]
+        f += interp2d_T((S, N, N), H.reshape(S, -1)[:, T['cids']], T['lp2C1'][k], T['lp2C2'][k], G.cubic)
+    if G.cubic:
+        f = prefilter2d_T(f)
+    o = N // 2 - N0 // 2
+    return f[:, o:o + N0, o:o + N0]
+
 
 # --------------------------------------------------------------------------
 # solvers (lpmethods.py), float64, used to check the GPU solvers

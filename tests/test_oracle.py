@@ -104,3 +104,23 @@ def test_reference_pin_adj_ptr():
     tr = O.Transform(512, 768, 1, 'none', 256, 'cubic')
     err = abs(np.sum(tr.fwd(f) * R) - np.sum(tr.adj(R) * f)) / abs(np.sum(tr.adj(R) * f))
     assert err < 1e-2
+
+
+def test_prefilter_transpose_matches_matrix():
+    for L in (5, 13, 40):
+        M = O.prefilter_lines(np.eye(L), 0)          # column j = filter applied to e_j
+        y = np.random.default_rng(L).standard_normal(L)
+        assert np.allclose(O.prefilter_lines_T(y[:, None], 0)[:, 0], M.T @ y, atol=1e-12)
+
+
+@pytest.mark.parametrize("args", [(48, 72, 'cubic', 21), (32, 24, 'linear', 16), (64, 96, 'cubic', 32)])
+def test_fwd_transpose_dot(args):
+    """<fwd f, g> == <f, fwd_T g> in float64 (exact discrete transpose)."""
+    N0, Nproj, interp, cor = args
+    tr = O.Transform(N0, Nproj, 1, 'none', cor, interp)
+    rng = np.random.default_rng(2)
+    f = rng.standard_normal((2, N0, N0))
+    g = rng.standard_normal((2, Nproj, N0))
+    lhs = np.sum(tr.fwd(f) * g)
+    rhs = np.sum(f * tr.fwd_T(g))
+    assert abs(lhs - rhs) <= 1e-10 * abs(lhs)
