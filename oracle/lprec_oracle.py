@@ -611,6 +611,17 @@ def lp_conv(G, grid, fZ):
 # --------------------------------------------------------------------------
 # pipelines (lpRgpu.cu:243-330)
 # --------------------------------------------------------------------------
+def fwd_span(G, T, fp, erho, k, tex8=False):
+    """One span of execFwd (lpRgpu.cu:257-285) on the prefiltered image fp[S, N, N]:
+    returns that span's values at its polar points pids[k] (shape [S, len(pids[k])])."""
+    S = fp.shape[0]
+    dfl = np.zeros((S, G.Nrho * G.Ntheta))
+    dfl[:, T['cids']] = interp2d(fp, T['lp2C1'][k], T['lp2C2'][k], G.cubic, tex8)
+    dfl = dfl.reshape(S, G.Nrho, G.Ntheta) * erho[None, :, None]
+    dfl = lp_conv(G, dfl, T['fZ'])
+    return interp2d(dfl, T['p2lp1'][k], T['p2lp2'][k], G.cubic, tex8)
+
+
 def fwd_core(G, T, f, erho, tex8=False):
     """execFwd on the padded image f[S, N, N]; returns R[S, Nproj, N] (internal angles)."""
     S = f.shape[0]
@@ -618,12 +629,20 @@ def fwd_core(G, T, f, erho, tex8=False):
     fp = prefilter2d(f) if G.cubic else np.asarray(f, dtype=np.float64)
     R = np.zeros((S, G.Nproj * N))
     for k in range(NSPAN):
-        dfl = np.zeros((S, G.Nrho * G.Ntheta))
-        dfl[:, T['cids']] = interp2d(fp, T['lp2C1'][k], T['lp2C2'][k], G.cubic, tex8)
-        dfl = dfl.reshape(S, G.Nrho, G.Ntheta) * erho[None, :, None]
-        dfl = lp_conv(G, dfl, T['fZ'])
-        R[:, T['pids'][k]] += interp2d(dfl, T['p2lp1'][k], T['p2lp2'][k], G.cubic, tex8)
+        R[:, T['pids'][k]] += fwd_span(G, T, fp, erho, k, tex8)
     return R.reshape(S, G.Nproj, N)
+
+
+def adj_span(G, T, Rp, k, tex8=False):
+    """One span of execAdj (lpRgpu.cu:302-329) on the prefiltered sinogram Rp[S, Nproj, N]:
+    returns that span's contribution at the disk pixels cids (shape [S, len(cids)])."""
+    S = Rp.shape[0]
+    dfl = np.zeros((S, G.Nrho * G.Ntheta))
+    dfl[:, T['lpids']] += interp2d(Rp, T['lp2p2'][k], T['lp2p1'][k], G.cubic, tex8)
+    if len(T['wids']):
+        dfl[:, T['wids']] += interp2d(Rp, T['lp2p2w'][k], T['lp2p1w'][k], G.cubic, tex8)
+    dfl = lp_conv(G, dfl.reshape(S, G.Nrho, G.Ntheta), T['fZ'])
+    return interp2d(dfl, T['C2lp1'][k], T['C2lp2'][k], G.cubic, tex8)
 
 
 def adj_core(G, T, R, tex8=False):
@@ -633,12 +652,7 @@ def adj_core(G, T, R, tex8=False):
     Rp = prefilter2d(R) if G.cubic else np.asarray(R, dtype=np.float64)
     f = np.zeros((S, N * N))
     for k in range(NSPAN):
-        dfl = np.zeros((S, G.Nrho * G.Ntheta))
-        dfl[:, T['lpids']] += interp2d(Rp, T['lp2p2'][k], T['lp2p1'][k], G.cubic, tex8)
-        if len(T['wids']):
-            dfl[:, T['wids']] += interp2d(Rp, T['lp2p2w'][k], T['lp2p1w'][k], G.cubic, tex8)
-        dfl = lp_conv(G, dfl.reshape(S, G.Nrho, G.Ntheta), T['fZ'])
-        f[:, T['cids']] += interp2d(dfl, T['C2lp1'][k], T['C2lp2'][k], G.cubic, tex8)
+        f[:, T['cids']] += adj_span(G, T, Rp, k, tex8)
     return f.reshape(S, N, N)
 
 
