@@ -272,6 +272,53 @@ def per_kernel_bytes(h, S, prof):
     return b
 
 
+def uneven_requests(seed=1, n=48):
+    """48 requests: N in {256,512,1024,2048} w.p. {.4,.3,.2,.1}, Nproj = 1.5 N, 1..32 slices."""
+    rng = np.random.default_rng(seed)
+    Ns = rng.choice([256, 512, 1024, 2048], size=n, p=[0.4, 0.3, 0.2, 0.1])
+    Ss = rng.integers(1, 33, size=n)
+    return [(int(N), int(3 * N // 2), int(S)) for N, S in zip(Ns, Ss)]
+
+
+def run_uneven(torch, dev, reps):
+    """One CUDA-graph launch running fwd+adj of all 48 requests; throughput and latencies."""
+    from lprec_gb300.batch import UnevenBatch
+    reqs = uneven_requests()
+    t0 = time.perf_counter()
+    b = UnevenBatch(reqs, "shepp-logan", "cubic", dev)
+    t_setup = time.perf_counter() - t0
+    seed = 1
+    for i, (N, Nproj, S) in enumerate(reqs):
+        b.input_f(i).copy_(phantoms_gpu(torch, N, S, 20, seed + i, dev))
+    b.run_eager()
+    for i in range(len(reqs)):
+        b.input_R(i).copy_(b.output_R(i))
+    b.capture()
+    stream = torch.cuda.current_stream(dev)
+    b.run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        b.run()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    lat = b.latencies_ms()
+    e0.record(stream)
+    for _ in range(reps):
+        b.run_eager()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_eager = e0.elapsed_time(e1) / reps
+    out = {"requests": len(reqs), "slices": b.slices, "geometries": len(b.groups), "ms_per_launch": ms,
+           "slices_per_s": b.slices / (ms / 1000.0), "ms_eager": ms_eager, "setup_s": round(t_setup, 2)}
+    if lat is not None:
+        out["latency_ms_p50"] = float(np.percentile(lat, 50))
+        out["latency_ms_p99"] = float(np.percentile(lat, 99))
+    return out
+
+
 def run_ours(args):
     import torch
     from lprec_gb300 import _lib
@@ -411,6 +458,8 @@ def run_ours(args):
                               "peak": peak, "frac": step_gbs / peak},
             "kernels": kernels,
             "clocks": clk.summary()}
+    if rank == 0 and not args.no_uneven and not args.small:
+        line["uneven_batch"] = run_uneven(torch, dev, max(2, args.steps // 2))
     if rank == 0 and not args.no_cpu:
         cores = len(os.sched_getaffinity(0))
         nproc = max(1, min(cores, 6))
@@ -435,6 +484,7 @@ def main():
     ap.add_argument("--small", action="store_true", help="N=256 smoke-size workload")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--slices", type=int, default=0, help="batch size (default 128); for profiling runs")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-geometry graph batch")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

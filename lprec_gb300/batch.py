@@ -1,0 +1,109 @@
+"""Requests of uneven geometry in one CUDA-graph launch.
+
+    b = UnevenBatch([(N, Nproj, slices), ...], filter_type, interp_type, gpu)
+    b.input_f(i)[:] = ...; b.input_R(i)[:] = ...     # device views per request
+    b.capture()                                      # fwd + adj of every request in one graph
+    b.run()                                          # one graph launch
+    b.output_R(i), b.output_f(i)
+
+Requests with the same (N, Nproj) share one native handle and are
+concatenated into one batch.  The groups run one after another inside the
+graph, smallest geometry first (running them on parallel graph branches was
+measured slower: the large groups already fill the GPU and the branches only
+compete for L2).  The graph records an event when each group finishes, which
+gives per-request latencies measured from the start of the launch.
+"""
+import torch
+
+from .lpTransform import lpTransform
+
+
+class UnevenBatch:
+    def __init__(self, requests, filter_type="ramp", interp_type="cubic", gpu=0, precision="fp64"):
+        self.gpu = gpu
+        self.dev = torch.device("cuda", gpu)
+        self.requests = [tuple(int(v) for v in r) for r in requests]
+        groups = {}
+        for i, (N, Nproj, S) in enumerate(self.requests):
+            groups.setdefault((N, Nproj), []).append(i)
+        self.groups = []
+        self.where = {}
+        for (N, Nproj), idx in sorted(groups.items(), key=lambda kv: kv[0][0]):
+            total = sum(self.requests[i][2] for i in idx)
+            lp = lpTransform(N, Nproj, total, filter_type, N / 2, interp_type, precision)
+            lp.precompute(1)
+            lp.initcmem(1, gpu)
+            g = dict(lp=lp, N=N, Nproj=Nproj, S=total, idx=idx,
+                     f=torch.zeros((total, N, N), device=self.dev),
+                     R=torch.zeros((total, Nproj, N), device=self.dev),
+                     Rout=torch.zeros((total, Nproj, N), device=self.dev),
+                     fout=torch.zeros((total, N, N), device=self.dev))
+            off = 0
+            for i in idx:
+                self.where[i] = (len(self.groups), off, self.requests[i][2])
+                off += self.requests[i][2]
+            self.groups.append(g)
+        self.graph = None
+
+    def _view(self, i, key):
+        gi, off, S = self.where[i]
+        return self.groups[gi][key][off:off + S]
+
+    def input_f(self, i):
+        return self._view(i, "f")
+
+    def input_R(self, i):
+        return self._view(i, "R")
+
+    def output_R(self, i):
+        return self._view(i, "Rout")
+
+    def output_f(self, i):
+        return self._view(i, "fout")
+
+    def _work(self, g):
+        g["lp"].fwdp(g["Rout"], g["f"], self.gpu)
+        g["lp"].adjp(g["fout"], g["R"], self.gpu)
+
+    def run_eager(self):
+        """The same work without the graph (one group after the other)."""
+        for g in self.groups:
+            self._work(g)
+
+    def capture(self):
+        main = torch.cuda.Stream(self.dev)
+        with torch.cuda.stream(main):
+            self.run_eager()  # warm-up outside capture
+        torch.cuda.synchronize(self.dev)
+        try:
+            self.t_start = torch.cuda.Event(enable_timing=True, external=True)
+            self.t_done = [torch.cuda.Event(enable_timing=True, external=True) for _ in self.groups]
+        except TypeError:  # torch without event-record graph nodes: no per-request latencies
+            self.t_start = None
+            self.t_done = [None for _ in self.groups]
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph, stream=main):
+            if self.t_start is not None:
+                self.t_start.record(main)
+            for g, ev in zip(self.groups, self.t_done):
+                self._work(g)
+                if ev is not None:
+                    ev.record(main)
+        self._main = main
+
+    def run(self):
+        if self.graph is None:
+            self.capture()
+        self.graph.replay()
+
+    def latencies_ms(self):
+        """Per-request latency of the last run: start of the launch to its group's end."""
+        torch.cuda.synchronize(self.dev)
+        if self.t_start is None:
+            return None
+        per_group = [self.t_start.elapsed_time(ev) for ev in self.t_done]
+        return [per_group[self.where[i][0]] for i in range(len(self.requests))]
+
+    @property
+    def slices(self):
+        return sum(r[2] for r in self.requests)

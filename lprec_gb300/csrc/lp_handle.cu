@@ -45,14 +45,21 @@ int lp_internal_set_err(int code, const char* msg) { return set_err(code, "%s", 
 
 namespace {
 
+// Makes `dev` current for the scope of a call (only switching when needed, so
+// calls made while a stream on that device is being captured stay free of
+// device changes).
 struct DeviceGuard {
   int prev = -1;
+  bool switched = false;
   explicit DeviceGuard(int dev) {
     if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-    cudaSetDevice(dev);
+    if (prev != dev) {
+      cudaSetDevice(dev);
+      switched = true;
+    }
   }
   ~DeviceGuard() {
-    if (prev >= 0) cudaSetDevice(prev);
+    if (switched && prev >= 0) cudaSetDevice(prev);
   }
 };
 

@@ -194,3 +194,32 @@ def test_host_array_pipeline(torch_cuda):
         lp.adjp(fd, torch.as_tensor(R[s:s + 1]).cuda(), 0)
         assert np.array_equal(Rh[s], Rd.cpu().numpy()[0])
         assert np.array_equal(fh[s], fd.cpu().numpy()[0])
+
+
+def test_uneven_batch_graph(torch_cuda):
+    """Requests of different geometry in one CUDA graph == per-request calls."""
+    torch = torch_cuda
+    from lprec_gb300.batch import UnevenBatch
+    from lprec_gb300.lpTransform import lpTransform
+    reqs = [(64, 96, 2), (128, 192, 1), (64, 96, 3), (256, 384, 2)]
+    b = UnevenBatch(reqs, 'ramp', 'cubic', 0)
+    rng = np.random.default_rng(8)
+    for i, (N, Nproj, S) in enumerate(reqs):
+        b.input_f(i).copy_(torch.as_tensor(rng.random((S, N, N), dtype=np.float32)))
+        b.input_R(i).copy_(torch.as_tensor(rng.random((S, Nproj, N), dtype=np.float32)))
+    b.capture()
+    b.run()
+    torch.cuda.synchronize()
+    lat = b.latencies_ms()
+    assert lat is None or len(lat) == len(reqs)
+    for i, (N, Nproj, S) in enumerate(reqs):
+        lp = lpTransform(N, Nproj, S, 'ramp', N / 2, 'cubic')
+        lp.precompute(1)
+        lp.initcmem(1, 0)
+        R = torch.zeros((S, Nproj, N), device='cuda')
+        f = torch.zeros((S, N, N), device='cuda')
+        lp.fwdp(R, b.input_f(i).contiguous(), 0)
+        lp.adjp(f, b.input_R(i).contiguous(), 0)
+        torch.cuda.synchronize()
+        assert torch.equal(R, b.output_R(i)), i
+        assert torch.equal(f, b.output_f(i)), i
