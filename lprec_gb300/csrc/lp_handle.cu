@@ -131,7 +131,14 @@ struct AdjDev {
   DevBuf<float> H;         // [4N] or empty
   bool filter = false;
   DevBuf<float> rbuf;      // [Nslices][Nproj][N]
-  DevBuf<float> G[3];      // [Nslices][W2][Nrho]
+  DevBuf<float> G[3];      // [Nslices][W2][Nrho] (linear mode)
+  // cubic mode: the real log-polar columns of each span and slice as 2-D CUDA
+  // arrays (x = rho, y = theta - lo2), written through surfaces, read by gathers
+  std::vector<cudaArray_t> arr;
+  std::vector<cudaTextureObject_t> tex_h[3];
+  std::vector<cudaSurfaceObject_t> surf_h[3];
+  DevBuf<cudaTextureObject_t> tex[3];
+  DevBuf<cudaSurfaceObject_t> surf[3];
 };
 
 enum KernelId {
@@ -211,6 +218,13 @@ static void free_adj(AdjDev* a) {
   a->fz.free_();
   a->H.free_();
   a->rbuf.free_();
+  for (int k = 0; k < 3; ++k) {
+    for (cudaTextureObject_t t : a->tex_h[k]) cudaDestroyTextureObject(t);
+    for (cudaSurfaceObject_t t : a->surf_h[k]) cudaDestroySurfaceObject(t);
+    a->tex[k].free_();
+    a->surf[k].free_();
+  }
+  for (cudaArray_t x : a->arr) cudaFreeArray(x);
   delete a;
 }
 
@@ -251,6 +265,30 @@ static std::vector<float2> extend_kernel(const float* v, int Nrho, int Nth) {
 }
 
 static bool finite_coord(float v, float lim) { return isfinite(v) && fabsf(v) < lim; }
+
+// A W x H float array with a gather texture (normalised, wrap) and a surface.
+static cudaError_t make_gather_array(int W, int H, std::vector<cudaArray_t>& arrs, cudaTextureObject_t* tex,
+                                     cudaSurfaceObject_t* surf) {
+  cudaChannelFormatDesc fd = cudaCreateChannelDesc<float>();
+  cudaArray_t a = nullptr;
+  cudaError_t e = cudaMallocArray(&a, &fd, W, H, cudaArrayTextureGather | cudaArraySurfaceLoadStore);
+  if (e != cudaSuccess) return e;
+  arrs.push_back(a);
+  cudaResourceDesc rd;
+  memset(&rd, 0, sizeof(rd));
+  rd.resType = cudaResourceTypeArray;
+  rd.res.array.array = a;
+  cudaTextureDesc td;
+  memset(&td, 0, sizeof(td));
+  td.addressMode[0] = cudaAddressModeWrap;
+  td.addressMode[1] = cudaAddressModeWrap;
+  td.filterMode = cudaFilterModePoint;
+  td.readMode = cudaReadModeElementType;
+  td.normalizedCoords = 1;
+  e = cudaCreateTextureObject(tex, &rd, &td, nullptr);
+  if (e != cudaSuccess) return e;
+  return cudaCreateSurfaceObject(surf, &rd);
+}
 
 // One N x N float array per slice, written through a surface by the column
 // prefilter and read through a gather texture (normalised, wrap on both axes)
@@ -731,7 +769,25 @@ int lp_init_adj(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
     A->filter = true;
   }
   if (e == cudaSuccess) e = dev_alloc(A->rbuf, (size_t)h->Nslices * Nproj * N);
-  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = dev_alloc(A->G[k], (size_t)h->Nslices * A->W2 * Nrho);
+  int gw = 0, gh = 0;
+  cudaDeviceGetAttribute(&gw, cudaDevAttrMaxTexture2DGatherWidth, h->device);
+  cudaDeviceGetAttribute(&gh, cudaDevAttrMaxTexture2DGatherHeight, h->device);
+  const bool use_tex = h->cubic && Nrho <= gw && A->W2 <= gh;
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+    if (use_tex) {
+      for (int s = 0; s < h->Nslices && e == cudaSuccess; ++s) {
+        cudaTextureObject_t t = 0;
+        cudaSurfaceObject_t so = 0;
+        e = make_gather_array(Nrho, A->W2, A->arr, &t, &so);
+        A->tex_h[k].push_back(t);
+        A->surf_h[k].push_back(so);
+      }
+      if (e == cudaSuccess) e = dev_upload(A->tex[k], A->tex_h[k]);
+      if (e == cudaSuccess) e = dev_upload(A->surf[k], A->surf_h[k]);
+    } else {
+      e = dev_alloc(A->G[k], (size_t)h->Nslices * A->W2 * Nrho);
+    }
+  }
   if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? LP_ERR_OOM : LP_ERR_CUDA, cudaGetErrorString(e));
   free_adj(h->adj);
   h->adj = A;
@@ -769,12 +825,14 @@ int lp_device_bytes(const lp_handle* h, int64_t* bytes) {
   if (h->fwd) {
     for (int k = 0; k < 3; ++k) b += h->fwd->c2lp[k].n * 8 + h->fwd->rows[k].n * 4;
     b += h->fwd->thc.n * 4 + h->fwd->rhoc.n * 4 + h->fwd->fz.n * 8 + h->fwd->fbuf.n * 4;
+    b += (int64_t)h->fwd->arr.size() * h->N * h->N * 4;
   }
   if (h->adj) {
     for (int k = 0; k < 3; ++k)
       b += h->adj->ta[k].n * 4 + h->adj->sx[k].n * 4 + h->adj->woff[k].n * 4 + h->adj->wpt[k].n * 16 +
            h->adj->c2lp[k].n * 8 + h->adj->G[k].n * 4;
     b += h->adj->fz.n * 8 + h->adj->H.n * 4 + h->adj->rbuf.n * 4;
+    b += (int64_t)h->adj->arr.size() * h->Nrho * h->adj->W2 * 4;
   }
   *bytes = b;
   return LP_OK;
@@ -864,6 +922,8 @@ int lp_adj(lp_handle* h, float* f, const float* R, int S0, void* stream) {
   }
   for (int k = 0; k < 3; ++k) {
     if (A->chi[k] < A->clo[k]) {
+      if (!A->tex_h[k].empty())
+        return set_err(LP_ERR_UNSUPPORTED, "lp_adj: span %d has no log-polar points", k);
       CUDA_TRY(cudaMemsetAsync(A->G[k].p, 0, A->G[k].n * sizeof(float), st));
       continue;
     }
@@ -873,11 +933,15 @@ int lp_adj(lp_handle* h, float* f, const float* R, int S0, void* stream) {
     ThetaConvArgs a2{h->spec.p, A->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), A->clo[k],
                      A->chi[k], A->lo2, A->hi2, 0, h->plan_th};
     CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
-    AdjLPColsArgs a3{h->spec.p, A->G[k].p, h->Nth, h->Nrho, h->Nk, A->lo2, A->hi2, A->W2, h->plan_rho};
+    const bool tex = !A->tex_h[k].empty();
+    AdjLPColsArgs a3{h->spec.p, A->G[k].p, h->Nth, h->Nrho, h->Nk, A->lo2, A->hi2, A->W2, h->plan_rho,
+                     tex ? A->surf[k].p : nullptr};
     CUDA_TRY(launch(h, K_ADJ_LPCOLS, st, [&] { return launch_adj_lpcols(a3, S0, st); }));
   }
+  const bool tex = !A->tex_h[0].empty();
   AdjLP2CartArgs a4{A->G[0].p, A->G[1].p, A->G[2].p, A->c2lp[0].p, A->c2lp[1].p, A->c2lp[2].p, f,
-                    h->N0, h->Nth, h->Nrho, A->lo2, A->W2, h->cubic, h->N0 * h->N0};
+                    h->N0, h->Nth, h->Nrho, A->lo2, A->W2, h->cubic, h->N0 * h->N0,
+                    tex ? A->tex[0].p : nullptr, tex ? A->tex[1].p : nullptr, tex ? A->tex[2].p : nullptr};
   CUDA_TRY(launch(h, K_ADJ_LP2CART, st, [&] { return launch_adj_lp2cart(a4, S0, st); }));
   return LP_OK;
 }

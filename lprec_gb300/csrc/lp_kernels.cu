@@ -86,13 +86,14 @@ __device__ __forceinline__ float interp2d(const float* __restrict__ img, int W, 
 // margin of the integer position makes the quad selection insensitive to
 // coordinate rounding.  Gather component order: w (i-1, j-1), z (i, j-1),
 // x (i-1, j), y (i, j).
-__device__ __forceinline__ float interp_tex_cubic(cudaTextureObject_t tx, float invN, float x, float y) {
+__device__ __forceinline__ float interp_tex_cubic(cudaTextureObject_t tx, float invW, float invH, float x,
+                                                 float y) {
   const float fx = floorf(x), fy = floorf(y);
   float wx[4], wy[4];
   bspline_w(x - fx, wx);
   bspline_w(y - fy, wy);
-  const float u0 = fx * invN, u1 = (fx + 2.0f) * invN;
-  const float v0 = fy * invN, v1 = (fy + 2.0f) * invN;
+  const float u0 = fx * invW, u1 = (fx + 2.0f) * invW;
+  const float v0 = fy * invH, v1 = (fy + 2.0f) * invH;
   const float4 q00 = tex2Dgather<float4>(tx, u0, v0, 0);
   const float4 q10 = tex2Dgather<float4>(tx, u1, v0, 0);
   const float4 q01 = tex2Dgather<float4>(tx, u0, v1, 0);
@@ -158,20 +159,17 @@ __device__ __forceinline__ float* carve(float* sm, int L, int nfft, CBuf& a, CBu
 // exact to |pole|^16 ~ 7e-10; the first and last chunk use the reference's
 // boundary initialisations.  `cp` is scratch of L floats.
 // ---------------------------------------------------------------------------
-// Shared-memory position of sample p of a line processed in chunks of C:
-// one pad word per chunk makes the chunk stride odd, so the threads walking
-// their chunks in lockstep hit distinct banks.
-// (an odd chunk stride is conflict-free already and gets no pad)
-__device__ __forceinline__ int lpos(int p, int C) { return (C & 1) ? p : p + p / C; }
-// floats a line of L samples occupies when split over nth threads
-__host__ __device__ inline int line_floats(int L, int nth) {
-  const int C = (L + nth - 1) / nth;
-  return (C & 1) ? L : L + (L - 1) / C + 1;
-}
+// Lines are split into chunks of odd length C, so the threads walking their
+// chunks in lockstep (stride C) hit distinct shared-memory banks without any
+// padding.  The last chunks may be short or empty.
+__host__ __device__ inline int line_chunk(int L, int nth) { return ((L + nth - 1) / nth) | 1; }
+__device__ __forceinline__ int lpos(int p, int C) { return p; }
+// floats a line of L samples occupies
+__host__ __device__ inline int line_floats(int L, int nth) { return L; }
 
 __device__ void prefilter_line(float* line, float* cp, int L, int tid, int nth) {
   const float z = LP_POLE;
-  const int C = (L + nth - 1) / nth;
+  const int C = line_chunk(L, nth);
   const int b = tid * C;
   const int e = min(b + C, L);
   if (b < L) {
@@ -225,7 +223,7 @@ __device__ void prefilter_line(float* line, float* cp, int L, int tid, int nth) 
 // ---------------------------------------------------------------------------
 __global__ void k_fwd_ingest(FwdIngestArgs a) {
   extern __shared__ float smf[];
-  const int C = (a.N + blockDim.x - 1) / blockDim.x;
+  const int C = line_chunk(a.N, blockDim.x);
   float* line = smf;
   float* cp = smf + line_floats(a.N, blockDim.x);
   const int s = blockIdx.x;
@@ -359,11 +357,11 @@ __global__ void __launch_bounds__(256, 2) k_fwd_c2lp(FwdC2LPArgs a) {
     const float2 pa = __ldg(ca + r);
     float va = 0.f, vb = 0.f;
     if (!isnan(pa.x))
-      va = e * (use_tex ? interp_tex_cubic(tx, invN, pa.x, pa.y) : interp2d(img, a.N, a.N, pa.x, pa.y, a.cubic));
+      va = e * (use_tex ? interp_tex_cubic(tx, invN, invN, pa.x, pa.y) : interp2d(img, a.N, a.N, pa.x, pa.y, a.cubic));
     if (thb >= 0) {
       const float2 pb = __ldg(cb + r);
       if (!isnan(pb.x))
-        vb = e * (use_tex ? interp_tex_cubic(tx, invN, pb.x, pb.y) : interp2d(img, a.N, a.N, pb.x, pb.y, a.cubic));
+        vb = e * (use_tex ? interp_tex_cubic(tx, invN, invN, pb.x, pb.y) : interp2d(img, a.N, a.N, pb.x, pb.y, a.cubic));
     }
     A.set(r, make_float2(va, vb));
   }
@@ -506,7 +504,7 @@ __global__ void __launch_bounds__(256, 2) k_adj_ingest(AdjIngestArgs a) {
   CBuf F0, F1;
   float* lines = filt ? carve(smf, M, 1, F0, F1) : smf;  // 2 rows, chunked layout
   const int half = blockDim.x / 2;
-  const int C = (N + half - 1) / half;
+  const int C = line_chunk(N, half);
   const int LF = line_floats(N, half);
   float* cp = lines + 2 * LF;                            // 2 rows of scratch
   const int s = blockIdx.x;
@@ -651,8 +649,13 @@ __global__ void __launch_bounds__(256, 2) k_adj_lpcols(AdjLPColsArgs a) {
   float* g0 = a.G + ((size_t)s * a.W2 + (th0 - a.lo2)) * a.Nrho;
   for (int r = threadIdx.x; r < a.Nrho; r += blockDim.x) {
     const float2 v = z.get(r);
-    g0[r] = v.x;
-    if (th1 >= 0) g0[a.Nrho + r] = v.y;
+    if (a.surf) {
+      surf2Dwrite(v.x, a.surf[s], r * (int)sizeof(float), th0 - a.lo2);
+      if (th1 >= 0) surf2Dwrite(v.y, a.surf[s], r * (int)sizeof(float), th1 - a.lo2);
+    } else {
+      g0[r] = v.x;
+      if (th1 >= 0) g0[a.Nrho + r] = v.y;
+    }
   }
 }
 
@@ -693,6 +696,18 @@ __global__ void k_adj_lp2cart(AdjLP2CartArgs a) {
   const size_t gs = (size_t)s * a.W2 * a.Nrho;
   float acc = 0.f;
   const float2 t0 = __ldg(a.c2lp0 + p);
+  if (a.tex0) {
+    // texture x = rho (wrap over Nrho), y = theta - lo2 (taps stay inside the stored band)
+    if (!isnan(t0.x)) {
+      const float iw = 1.0f / (float)a.Nrho, ih = 1.0f / (float)a.W2, l2 = (float)a.lo2;
+      const float2 t1 = __ldg(a.c2lp1 + p), t2 = __ldg(a.c2lp2 + p);
+      acc += interp_tex_cubic(a.tex0[s], iw, ih, t0.y, t0.x - l2);
+      acc += interp_tex_cubic(a.tex1[s], iw, ih, t1.y, t1.x - l2);
+      acc += interp_tex_cubic(a.tex2[s], iw, ih, t2.y, t2.x - l2);
+    }
+    a.fout[(size_t)s * a.npix + p] = acc;
+    return;
+  }
   if (!isnan(t0.x)) {
     acc += interp_cols(a.G0 + gs, a.Nrho, a.Nth, a.lo2, a.W2, t0, a.cubic);
     acc += interp_cols(a.G1 + gs, a.Nrho, a.Nth, a.lo2, a.W2, __ldg(a.c2lp1 + p), a.cubic);
@@ -875,11 +890,11 @@ __global__ void __launch_bounds__(256, 3) k_fwd_c2lp_p2(FwdC2LPArgs a) {
       const float e = __ldg(a.erho + r);
       const float2 pa = __ldg(ca + r);
       if (!isnan(pa.x))
-        va = e * (use_tex ? interp_tex_cubic(tx, invN, pa.x, pa.y) : interp2d(img, a.N, a.N, pa.x, pa.y, a.cubic));
+        va = e * (use_tex ? interp_tex_cubic(tx, invN, invN, pa.x, pa.y) : interp2d(img, a.N, a.N, pa.x, pa.y, a.cubic));
       if (thb >= 0) {
         const float2 pb = __ldg(cb + r);
         if (!isnan(pb.x))
-          vb = e * (use_tex ? interp_tex_cubic(tx, invN, pb.x, pb.y)
+          vb = e * (use_tex ? interp_tex_cubic(tx, invN, invN, pb.x, pb.y)
                             : interp2d(img, a.N, a.N, pb.x, pb.y, a.cubic));
       }
     }
@@ -1039,7 +1054,7 @@ __global__ void __launch_bounds__(256, 2) k_adj_ingest_p2(AdjIngestArgs a) {
   const bool filt = a.H != nullptr;
   float2* sm = sm2;
   const int half = T / 2;
-  const int C = (N + half - 1) / half;
+  const int C = line_chunk(N, half);
   const int LF = line_floats(N, half);
   float* lines = reinterpret_cast<float*>(sm2 + (filt ? P2<L>::SLOTS : 0));  // 2 rows, chunked layout
   float* cp = lines + 2 * LF;
@@ -1219,8 +1234,13 @@ __global__ void __launch_bounds__(256, 3) k_adj_lpcols_p2(AdjLPColsArgs a) {
   float* g0 = a.G + ((size_t)s * a.W2 + (th0 - a.lo2)) * L;
   for (int r = t; r < L; r += T) {
     const float2 z = sm[spad(r)];
-    g0[r] = z.x;
-    if (th1 >= 0) g0[L + r] = z.y;
+    if (a.surf) {
+      surf2Dwrite(z.x, a.surf[s], r * (int)sizeof(float), th0 - a.lo2);
+      if (th1 >= 0) surf2Dwrite(z.y, a.surf[s], r * (int)sizeof(float), th1 - a.lo2);
+    } else {
+      g0[r] = z.x;
+      if (th1 >= 0) g0[L + r] = z.y;
+    }
   }
 }
 

@@ -78,6 +78,7 @@ struct AdjLPColsArgs {        // inverse FFT along rho, write real log-polar col
   float* G;                   // [S][W2][Nrho]
   int Nth, Nrho, Nk, lo2, hi2, W2;
   FFTPlan plan;
+  const cudaSurfaceObject_t* surf;  // if set: columns go to per-slice 2-D arrays (x = rho, y = theta - lo2)
 };
 
 struct AdjLP2CartArgs {       // log-polar -> Cartesian gather summed over spans, crop
@@ -90,6 +91,9 @@ struct AdjLP2CartArgs {       // log-polar -> Cartesian gather summed over spans
   float* fout;                // [S][N0][N0]
   int N0, Nth, Nrho, lo2, W2, cubic;
   int npix;
+  const cudaTextureObject_t* tex0;  // if set (cubic): the columns of each span and slice as gather textures
+  const cudaTextureObject_t* tex1;
+  const cudaTextureObject_t* tex2;
 };
 
 // launches (defined in lp_kernels.cu); return the launch error
