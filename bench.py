@@ -475,6 +475,137 @@ def run_ours(args):
         print(json.dumps(line))
 
 
+def run_report(args):
+    """Precision and differentiation report (float64 oracle comparisons)."""
+    import torch
+    sys.path.insert(0, ROOT)
+    from oracle import lprec_oracle as O
+    from lprec_gb300.lpTransform import lpTransform
+    from lprec_gb300 import lpmethods
+    from lprec_gb300.autograd import radon
+    rep = {}
+
+    def rel(a, b):
+        return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+
+    # (1) N=2048, Nproj=3000: fwd, adj, FBP against the float64 oracle (float64 tables, unrounded)
+    N, Nproj = 2048, 3000
+    rng = np.random.default_rng(3)
+    f = O.ellipse_phantom(N, 30, rng)[None]
+    t0 = time.perf_counter()
+    tr64 = O.Transform(N, Nproj, 1, "shepp-logan", N / 2, "cubic", mode="fp64", rounded=False)
+    R64 = tr64.fwd(f)
+    Rn = R64 + 0.01 * np.abs(R64).max() * rng.standard_normal(R64.shape)
+    fbp64 = tr64.adj(Rn)
+    tr64n = O.Transform(N, Nproj, 1, "none", N / 2, "cubic", mode="fp64", rounded=False)
+    adj64 = tr64n.adj(Rn)
+    t_oracle = time.perf_counter() - t0
+    for prec in ("fp64", "reference"):
+        out = {}
+        for filt, ref in (("shepp-logan", fbp64), ("none", adj64)):
+            lp = lpTransform(N, Nproj, 1, filt, N / 2, "cubic", precision=prec)
+            lp.precompute(1)
+            lp.initcmem(1, 0)
+            if filt == "none":
+                out["fwd"] = rel(lp.fwd(np.float32(f)), R64)
+                out["adj"] = rel(lp.adj(np.float32(Rn)), ref)
+            else:
+                out["fbp"] = rel(lp.adj(np.float32(Rn)), ref)
+            lp.close()
+        rep["n2048_vs_fp64_oracle_tables_" + prec] = out
+    rep["n2048_oracle_seconds"] = round(t_oracle, 1)
+
+    # (2) N=512: CG x30 and EM x30 against float64 oracle solvers
+    N, Nproj = 512, 768
+    rng = np.random.default_rng(3)
+    f = O.ellipse_phantom(N, 30, rng)[None]
+    tr = O.Transform(N, Nproj, 1, "none", N / 2, "cubic", mode="fp64", rounded=False)
+    R = tr.fwd(f)
+    Rn = R + 0.01 * np.abs(R).max() * rng.standard_normal(R.shape)
+    lp = lpTransform(N, Nproj, 1, "none", N / 2, "cubic")
+    lp.precompute(1)
+    lp.initcmem(1, 0)
+    z = np.zeros((1, N, N), np.float32)
+    rep["n512_cg30_vs_fp64_oracle"] = rel(lpmethods.cg(lp, z, np.float32(Rn), 30, 0, 0),
+                                          O.solve_cg(tr, z.astype(np.float64), Rn, 30))
+    Rp = np.abs(Rn)
+    rep["n512_em30_vs_fp64_oracle"] = rel(lpmethods.em(lp, z + 1e-3, np.float32(Rp), 30, 0.01, 0),
+                                          O.solve_em(tr, z.astype(np.float64) + 1e-3, Rp, 30, 0.01))
+
+    # (3) differentiation, N=512, Nproj=768, 16 slices, Poisson data at 1e4 photons/ray
+    S = 16
+    rng = np.random.default_rng(2)
+    ph = np.stack([O.ellipse_phantom(N, 10, rng) for _ in range(S)]).astype(np.float32)
+    lp16 = lpTransform(N, Nproj, S, "none", N / 2, "cubic")
+    lp16.precompute(1)
+    lp16.initcmem(1, 0)
+    Rt = torch.zeros((S, Nproj, N), device="cuda")
+    lp16.fwdp(Rt, torch.as_tensor(ph).cuda(), 0)
+    P = Rt.cpu().double().numpy()
+    scale = 3.0 / P.max()          # attenuation scaled so that the largest line integral is 3
+    P = P * scale
+    counts = rng.poisson(1e4 * np.exp(-P))
+    data = np.float32(-np.log(np.maximum(counts, 1) / 1e4))
+    x0 = torch.zeros((S, N, N), device="cuda", requires_grad=True)
+    y = torch.as_tensor(data).cuda()
+    loss = 0.5 * ((radon(x0 + torch.as_tensor(ph).cuda() * 0.5, lp16, 0) - y) ** 2).sum()
+    loss.backward()
+    grad = x0.grad.cpu().double().numpy()
+    # finite differences with the float64 oracle on 2 slices (same float32 tables)
+    tr2 = O.Transform.from_packed(lp16.glpars, lp16.fwdparsi, lp16.fwdparamsf, lp16.adjparsi, lp16.adjparamsf)
+    xx = ph[:2].astype(np.float64) * 0.5
+
+    def L(v):
+        return 0.5 * np.sum((tr2.fwd(v) - data[:2]) ** 2)
+    errs = []
+    drng = np.random.default_rng(7)
+    for i in range(8):
+        d = drng.standard_normal(xx.shape)
+        fd = (L(xx + 1e-3 * d) - L(xx - 1e-3 * d)) / 2e-3
+        errs.append(abs(fd - np.sum(grad[:2] * d)) / np.linalg.norm(grad[:2]))
+    rep["grad_fd_max_err_over_norm"] = float(max(errs))
+    # the reference's adjoint as a gradient: R_adj(R f - y) vs the exact transpose
+    resid = torch.zeros((S, Nproj, N), device="cuda")
+    lp16.fwdp(resid, torch.as_tensor(ph * 0.5).cuda(), 0)
+    resid -= y
+    gadj = torch.zeros((S, N, N), device="cuda")
+    lp16.adjp(gadj, resid, 0)
+    rep["grad_vs_reference_adj_rel_l2"] = rel(gadj.cpu().numpy(), grad)
+    # dot test
+    fr = np.random.default_rng(0).random((S, N, N), dtype=np.float32)
+    gr = np.random.default_rng(1).random((S, Nproj, N), dtype=np.float32)
+    Rf = torch.zeros((S, Nproj, N), device="cuda")
+    lp16.fwdp(Rf, torch.as_tensor(fr).cuda(), 0)
+    fT = torch.zeros((S, N, N), device="cuda")
+    lp16.fwdp_T(fT, torch.as_tensor(gr).cuda(), 0)
+    lhs = float(np.sum(Rf.cpu().double().numpy() * gr))
+    rhs = float(np.sum(fr.astype(np.float64) * fT.cpu().double().numpy()))
+    rep["dot_test_exact_transpose"] = abs(lhs - rhs) / abs(lhs)
+    Ra = torch.zeros((S, N, N), device="cuda")
+    lp16.adjp(Ra, torch.as_tensor(gr).cuda(), 0)
+    rhs2 = float(np.sum(fr.astype(np.float64) * Ra.cpu().double().numpy()))
+    rep["dot_test_reference_adj"] = abs(lhs - rhs2) / abs(lhs)
+    # CG x50 (exact normal equations) and TV gradient descent x100 (lambda 1e-3)
+    z = np.zeros((S, N, N), np.float32)
+
+    def resid_norm(x):
+        Rx = torch.zeros((S, Nproj, N), device="cuda")
+        lp16.fwdp(Rx, torch.as_tensor(x).cuda(), 0)
+        return float(torch.linalg.vector_norm((Rx - y).double()) / torch.linalg.vector_norm(y.double()))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    xc = lpmethods.cg_exact(lp16, z, data, 50, 0, 0)
+    t_cg = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    xt = lpmethods.tv_gd(lp16, z, data, 100, 1e-3, 0)
+    t_tv = time.perf_counter() - t0
+    rep["cg50_exact"] = {"relative_residual": resid_norm(xc), "seconds": round(t_cg, 2),
+                         "rel_l2_to_phantom": rel(xc, ph * scale)}
+    rep["tv_gd100"] = {"relative_residual": resid_norm(xt), "seconds": round(t_tv, 2),
+                       "rel_l2_to_phantom": rel(xt, ph * scale)}
+    print(json.dumps(rep))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -485,8 +616,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--slices", type=int, default=0, help="batch size (default 128); for profiling runs")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-geometry graph batch")
+    ap.add_argument("--report", action="store_true", help="precision / differentiation report instead of timing")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.report:
+        run_report(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -145,6 +145,15 @@ const char* lp_kernel_name(int id);
 int lp_set_profiling(lp_handle* h, int enable);
 int lp_profile_collect(lp_handle* h, double* ms, int64_t* launches);
 
+/*
+ * Test hook (no reference counterpart): fill the handle's intermediate device
+ * buffers (log-polar spectrum, prefiltered image and sinogram, log-polar
+ * columns) with `value`, enqueued on `stream`.  Results of later calls must
+ * not depend on it: every buffer element a kernel reads was written earlier
+ * in the same call.
+ */
+int lp_debug_fill_scratch(lp_handle* h, float value, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

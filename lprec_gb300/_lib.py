@@ -23,7 +23,7 @@ PRECISION = {"reference": 0, "fp64": 1}
 EXPORTS = ("lp_last_error", "lp_version", "lp_precompute_sizes", "lp_precompute", "lp_create", "lp_init_fwd",
            "lp_init_adj", "lp_destroy", "lp_fwd", "lp_adj", "lp_get_geometry", "lp_device_bytes",
            "lp_launch_count", "lp_kernel_count", "lp_kernel_name", "lp_set_profiling", "lp_profile_collect",
-           "lp_fwd_noalloc", "lp_noalloc_scratch_bytes", "lp_fwd_transpose")
+           "lp_fwd_noalloc", "lp_noalloc_scratch_bytes", "lp_fwd_transpose", "lp_debug_fill_scratch")
 
 
 class LprecError(RuntimeError):
@@ -69,6 +69,7 @@ def lib():
         "lp_kernel_name": (c_char_p, [c_int]),
         "lp_set_profiling": (c_int, [c_void_p, c_int]),
         "lp_profile_collect": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_double), P_i64]),
+        "lp_debug_fill_scratch": (c_int, [c_void_p, ctypes.c_float, c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -163,6 +164,10 @@ class Handle:
         b = np.zeros(1, np.int64)
         check(lib().lp_device_bytes(self._h, _ptr(b, ctypes.c_int64)))
         return int(b[0])
+
+    def debug_fill_scratch(self, value, stream):
+        """Fill the intermediate buffers with `value` (test hook: results must not change)."""
+        check(lib().lp_debug_fill_scratch(self._h, float(value), stream))
 
     def set_profiling(self, on):
         check(lib().lp_set_profiling(self._h, 1 if on else 0))

@@ -116,6 +116,7 @@ struct FwdDev {
   DevBuf<int2> blk[3];
   int nblk[3] = {0, 0, 0};
   int dlo = 0, dhi = -1;
+  DevBuf<int2> ival;       // [Nth] rho interval of each column's disk points (same for every span)
 };
 static const int kTransposeCW = 8;
 
@@ -197,6 +198,7 @@ static void free_fwd(FwdDev* f) {
   f->rhoc.free_();
   f->fz.free_();
   f->fbuf.free_();
+  f->ival.free_();
   for (cudaTextureObject_t t : f->tex_h) cudaDestroyTextureObject(t);
   for (cudaSurfaceObject_t t : f->surf_h) cudaDestroySurfaceObject(t);
   for (cudaArray_t a : f->arr) cudaFreeArray(a);
@@ -524,6 +526,7 @@ int lp_init_fwd(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
 
   FwdDev* F = new FwdDev();
   const float lim = 8.0f * (float)Nrho;
+  std::vector<int2> ival(Nth, make_int2(1, 0));
   // dense column-major Cartesian coordinates of every log-polar point
   std::vector<float2> c2lp((size_t)Nth * Nrho);
   for (int k = 0; k < 3; ++k) {
@@ -537,6 +540,9 @@ int lp_init_fwd(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
       }
       const int r = idx / Nth, t = idx % Nth;
       c2lp[(size_t)t * Nrho + r] = make_float2(x, y);
+      int2& iv = ival[t];
+      if (iv.y < iv.x) iv = make_int2(r, r);
+      else iv = make_int2(std::min(iv.x, r), std::max(iv.y, r));
       if (F->dhi < F->dlo) {
         F->dlo = t;
         F->dhi = t;
@@ -547,6 +553,7 @@ int lp_init_fwd(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
     }
     DeviceGuard g(h->device);
     cudaError_t e = dev_upload(F->c2lp[k], c2lp);
+    if (e == cudaSuccess && k == 0) e = dev_upload(F->ival, ival);
     if (e != cudaSuccess) {
       free_fwd(F);
       return set_err(LP_ERR_OOM, "lp_init_fwd: %s", cudaGetErrorString(e));
@@ -819,6 +826,32 @@ int lp_get_geometry(const lp_handle* h, int32_t out[10]) {
   return LP_OK;
 }
 
+namespace {
+__global__ void k_fill(float* p, size_t n, float v) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+cudaError_t fill_async(float* p, size_t n, float v, cudaStream_t st) {
+  if (!p || n == 0) return cudaSuccess;
+  k_fill<<<1024, 256, 0, st>>>(p, n, v);
+  return cudaGetLastError();
+}
+}  // namespace
+
+int lp_debug_fill_scratch(lp_handle* h, float value, void* stream) {
+  if (!h) return set_err(LP_ERR_ARG, "lp_debug_fill_scratch: null handle");
+  DeviceGuard g(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = fill_async((float*)h->spec.p, h->spec.n * 2, value, st);
+  if (e == cudaSuccess && h->fwd) e = fill_async(h->fwd->fbuf.p, h->fwd->fbuf.n, value, st);
+  if (e == cudaSuccess && h->adj) {
+    e = fill_async(h->adj->rbuf.p, h->adj->rbuf.n, value, st);
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = fill_async(h->adj->G[k].p, h->adj->G[k].n, value, st);
+  }
+  if (e != cudaSuccess) return set_err(LP_ERR_CUDA, "lp_debug_fill_scratch: %s", cudaGetErrorString(e));
+  return LP_OK;
+}
+
 int lp_device_bytes(const lp_handle* h, int64_t* bytes) {
   if (!h || !bytes) return set_err(LP_ERR_ARG, "lp_device_bytes: null pointer");
   int64_t b = h->erho.n * 4 + h->spec.n * 8 + h->tw_rho.n * 8 + h->tw_th.n * 8;
@@ -856,10 +889,10 @@ int lp_fwd(lp_handle* h, float* R, const float* f, int S0, void* stream) {
   }
   for (int k = 0; k < 3; ++k) {
     FwdC2LPArgs a1{F->fbuf.p, h->spec.p, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, h->cubic,
-                   h->plan_rho, tex ? F->tex.p : nullptr};
+                   h->plan_rho, tex ? F->tex.p : nullptr, F->ival.p, F->dlo, F->dhi};
     CUDA_TRY(launch(h, K_FWD_C2LP, st, [&] { return launch_fwd_c2lp(a1, S0, st); }));
-    ThetaConvArgs a2{h->spec.p, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), 0, h->Nth - 1,
-                     F->lo, F->hi, 0, h->plan_th};
+    ThetaConvArgs a2{h->spec.p, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), F->dlo, F->dhi,
+                     F->lo & ~1, std::min(F->hi | 1, h->Nth - 1), 0, h->plan_th};
     CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
     FwdLP2PolarArgs a3{h->spec.p, R, F->thc.p, F->rhoc.p, F->rows[k].p, F->nrows[k], h->N, h->N0, h->Nth,
                        h->Nrho, h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho};
@@ -1030,10 +1063,11 @@ extern "C" int lp_fwd_noalloc(lp_handle* h, float* R, const float* f, int S0, vo
     CUDA_TRY(launch(h, K_COL_PREFILTER, st, [&] { return launch_col_prefilter(ca, S0, st); }));
   }
   for (int k = 0; k < 3; ++k) {
-    FwdC2LPArgs a1{fbuf, spec, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, h->cubic, h->plan_rho};
+    FwdC2LPArgs a1{fbuf, spec, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, h->cubic, h->plan_rho,
+                   nullptr, F->ival.p, F->dlo, F->dhi};
     CUDA_TRY(launch(h, K_FWD_C2LP, st, [&] { return launch_fwd_c2lp(a1, S0, st); }));
-    ThetaConvArgs a2{spec, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), 0, h->Nth - 1,
-                     F->lo, F->hi, 0, h->plan_th};
+    ThetaConvArgs a2{spec, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), F->dlo, F->dhi,
+                     F->lo & ~1, std::min(F->hi | 1, h->Nth - 1), 0, h->plan_th};
     CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
     FwdLP2PolarArgs a3{spec, R, F->thc.p, F->rhoc.p, F->rows[k].p, F->nrows[k], h->N, h->N0, h->Nth,
                        h->Nrho, h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho};

@@ -291,6 +291,17 @@ __global__ void k_col_prefilter(ColPrefilterArgs a) {
       for (int i = 0; i < LP_WARM; ++i) prev = LP_LAMBDA * wu[i] + z * prev;
       n = b;
     }
+    // groups of 8: the loads of a group are issued before its recursion steps
+    for (; n + 8 <= e; n += 8) {
+      float xv[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) xv[i] = col[(size_t)(n + i) * W];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        prev = LP_LAMBDA * xv[i] + z * prev;
+        col[(size_t)(n + i) * W] = prev;
+      }
+    }
     for (; n < e; ++n) {
       prev = LP_LAMBDA * col[(size_t)n * W] + z * prev;
       col[(size_t)n * W] = prev;
@@ -325,6 +336,17 @@ __global__ void k_col_prefilter(ColPrefilterArgs a) {
       c = -z * wu[LP_WARM - 1];
       for (int i = LP_WARM - 2; i >= 0; --i) c = z * (c - wu[i]);
       n = e - 1;
+    }
+    for (; n - 8 >= b - 1; n -= 8) {
+      float xv[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) xv[i] = col[(size_t)(n - i) * W];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        c = z * (c - xv[i]);
+        if (a.surf) surf2Dwrite(c, so, x * (int)sizeof(float), n - i);
+        else col[(size_t)(n - i) * W] = c;
+      }
     }
     for (; n >= b; --n) {
       c = z * (c - col[(size_t)n * W]);
@@ -697,13 +719,20 @@ __global__ void k_adj_lp2cart(AdjLP2CartArgs a) {
   float acc = 0.f;
   const float2 t0 = __ldg(a.c2lp0 + p);
   if (a.tex0) {
-    // texture x = rho (wrap over Nrho), y = theta - lo2 (taps stay inside the stored band)
-    if (!isnan(t0.x)) {
+    // texture x = rho (wrap over Nrho), y = theta - lo2 (taps stay inside the stored band).
+    // Straight-line: the three spans' twelve gathers are in flight together; pixels
+    // outside the disk sample (0, 0) and are discarded, warps entirely outside skip.
+    const bool ok = !isnan(t0.x);
+    if (__any_sync(__activemask(), ok)) {
       const float iw = 1.0f / (float)a.Nrho, ih = 1.0f / (float)a.W2, l2 = (float)a.lo2;
-      const float2 t1 = __ldg(a.c2lp1 + p), t2 = __ldg(a.c2lp2 + p);
-      acc += interp_tex_cubic(a.tex0[s], iw, ih, t0.y, t0.x - l2);
-      acc += interp_tex_cubic(a.tex1[s], iw, ih, t1.y, t1.x - l2);
-      acc += interp_tex_cubic(a.tex2[s], iw, ih, t2.y, t2.x - l2);
+      float2 t1 = __ldg(a.c2lp1 + p), t2 = __ldg(a.c2lp2 + p);
+      const float2 q0 = ok ? make_float2(t0.y, t0.x - l2) : make_float2(0.f, 0.f);
+      const float2 q1 = ok ? make_float2(t1.y, t1.x - l2) : make_float2(0.f, 0.f);
+      const float2 q2 = ok ? make_float2(t2.y, t2.x - l2) : make_float2(0.f, 0.f);
+      const float v = interp_tex_cubic(a.tex0[s], iw, ih, q0.x, q0.y) +
+                      interp_tex_cubic(a.tex1[s], iw, ih, q1.x, q1.y) +
+                      interp_tex_cubic(a.tex2[s], iw, ih, q2.x, q2.y);
+      acc = ok ? v : 0.f;
     }
     a.fout[(size_t)s * a.npix + p] = acc;
     return;
@@ -864,7 +893,16 @@ struct P2 {
   static constexpr int SLOTS = reg_fft_slots(L);
 };
 
-// forward, per span: Cartesian -> log-polar gather for column pairs, e^rho, FFT along rho
+// forward, per span: Cartesian -> log-polar gather for column pairs, e^rho, FFT along rho.
+// The disk points of a column form one rho interval (a.ival), so the two
+// columns' points are enumerated as one compact list and gathered in
+// straight-line groups of kGatherUnroll per thread: every thread keeps that
+// many independent texture gathers in flight and no fetch is spent outside the
+// disk.  Values land in the zeroed shared buffer at their rho position (real
+// part: column th, imaginary part: column th+1), from which the register FFT
+// takes its inputs.
+constexpr int kGatherUnroll = 4;
+
 template <int L>
 __global__ void __launch_bounds__(256, 3) k_fwd_c2lp_p2(FwdC2LPArgs a) {
   extern __shared__ float2 sm2[];
@@ -872,34 +910,48 @@ __global__ void __launch_bounds__(256, 3) k_fwd_c2lp_p2(FwdC2LPArgs a) {
   const int sig = threadIdx.x / T, t = threadIdx.x % T;
   float2* sm = sm2 + sig * P2<L>::SLOTS;
   const int s = blockIdx.x;
-  const int th = 2 * (blockIdx.y * P2<L>::NSIG + sig);
-  const bool live = th < a.Nth;
-  const int thb = (live && th + 1 < a.Nth) ? th + 1 : -1;
+  const int th = 2 * ((a.col_lo >> 1) + blockIdx.y * P2<L>::NSIG + sig);
+  const bool live = th <= a.col_hi && th < a.Nth;
+  const bool has_b = live && th + 1 < a.Nth;
+  const int2 ia = live ? __ldg(a.ival + th) : make_int2(1, 0);
+  const int2 ib = has_b ? __ldg(a.ival + th + 1) : make_int2(1, 0);
+  const int na = max(0, ia.y - ia.x + 1), nb = max(0, ib.y - ib.x + 1);
+  const int n = na + nb;
   const float* img = a.fbuf + (size_t)s * a.N * a.N;
-  const float2* ca = a.c2lp + (size_t)(live ? th : 0) * L;
-  const float2* cb = a.c2lp + (size_t)max(thb, 0) * L;
   const bool use_tex = a.tex != nullptr;
   const cudaTextureObject_t tx = use_tex ? a.tex[s] : 0;
   const float invN = 1.0f / (float)a.N;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) sm[spad(t + i * T)] = make_float2(0.f, 0.f);
+  __syncthreads();
+  float* smf = reinterpret_cast<float*>(sm);
+  for (int j0 = 0; j0 < n; j0 += kGatherUnroll * T) {
+    float val[kGatherUnroll];
+    int pos[kGatherUnroll];
+#pragma unroll
+    for (int u = 0; u < kGatherUnroll; ++u) {
+      const int j = j0 + u * T + t;
+      const bool inb = j < n;
+      const bool isa = j < na;
+      const int r = inb ? (isa ? ia.x + j : ib.x + (j - na)) : 0;
+      const int col = (inb && !isa) ? th + 1 : th;
+      float2 p = __ldg(a.c2lp + (size_t)col * L + r);
+      const bool ok = inb && !isnan(p.x);
+      if (!ok) p = make_float2(0.f, 0.f);
+      const float e = __ldg(a.erho + r);
+      const float v = use_tex ? interp_tex_cubic(tx, invN, invN, p.x, p.y) : interp2d(img, a.N, a.N, p.x, p.y, a.cubic);
+      val[u] = ok ? e * v : 0.f;
+      pos[u] = inb ? 2 * spad(r) + (isa ? 0 : 1) : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < kGatherUnroll; ++u)
+      if (pos[u] >= 0) smf[pos[u]] = val[u];
+  }
+  __syncthreads();
   float2 v[16];
 #pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    const int r = t + i * T;
-    float va = 0.f, vb = 0.f;
-    if (live) {
-      const float e = __ldg(a.erho + r);
-      const float2 pa = __ldg(ca + r);
-      if (!isnan(pa.x))
-        va = e * (use_tex ? interp_tex_cubic(tx, invN, invN, pa.x, pa.y) : interp2d(img, a.N, a.N, pa.x, pa.y, a.cubic));
-      if (thb >= 0) {
-        const float2 pb = __ldg(cb + r);
-        if (!isnan(pb.x))
-          vb = e * (use_tex ? interp_tex_cubic(tx, invN, invN, pb.x, pb.y)
-                            : interp2d(img, a.N, a.N, pb.x, pb.y, a.cubic));
-      }
-    }
-    v[i] = make_float2(va, vb);
-  }
+  for (int i = 0; i < 16; ++i) v[i] = sm[spad(t + i * T)];
+  __syncthreads();
   reg_fft<L, -1>(v, sm, t);
   if (!live) return;
   float2* out = a.spec + (size_t)s * a.Nk * a.Nth;
@@ -908,7 +960,7 @@ __global__ void __launch_bounds__(256, 3) k_fwd_c2lp_p2(FwdC2LPArgs a) {
     const float2 z2 = sm[spad((L - k) & (L - 1))];
     const float4 pr = make_float4(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y), 0.5f * (z1.y + z2.y),
                                   0.5f * (z2.x - z1.x));
-    if (thb >= 0) *reinterpret_cast<float4*>(out + (size_t)k * a.Nth + th) = pr;
+    if (has_b) *reinterpret_cast<float4*>(out + (size_t)k * a.Nth + th) = pr;
     else out[(size_t)k * a.Nth + th] = make_float2(pr.x, pr.y);
   }
 }
@@ -988,25 +1040,32 @@ __global__ void __launch_bounds__(256, 3) k_fwd_lp2polar_p2(FwdLP2PolarArgs a) {
   const int cu = min(c0, r1 >= 0 ? c1 : c0);
   const int nu = max(c0, r1 >= 0 ? c1 : c0) - cu + ntap;
   const bool run = nu <= 8 && cu >= 0 && cu + nu <= a.Nth;
-  float u0[8], u1[8];
+  // the run read as 16-byte pairs of columns from an even column cu2 (Nth is even);
+  // the theta convolution writes whole even-aligned column pairs around the
+  // taps, so the extra column of a pair holds finite data (its weight is 0)
+  const int cu2 = cu & ~1;
+  const int nq = (cu + nu - cu2 + 1) >> 1;
+  float u0[10], u1[10];
 #pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    const int j0 = cu + q - c0, j1 = cu + q - c1;
+  for (int q = 0; q < 10; ++q) {
+    const int j0 = cu2 + q - c0, j1 = cu2 + q - c1;
     u0[q] = (j0 >= 0 && j0 < ntap) ? w0[j0] : 0.f;
     u1[q] = (r1 >= 0 && j1 >= 0 && j1 < ntap) ? w1[j1] : 0.f;
   }
+#pragma unroll 3
   for (int kk = t; kk <= L / 2; kk += T) {
     const float2* row = sp + (size_t)kk * a.Nth;
     float2 v0 = make_float2(0.f, 0.f), v1 = make_float2(0.f, 0.f);
     if (run) {
+      const float4* row4 = reinterpret_cast<const float4*>(row + cu2);
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        if (q < nu) {
-          const float2 z = row[cu + q];
-          v0.x += u0[q] * z.x;
-          v0.y += u0[q] * z.y;
-          v1.x += u1[q] * z.x;
-          v1.y += u1[q] * z.y;
+      for (int q = 0; q < 5; ++q) {
+        if (q < nq) {
+          const float4 z = row4[q];
+          v0.x += u0[2 * q] * z.x + u0[2 * q + 1] * z.z;
+          v0.y += u0[2 * q] * z.y + u0[2 * q + 1] * z.w;
+          v1.x += u1[2 * q] * z.x + u1[2 * q + 1] * z.z;
+          v1.y += u1[2 * q] * z.y + u1[2 * q + 1] * z.w;
         }
       }
     } else {
@@ -1027,21 +1086,25 @@ __global__ void __launch_bounds__(256, 3) k_fwd_lp2polar_p2(FwdLP2PolarArgs a) {
 #pragma unroll
   for (int i = 0; i < 16; ++i) v[i] = sm[spad(t + i * T)];
   __syncthreads();
+  // rho coordinates of both rows' N = 8 T polar points, loaded while the FFT runs
+  float tr0[8], tr1[8];
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    tr0[m] = __ldg(a.rhoc + (size_t)r0 * a.N + t + m * T);
+    tr1[m] = __ldg(a.rhoc + (size_t)max(r1, 0) * a.N + t + m * T);
+  }
   reg_fft<L, 1>(v, sm, t);
   if (!live) return;
-  for (int x = t; x < a.N; x += T) {
+  const bool o0 = r0 % a.os == 0, o1 = r1 >= 0 && r1 % a.os == 0;
+  float* out0 = a.Rout + ((size_t)s * a.Nproj0 + r0 / a.os) * a.N0;
+  float* out1 = a.Rout + ((size_t)s * a.Nproj0 + max(r1, 0) / a.os) * a.N0;
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    const int x = t + m * T;
     const int xo = x - a.cor_off;
     if (xo < 0 || xo >= a.N0) continue;
-    if (r0 % a.os == 0) {
-      const float tr = __ldg(a.rhoc + (size_t)r0 * a.N + x);
-      const float val = interp1d([&](int i) { return sm[spad(i)].x; }, L, tr, a.cubic);
-      a.Rout[((size_t)s * a.Nproj0 + r0 / a.os) * a.N0 + xo] = val;
-    }
-    if (r1 >= 0 && r1 % a.os == 0) {
-      const float tr = __ldg(a.rhoc + (size_t)r1 * a.N + x);
-      const float val = interp1d([&](int i) { return sm[spad(i)].y; }, L, tr, a.cubic);
-      a.Rout[((size_t)s * a.Nproj0 + r1 / a.os) * a.N0 + xo] = val;
-    }
+    if (o0) out0[xo] = interp1d([&](int i) { return sm[spad(i)].x; }, L, tr0[m], a.cubic);
+    if (o1) out1[xo] = interp1d([&](int i) { return sm[spad(i)].y; }, L, tr1[m], a.cubic);
   }
 }
 
@@ -1137,11 +1200,20 @@ __global__ void __launch_bounds__(256, 3) k_adj_polar2lp_p2(AdjPolar2LPArgs a) {
       rw1[j] = wrapi(c1 + j, a.Nproj);
     }
   }
-  for (int x = t; x < N; x += T) {
+  // N / T = 8 profile points per thread; the loads of all taps are issued
+  // before any is used (straight-line, no per-point branches)
+  if (!has0) w0[0] = w0[1] = w0[2] = w0[3] = 0.f;
+  if (!has1) w1[0] = w1[1] = w1[2] = w1[3] = 0.f;
+#pragma unroll
+  for (int m = 0; m < N / T; ++m) {
+    const int x = t + m * T;
     float p0 = 0.f, p1 = 0.f;
-    for (int j = 0; j < ntap; ++j) {
-      if (has0) p0 += w0[j] * __ldg(img + (size_t)rw0[j] * N + x);
-      if (has1) p1 += w1[j] * __ldg(img + (size_t)rw1[j] * N + x);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (j < ntap) {
+        p0 += w0[j] * (has0 ? __ldg(img + (size_t)rw0[j] * N + x) : 0.f);
+        p1 += w1[j] * (has1 ? __ldg(img + (size_t)rw1[j] * N + x) : 0.f);
+      }
     }
     prof[x] = p0;
     prof[N + x] = p1;
@@ -1149,17 +1221,18 @@ __global__ void __launch_bounds__(256, 3) k_adj_polar2lp_p2(AdjPolar2LPArgs a) {
   __syncthreads();
   const float* sx0 = a.sx + (size_t)(live ? th0 : 0) * L;
   const float* sx1 = a.sx + (size_t)max(th1, 0) * L;
-  for (int r = t; r < L; r += T) {
-    float v0 = 0.f, v1 = 0.f;
-    if (live) {
-      const float x0 = __ldg(sx0 + r);
-      if (!isnan(x0)) v0 = interp1d([&](int i) { return prof[i]; }, N, x0, a.cubic);
-    }
-    if (th1 >= 0) {
-      const float x1 = __ldg(sx1 + r);
-      if (!isnan(x1)) v1 = interp1d([&](int i) { return prof[N + i]; }, N, x1, a.cubic);
-    }
-    sm[spad(r)] = make_float2(v0, v1);
+  float xs0[16], xs1[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    xs0[i] = live ? __ldg(sx0 + t + i * T) : nanv;
+    xs1[i] = th1 >= 0 ? __ldg(sx1 + t + i * T) : nanv;
+  }
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const bool ok0 = !isnan(xs0[i]), ok1 = !isnan(xs1[i]);
+    const float v0 = interp1d([&](int q) { return prof[q]; }, N, ok0 ? xs0[i] : 0.f, a.cubic);
+    const float v1 = interp1d([&](int q) { return prof[N + q]; }, N, ok1 ? xs1[i] : 0.f, a.cubic);
+    sm[spad(t + i * T)] = make_float2(ok0 ? v0 : 0.f, ok1 ? v1 : 0.f);
   }
   __syncthreads();
   // wrap points (distinct rho within a column) add a direct 2-D sample
@@ -1211,7 +1284,10 @@ __global__ void __launch_bounds__(256, 3) k_adj_lpcols_p2(AdjLPColsArgs a) {
   const int th1 = (live && th0 + 1 <= a.hi2) ? th0 + 1 : -1;
   const float2* sp = a.spec + (size_t)s * a.Nk * a.Nth;
   const bool al = ((th0 & 1) == 0) && th1 >= 0;
-  for (int kk = t; kk <= L / 2; kk += T) {
+#pragma unroll
+  for (int m = 0; m <= L / 2 / T; ++m) {
+    const int kk = t + m * T;
+    if (kk > L / 2) break;
     float2 v0 = make_float2(0.f, 0.f), v1 = make_float2(0.f, 0.f);
     if (al) {
       const float4 q = *reinterpret_cast<const float4*>(sp + (size_t)kk * a.Nth + th0);
@@ -1269,12 +1345,15 @@ cudaError_t configure_p2_kernels(int optin) {
 
 bool p2_fwd_c2lp(const FwdC2LPArgs& a, int S, cudaStream_t st, cudaError_t* err) {
   const int L = a.Nrho;
-  if (!p2_ok(L)) return false;
+  if (!p2_ok(L) || a.ival == nullptr) return false;
+  if (a.col_lo < 0 || a.col_hi >= a.Nth) { *err = cudaErrorInvalidValue; return true; }
+  const int npairs = a.col_hi < a.col_lo ? 0 : (a.col_hi >> 1) - (a.col_lo >> 1) + 1;
+  if (npairs == 0) { *err = cudaSuccess; return true; }
 #define CALL(LL)                                                                              \
   {                                                                                           \
     const size_t sm = (size_t)P2<LL>::NSIG * P2<LL>::SLOTS * sizeof(float2);                 \
     if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; }   \
-    dim3 grid(S, (a.Nth / 2 + P2<LL>::NSIG - 1) / P2<LL>::NSIG);                               \
+    dim3 grid(S, (npairs + P2<LL>::NSIG - 1) / P2<LL>::NSIG);                                  \
     k_fwd_c2lp_p2<LL><<<grid, P2<LL>::BLOCK, sm, st>>>(a);                                    \
   }
   switch (L) { case 256: CALL(256) break; case 512: CALL(512) break; case 1024: CALL(1024) break;

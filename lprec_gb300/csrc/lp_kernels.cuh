@@ -28,6 +28,8 @@ struct FwdC2LPArgs {          // Cartesian -> log-polar gather, e^rho, FFT along
   int N, Nth, Nrho, Nk, cubic;
   FFTPlan plan;               // length Nrho
   const cudaTextureObject_t* tex;  // if set: the prefiltered image per slice as a gather texture (cubic)
+  const int2* ival;           // [Nth] rho interval [x, y] of a column's disk points (y < x: none); if set,
+  int col_lo, col_hi;         //   only column pairs meeting [col_lo, col_hi] are launched (others untouched)
 };
 
 struct ThetaConvArgs {        // FFT along theta, multiply by the kernel, inverse

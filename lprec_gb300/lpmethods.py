@@ -186,3 +186,66 @@ def tvl1(lp, init_recon, tomo0, num_iter, reg_par, gpu=0):
         tmp2 = torch.clamp(tmp.abs() - 1, min=0)
         return tmp - tmp2 * torch.sign(tmp)
     return _tv_family(lp, init_recon, tomo0, num_iter, reg_par, gpu, prox)
+
+
+# ---------------------------------------------------------------------------
+# Methods on the exact transpose (not in the reference, whose adjp is only
+# approximately the transpose of fwdp): least squares with the true normal
+# equations R^T R f = R^T g, and gradient descent through autograd.
+# ---------------------------------------------------------------------------
+def cg_exact(lp, init_recon, tomo0, num_iter, reg_par=0, gpu=0):
+    """CG on R^T R f = R^T g with R^T the exact transpose (lp.fwdp_T); float64 inner products."""
+    torch = _torch()
+    with torch.cuda.device(gpu):
+        recon = _dev(init_recon, gpu)
+        tomo = _dev(tomo0, gpu)
+        g = torch.zeros_like(tomo)
+        b = torch.zeros_like(recon)
+        q = torch.zeros_like(recon)
+        lp.fwdp_T(b, tomo, gpu)
+        lp.fwdp(g, recon, gpu)
+        lp.fwdp_T(q, g, gpu)
+        r = b - q
+        p = r.clone()
+        rsold = _dot(r, r)
+        for i in range(num_iter):
+            lp.fwdp(g, p, gpu)
+            lp.fwdp_T(q, g, gpu)
+            alpha = (rsold / _dot(p, q)).float()
+            recon.add_(alpha * p)
+            r.sub_(alpha * q)
+            rsnew = _dot(r, r)
+            p.mul_((rsnew / rsold).float()).add_(r)
+            rsold = rsnew
+        return _out(recon)
+
+
+def tv_gd(lp, init_recon, tomo0, num_iter, reg_par, gpu=0, step=None, eps=1e-8):
+    """Gradient descent on 1/2||R f - g||^2 + reg_par * TV_eps(f) with gradients from
+    autograd (backward = exact transpose).  `step` defaults to 1/||R^T R|| estimated
+    by a few power iterations."""
+    torch = _torch()
+    from .autograd import radon
+    with torch.cuda.device(gpu):
+        x = _dev(init_recon, gpu)
+        tomo = _dev(tomo0, gpu)
+        if step is None:
+            v = torch.rand_like(x)
+            for _ in range(8):
+                w = torch.zeros_like(tomo)
+                lp.fwdp(w, v, gpu)
+                u = torch.zeros_like(x)
+                lp.fwdp_T(u, w, gpu)
+                nrm = torch.linalg.vector_norm(u.double())
+                v = (u / nrm).float()
+            step = 0.9 / float(nrm)
+        for i in range(num_iter):
+            x.requires_grad_(True)
+            dx = x[:, :, 1:] - x[:, :, :-1]
+            dy = x[:, 1:, :] - x[:, :-1, :]
+            tv = torch.sqrt(dx[:, :-1, :] ** 2 + dy[:, :, :-1] ** 2 + eps).sum()
+            loss = 0.5 * ((radon(x, lp, gpu) - tomo) ** 2).sum() + reg_par * tv
+            (gx,) = torch.autograd.grad(loss, x)
+            with torch.no_grad():
+                x = x - step * gx
+        return _out(x.detach())

@@ -155,6 +155,27 @@ def test_deterministic(torch_cuda):
     assert np.array_equal(_adj(torch_cuda, h, R), _adj(torch_cuda, h, R))
 
 
+@pytest.mark.parametrize("args", [(128, 192, 64, 'cubic', 'ramp'), (96, 144, 45, 'cubic', 'none'),
+                                  (256, 384, 128, 'linear', 'hann'), (64, 96, 32, 'cubic', 'shepp-logan')])
+def test_scratch_poison_invariant(torch_cuda, args):
+    """Intermediate buffers filled with NaN or a large value before a call give the same
+    result: no kernel reads an element that the call itself did not write first."""
+    torch = torch_cuda
+    from lprec_gb300 import _lib
+    N0, Nproj, cor, interp, filt = args
+    packed = _lib.precompute(N0, Nproj, 2, cor, interp, filt, precision='fp64')
+    h = _handle(packed)
+    G = O.create_geometry(N0, Nproj, 2, cor, interp)
+    f, R = _inputs(G, 2, 17)
+    st = torch.cuda.current_stream().cuda_stream
+    Rc, fc = _fwd(torch, h, f), _adj(torch, h, R)
+    for v in (float('nan'), 1e30):
+        h.debug_fill_scratch(v, st)
+        assert np.array_equal(_fwd(torch, h, f), Rc), v
+        h.debug_fill_scratch(v, st)
+        assert np.array_equal(_adj(torch, h, R), fc), v
+
+
 @pytest.mark.parametrize("args", [(512, 768, 'cubic', 'shepp-logan', 256, 2), (1024, 1536, 'linear', 'hann', 512, 1),
                                   (2048, 3000, 'cubic', 'shepp-logan', 1024, 1)])
 def test_large_sizes(torch_cuda, args):

@@ -92,3 +92,62 @@ def test_autograd_finite_differences(torch_cuda):
         fd = (L(f64 + eps * d) - L(f64 - eps * d)) / (2 * eps)
         an = np.sum(grad * d)
         assert abs(fd - an) <= 1e-5 * scale, (i, fd, an, scale)
+
+
+def _cg_exact_oracle(tr, init, tomo, num_iter):
+    """CG on R^T R f = R^T g with the oracle's exact transpose (float64)."""
+    recon = np.array(init, dtype=np.float64)
+    r = tr.fwd_T(tomo) - tr.fwd_T(tr.fwd(recon))
+    p = r.copy()
+    rsold = np.sum(r * r)
+    for _ in range(num_iter):
+        q = tr.fwd_T(tr.fwd(p))
+        alpha = rsold / np.sum(p * q)
+        recon = recon + alpha * p
+        r = r - alpha * q
+        rsnew = np.sum(r * r)
+        p = r + (rsnew / rsold) * p
+        rsold = rsnew
+    return recon
+
+
+def test_cg_exact_matches_oracle(torch_cuda):
+    from lprec_gb300 import lpmethods
+    N0, Nproj = 64, 96
+    lp = _lp(N0, Nproj, 2, 32, 'cubic')
+    tr = O.Transform.from_packed(lp.glpars, lp.fwdparsi, lp.fwdparamsf, lp.adjparsi, lp.adjparamsf)
+    rng = np.random.default_rng(4)
+    ph = np.stack([O.ellipse_phantom(N0, 5, rng) for _ in range(2)])
+    tomo = np.float32(tr.fwd(ph)).astype(np.float64)
+    z = np.zeros((2, N0, N0), np.float32)
+    got = lpmethods.cg_exact(lp, z, np.float32(tomo), 10, 0, 0)
+    ref = _cg_exact_oracle(tr, z, tomo, 10)
+    # R^T R is ill-conditioned: ten CG steps amplify the float32 rounding of the
+    # operator (~1e-7) to ~1e-3 against the float64 iteration
+    assert O.rel_l2(got, ref) < 5e-3, O.rel_l2(got, ref)
+    # the data residual falls below the one of the starting point
+    assert np.linalg.norm(tr.fwd(got) - tomo) < 0.2 * np.linalg.norm(tomo)
+
+
+def test_tv_gd_decreases_objective(torch_cuda):
+    """Gradient descent with autograd gradients (exact transpose) decreases its objective."""
+    torch = torch_cuda
+    from lprec_gb300 import lpmethods
+    N0, Nproj = 64, 96
+    lp = _lp(N0, Nproj, 2, 32, 'cubic')
+    tr = O.Transform.from_packed(lp.glpars, lp.fwdparsi, lp.fwdparamsf, lp.adjparsi, lp.adjparamsf)
+    rng = np.random.default_rng(6)
+    ph = np.stack([O.ellipse_phantom(N0, 5, rng) for _ in range(2)])
+    tomo = tr.fwd(ph)
+
+    def objective(x, lam=1e-3, eps=1e-8):
+        dx = x[:, :, 1:] - x[:, :, :-1]
+        dy = x[:, 1:, :] - x[:, :-1, :]
+        tv = np.sqrt(dx[:, :-1, :] ** 2 + dy[:, :, :-1] ** 2 + eps).sum()
+        return 0.5 * np.sum((tr.fwd(x) - tomo) ** 2) + lam * tv
+    z = np.zeros((2, N0, N0), np.float32)
+    o0 = objective(z.astype(np.float64))
+    x5 = lpmethods.tv_gd(lp, z, np.float32(tomo), 5, 1e-3, 0)
+    x20 = lpmethods.tv_gd(lp, z, np.float32(tomo), 20, 1e-3, 0)
+    o5, o20 = objective(x5.astype(np.float64)), objective(x20.astype(np.float64))
+    assert o20 < o5 < o0, (o0, o5, o20)
