@@ -319,10 +319,85 @@ def run_uneven(torch, dev, reps):
     return out
 
 
+def run_side_configs(torch, dev, reps=5):
+    """The two smaller workloads of the benchmark spec, reported beside the headline:
+    64 slices at N=1024 (one batched call vs 64 one-slice calls) and one slice at
+    N=256 (call latency, dot tests)."""
+    from lprec_gb300.lpTransform import lpTransform
+    out = {}
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn, n):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(n):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / n
+
+    N, Nproj, S = 1024, 1536, 64
+    lp = lpTransform(N, Nproj, S, "shepp-logan", N / 2, "cubic")
+    lp.precompute(1)
+    lp.initcmem(1, dev)
+    sched = lp.autotune(dev)
+    f = phantoms_gpu(torch, N, S, 20, 1, dev)
+    R = torch.empty((S, Nproj, N), device=dev)
+    fo = torch.empty_like(f)
+
+    def batched():
+        lp.fwdp(R, f, dev)
+        lp.adjp(fo, R, dev)
+
+    def plain():
+        for s in range(S):
+            lp.fwdp(R[s:s + 1], f[s:s + 1], dev)
+            lp.adjp(fo[s:s + 1], R[s:s + 1], dev)
+    tb, tp = timed(batched, reps), timed(plain, max(1, reps // 2))
+    algo = 4.0e8  # algorithmic HBM bytes per slice of fwd+adj at N=1024, Nproj=1536, batch 64
+    out["batched_n1024_s64"] = {"slices_per_s": S / tb * 1e3, "plain_slices_per_s": S / tp * 1e3,
+                                "batched_over_plain": tp / tb, "ms_batched": tb, "ms_plain": tp,
+                                "hbm_gbs_algorithmic": algo * S / tb * 1e-6, "schedule": sched}
+    lp.close()
+    del f, R, fo
+
+    N, Nproj = 256, 384
+    lp = lpTransform(N, Nproj, 1, "ramp", N / 2, "cubic")
+    lp.precompute(1)
+    lp.initcmem(1, dev)
+    f = phantoms_gpu(torch, N, 1, 10, 0, dev)
+    R = torch.empty((1, Nproj, N), device=dev)
+    fo = torch.empty_like(f)
+    tf = timed(lambda: lp.fwdp(R, f, dev), 20)
+    ta = timed(lambda: lp.adjp(fo, R, dev), 20)
+    rng = np.random.default_rng(0)
+    fr = torch.as_tensor(rng.random((1, N, N), dtype=np.float32)).to(dev)
+    gr = torch.as_tensor(rng.random((1, Nproj, N), dtype=np.float32)).to(dev)
+    lp0 = lpTransform(N, Nproj, 1, "none", N / 2, "cubic")
+    lp0.precompute(1)
+    lp0.initcmem(1, dev)
+    Rf = torch.empty_like(R)
+    lp0.fwdp(Rf, fr, dev)
+    Ag = torch.empty_like(fr)
+    lp0.adjp(Ag, gr, dev)
+    Tg = torch.empty_like(fr)
+    lp0.fwdp_T(Tg, gr, dev)
+    lhs = float((Rf.double() * gr.double()).sum())
+    out["single_n256"] = {"fwd_ms": tf, "fbp_ms": ta,
+                          "dot_test_adj": abs(lhs - float((fr.double() * Ag.double()).sum())) / abs(lhs),
+                          "dot_test_exact_transpose": abs(lhs - float((fr.double() * Tg.double()).sum())) / abs(lhs)}
+    lp.close()
+    lp0.close()
+    return out
+
+
 def run_ours(args):
     import torch
     from lprec_gb300 import _lib
     from lprec_gb300.lpTransform import lpTransform
+    from lprec_gb300.replicas import max_over_ranks
     ws, rank, local = dist_env()
     dist = ws > 1
     if dist:
@@ -356,13 +431,15 @@ def run_ours(args):
         lp.fwdp(Rout, f, dev)
         lp.adjp(fout, Rn, dev)
 
+    # batch schedule (slice chunks, one or two streams) picked by the autotuner
+    t0 = time.perf_counter()
+    sched = lp.autotune(dev) if not args.no_tune else h.schedule()
+    t_tune = time.perf_counter() - t0
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
     if dist:
         tdist.barrier()
-    h.set_profiling(True)
-    h.profile()  # clear
     n0 = _lib.launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(dev) as clk:
@@ -373,13 +450,21 @@ def run_ours(args):
         e1.record(stream)
         torch.cuda.synchronize()
     launches = _lib.launch_count() - n0
+    ms = e0.elapsed_time(e1)
+    # per-kernel times: the same steps with the whole batch in one chunk on one
+    # stream (launches do not overlap), CUDA events around every launch
+    h.set_schedule()
+    step()
+    torch.cuda.synchronize()
+    h.set_profiling(True)
+    h.profile()  # clear
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
     prof = h.profile()
     h.set_profiling(False)
-    ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        ms = float(t.item())
+    h.set_schedule(**sched)
+    ms = max_over_ranks(ms, device=dev)
     ms_step = ms / args.steps
     value = ws * S / (ms_step / 1000.0)
 
@@ -417,10 +502,7 @@ def run_ours(args):
     q1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = q0.elapsed_time(q1) / ke
-    if dist:
-        t = torch.tensor([e2e_ms], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e2e_ms, device=dev)
     e2e = ws * S / (e2e_ms / 1000.0)
     h2d = (f.numel() + R.numel()) * 4
     d2h = h2d
@@ -446,7 +528,7 @@ def run_ours(args):
             "config": {"workload": "fwd+adj batch: %d slices N=%d Nproj=%d cubic %s" % (S, N, Nproj, W["filter"]),
                        "slices": S, "N": N, "Nproj": Nproj, "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "inputs larger than L2 (%.1f GB per step)" % (S * (N * N + Nproj * N) * 4 / 1e9),
-                       "precompute_s": round(t_pre, 2)},
+                       "precompute_s": round(t_pre, 2), "schedule": sched, "autotune_s": round(t_tune, 2)},
             "plain_value": plain, "batched_over_plain": value / plain / ws,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "matches_device_result": e2e_ok},
@@ -460,6 +542,8 @@ def run_ours(args):
             "clocks": clk.summary()}
     if rank == 0 and not args.no_uneven and not args.small:
         line["uneven_batch"] = run_uneven(torch, dev, max(2, args.steps // 2))
+    if rank == 0 and not args.no_side and not args.small:
+        line.update(run_side_configs(torch, dev))
     if rank == 0 and not args.no_cpu:
         cores = len(os.sched_getaffinity(0))
         nproc = max(1, min(cores, 6))
@@ -617,6 +701,8 @@ def main():
     ap.add_argument("--slices", type=int, default=0, help="batch size (default 128); for profiling runs")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-geometry graph batch")
     ap.add_argument("--report", action="store_true", help="precision / differentiation report instead of timing")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default schedule (no autotuner)")
+    ap.add_argument("--no-side", action="store_true", help="skip the N=1024 batch and N=256 single-slice lines")
     args = ap.parse_args()
     if args.report:
         run_report(args)

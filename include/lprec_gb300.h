@@ -146,6 +146,29 @@ int lp_set_profiling(lp_handle* h, int enable);
 int lp_profile_collect(lp_handle* h, double* ms, int64_t* launches);
 
 /*
+ * Batch schedule (no reference counterpart; the reference runs every kernel
+ * once over the whole batch on the legacy stream).  lp_fwd / lp_adj split a
+ * call's S0 slices into chunks of `chunk` slices (0: one chunk) processed in
+ * turn, alternating between the caller's stream and a second stream owned by
+ * the handle when `streams` is 2 (forked from and joined back into the
+ * caller's stream with events).  Results do not depend on the schedule.
+ * Defaults: chunk 0, streams 1.  out[4] = {fwd_chunk, fwd_streams,
+ * adj_chunk, adj_streams}.
+ */
+int lp_set_schedule(lp_handle* h, int fwd_chunk, int fwd_streams, int adj_chunk, int adj_streams);
+int lp_get_schedule(const lp_handle* h, int32_t out[4]);
+
+/*
+ * Autotuner (no reference counterpart): time every candidate schedule (chunks
+ * of 64, 32, 16, 8 slices or none; one or two streams) of lp_fwd and lp_adj on
+ * S0 slices, using the caller's device buffers R[S0][Nproj][N0] and
+ * f[S0][N0][N0] as scratch input/output (their contents are overwritten), and
+ * keep the fastest for this handle.  Synchronises `stream`; do not call it
+ * during graph capture.  out_ms (may be NULL): best fwd and adj ms per call.
+ */
+int lp_autotune(lp_handle* h, float* R, float* f, int S0, void* stream, float out_ms[2]);
+
+/*
  * Test hook (no reference counterpart): fill the handle's intermediate device
  * buffers (log-polar spectrum, prefiltered image and sinogram, log-polar
  * columns) with `value`, enqueued on `stream`.  Results of later calls must

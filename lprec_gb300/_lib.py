@@ -23,7 +23,8 @@ PRECISION = {"reference": 0, "fp64": 1}
 EXPORTS = ("lp_last_error", "lp_version", "lp_precompute_sizes", "lp_precompute", "lp_create", "lp_init_fwd",
            "lp_init_adj", "lp_destroy", "lp_fwd", "lp_adj", "lp_get_geometry", "lp_device_bytes",
            "lp_launch_count", "lp_kernel_count", "lp_kernel_name", "lp_set_profiling", "lp_profile_collect",
-           "lp_fwd_noalloc", "lp_noalloc_scratch_bytes", "lp_fwd_transpose", "lp_debug_fill_scratch")
+           "lp_fwd_noalloc", "lp_noalloc_scratch_bytes", "lp_fwd_transpose", "lp_debug_fill_scratch",
+           "lp_set_schedule", "lp_get_schedule", "lp_autotune")
 
 
 class LprecError(RuntimeError):
@@ -70,6 +71,9 @@ def lib():
         "lp_set_profiling": (c_int, [c_void_p, c_int]),
         "lp_profile_collect": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_double), P_i64]),
         "lp_debug_fill_scratch": (c_int, [c_void_p, ctypes.c_float, c_void_p]),
+        "lp_set_schedule": (c_int, [c_void_p, c_int, c_int, c_int, c_int]),
+        "lp_get_schedule": (c_int, [c_void_p, P_i32]),
+        "lp_autotune": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, P_f32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -164,6 +168,20 @@ class Handle:
         b = np.zeros(1, np.int64)
         check(lib().lp_device_bytes(self._h, _ptr(b, ctypes.c_int64)))
         return int(b[0])
+
+    def set_schedule(self, fwd_chunk=0, fwd_streams=1, adj_chunk=0, adj_streams=1):
+        check(lib().lp_set_schedule(self._h, int(fwd_chunk), int(fwd_streams), int(adj_chunk), int(adj_streams)))
+
+    def schedule(self):
+        out = np.zeros(4, np.int32)
+        check(lib().lp_get_schedule(self._h, _ptr(out, ctypes.c_int32)))
+        return dict(fwd_chunk=int(out[0]), fwd_streams=int(out[1]), adj_chunk=int(out[2]), adj_streams=int(out[3]))
+
+    def autotune(self, R, f, S0, stream):
+        """Pick the fastest batch schedule on S0 slices of the device buffers R, f (overwritten)."""
+        ms = np.zeros(2, np.float32)
+        check(lib().lp_autotune(self._h, R, f, int(S0), stream, _ptr(ms, ctypes.c_float)))
+        return float(ms[0]), float(ms[1])
 
     def debug_fill_scratch(self, value, stream):
         """Fill the intermediate buffers with `value` (test hook: results must not change)."""

@@ -185,6 +185,12 @@ struct lp_handle {
   FwdDev* fwd = nullptr;
   AdjDev* adj = nullptr;
   FFTPlan plan_rho, plan_th, plan_filt;
+  // batch schedule of lp_fwd / lp_adj: slices per chunk (0: the whole call in
+  // one chunk) and streams the chunks alternate on (1 or 2); set by
+  // lp_set_schedule or lp_autotune
+  int fwd_chunk = 0, fwd_streams = 1, adj_chunk = 0, adj_streams = 1;
+  cudaStream_t side = nullptr;        // second stream of a 2-stream schedule
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 static void free_fwd(FwdDev* f) {
@@ -476,6 +482,9 @@ int lp_create(const float* glpars, int64_t n, int device, lp_handle** out) {
   if (e == cudaSuccess) e = dev_upload(h->tw_rho, twiddles(h->Nrho));
   if (e == cudaSuccess) e = dev_upload(h->tw_th, twiddles(h->Nth));
   if (e == cudaSuccess) e = dev_alloc(h->spec, (size_t)h->Nslices * h->Nk * h->Nth);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
   h->plan_rho = make_fft_plan(h->Nrho, h->tw_rho.p);
   h->plan_th = make_fft_plan(h->Nth, h->tw_th.p);
   h->plan_filt = h->plan_rho;
@@ -484,6 +493,9 @@ int lp_create(const float* glpars, int64_t n, int device, lp_handle** out) {
     h->tw_rho.free_();
     h->tw_th.free_();
     h->spec.free_();
+    if (h->side) cudaStreamDestroy(h->side);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
     delete h;
     return set_err(e == cudaErrorMemoryAllocation ? LP_ERR_OOM : LP_ERR_CUDA, "lp_create: %s",
                    cudaGetErrorString(e));
@@ -815,6 +827,9 @@ int lp_destroy(lp_handle* h) {
     cudaEventDestroy(r.b);
   }
   for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
+  if (h->side) cudaStreamDestroy(h->side);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
   delete h;
   return LP_OK;
 }
@@ -871,6 +886,109 @@ int lp_device_bytes(const lp_handle* h, int64_t* bytes) {
   return LP_OK;
 }
 
+}  // extern "C"
+
+// Run `body(s0, n, stream)` over the slices [0, S0) in chunks of `chunk`
+// (0: one chunk), alternating between the caller's stream and the handle's
+// second stream when `streams` is 2.  Chunks use disjoint slices of every
+// scratch buffer, so chunks on the two streams never share memory; the
+// second stream is forked from and joined back into the caller's stream with
+// events (graph capture turns them into parallel branches).
+template <typename Body>
+static int run_chunks(lp_handle* h, cudaStream_t st, int S0, int chunk, int streams, Body body) {
+  const int c = chunk > 0 ? std::min(chunk, S0) : S0;
+  const int nch = (S0 + c - 1) / c;
+  const bool two = streams == 2 && nch >= 2;
+  if (two) {
+    CUDA_TRY(cudaEventRecord(h->ev_fork, st));
+    CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
+  }
+  for (int i = 0; i < nch; ++i) {
+    const int rc = body(i * c, std::min(c, S0 - i * c), (two && (i & 1)) ? h->side : st);
+    if (rc != LP_OK) return rc;
+  }
+  if (two) {
+    CUDA_TRY(cudaEventRecord(h->ev_join, h->side));
+    CUDA_TRY(cudaStreamWaitEvent(st, h->ev_join, 0));
+  }
+  return LP_OK;
+}
+
+// forward transform of slices [s0, s0 + n) of the call (scratch slots s0..)
+static int fwd_slices(lp_handle* h, float* R, const float* f, int s0, int n, cudaStream_t st) {
+  FwdDev* F = h->fwd;
+  const bool tex = !F->tex_h.empty();
+  f += (size_t)s0 * h->N0 * h->N0;
+  R += (size_t)s0 * h->Nproj0 * h->N0;
+  float* fbuf = F->fbuf.p + (size_t)s0 * h->N * h->N;
+  float2* spec = h->spec.p + (size_t)s0 * h->Nk * h->Nth;
+  const cudaTextureObject_t* tx = tex ? F->tex.p + s0 : nullptr;
+  const cudaSurfaceObject_t* sf = tex ? F->surf.p + s0 : nullptr;
+  FwdIngestArgs ia{f, fbuf, h->N, h->N0, h->N / 2 - h->N0 / 2, h->cubic};
+  CUDA_TRY(launch(h, K_FWD_INGEST, st, [&] { return launch_fwd_ingest(ia, n, st); }));
+  if (h->cubic) {
+    ColPrefilterArgs ca{fbuf, h->N, h->N, sf};
+    CUDA_TRY(launch(h, K_COL_PREFILTER, st, [&] { return launch_col_prefilter(ca, n, st); }));
+  }
+  for (int k = 0; k < 3; ++k) {
+    FwdC2LPArgs a1{fbuf, spec, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, h->cubic,
+                   h->plan_rho, tx, F->ival.p, F->dlo, F->dhi};
+    CUDA_TRY(launch(h, K_FWD_C2LP, st, [&] { return launch_fwd_c2lp(a1, n, st); }));
+    ThetaConvArgs a2{spec, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), F->dlo, F->dhi,
+                     F->lo & ~1, std::min(F->hi | 1, h->Nth - 1), 0, h->plan_th};
+    CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, n, st); }));
+    FwdLP2PolarArgs a3{spec, R, F->thc.p, F->rhoc.p, F->rows[k].p, F->nrows[k], h->N, h->N0, h->Nth,
+                       h->Nrho, h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho};
+    CUDA_TRY(launch(h, K_FWD_LP2POLAR, st, [&] { return launch_fwd_lp2polar(a3, n, st); }));
+  }
+  return LP_OK;
+}
+
+// adjoint of slices [s0, s0 + n) of the call (scratch slots s0..)
+static int adj_slices(lp_handle* h, float* f, const float* R, int s0, int n, cudaStream_t st) {
+  AdjDev* A = h->adj;
+  R += (size_t)s0 * h->Nproj0 * h->N0;
+  f += (size_t)s0 * h->N0 * h->N0;
+  float* rbuf = A->rbuf.p + (size_t)s0 * h->Nproj * h->N;
+  float2* spec = h->spec.p + (size_t)s0 * h->Nk * h->Nth;
+  const size_t gstride = (size_t)A->W2 * h->Nrho;
+  AdjIngestArgs ia{R, rbuf, A->filter ? A->H.p : nullptr, h->N, h->N0, h->Nproj, h->Nproj0, h->os,
+                   h->N / 2 - h->cor, h->cubic, h->plan_filt};
+  CUDA_TRY(launch(h, K_ADJ_INGEST, st, [&] { return launch_adj_ingest(ia, n, st); }));
+  if (h->cubic) {
+    ColPrefilterArgs ca{rbuf, h->Nproj, h->N};
+    CUDA_TRY(launch(h, K_COL_PREFILTER, st, [&] { return launch_col_prefilter(ca, n, st); }));
+  }
+  float* G[3];
+  for (int k = 0; k < 3; ++k) G[k] = A->G[k].p ? A->G[k].p + s0 * gstride : nullptr;
+  for (int k = 0; k < 3; ++k) {
+    const bool tex = !A->tex_h[k].empty();
+    if (A->chi[k] < A->clo[k]) {
+      if (tex) return set_err(LP_ERR_UNSUPPORTED, "lp_adj: span %d has no log-polar points", k);
+      CUDA_TRY(cudaMemsetAsync(G[k], 0, n * gstride * sizeof(float), st));
+      continue;
+    }
+    AdjPolar2LPArgs a1{rbuf, spec, A->ta[k].p, A->sx[k].p, A->woff[k].p, A->wpt[k].p, h->N, h->Nth,
+                       h->Nrho, h->Nk, h->Nproj, h->cubic, A->clo[k], A->chi[k], h->plan_rho};
+    CUDA_TRY(launch(h, K_ADJ_POLAR2LP, st, [&] { return launch_adj_polar2lp(a1, n, st); }));
+    ThetaConvArgs a2{spec, A->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), A->clo[k],
+                     A->chi[k], A->lo2, A->hi2, 0, h->plan_th};
+    CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, n, st); }));
+    AdjLPColsArgs a3{spec, G[k], h->Nth, h->Nrho, h->Nk, A->lo2, A->hi2, A->W2, h->plan_rho,
+                     tex ? A->surf[k].p + s0 : nullptr};
+    CUDA_TRY(launch(h, K_ADJ_LPCOLS, st, [&] { return launch_adj_lpcols(a3, n, st); }));
+  }
+  const bool tex = !A->tex_h[0].empty();
+  AdjLP2CartArgs a4{G[0], G[1], G[2], A->c2lp[0].p, A->c2lp[1].p, A->c2lp[2].p, f,
+                    h->N0, h->Nth, h->Nrho, A->lo2, A->W2, h->cubic, h->N0 * h->N0,
+                    tex ? A->tex[0].p + s0 : nullptr, tex ? A->tex[1].p + s0 : nullptr,
+                    tex ? A->tex[2].p + s0 : nullptr};
+  CUDA_TRY(launch(h, K_ADJ_LP2CART, st, [&] { return launch_adj_lp2cart(a4, n, st); }));
+  return LP_OK;
+}
+
+extern "C" {
+
 int lp_fwd(lp_handle* h, float* R, const float* f, int S0, void* stream) {
   if (!h) return set_err(LP_ERR_ARG, "lp_fwd: null handle");
   if (!h->fwd) return set_err(LP_ERR_STATE, "lp_fwd: forward tables not initialised (lp_init_fwd)");
@@ -878,27 +996,8 @@ int lp_fwd(lp_handle* h, float* R, const float* f, int S0, void* stream) {
   if (S0 == 0) return LP_OK;
   if (!R || !f) return set_err(LP_ERR_ARG, "lp_fwd: null data pointer");
   DeviceGuard g(h->device);
-  cudaStream_t st = (cudaStream_t)stream;
-  FwdDev* F = h->fwd;
-  const bool tex = !F->tex_h.empty();
-  FwdIngestArgs ia{f, F->fbuf.p, h->N, h->N0, h->N / 2 - h->N0 / 2, h->cubic};
-  CUDA_TRY(launch(h, K_FWD_INGEST, st, [&] { return launch_fwd_ingest(ia, S0, st); }));
-  if (h->cubic) {
-    ColPrefilterArgs ca{F->fbuf.p, h->N, h->N, tex ? F->surf.p : nullptr};
-    CUDA_TRY(launch(h, K_COL_PREFILTER, st, [&] { return launch_col_prefilter(ca, S0, st); }));
-  }
-  for (int k = 0; k < 3; ++k) {
-    FwdC2LPArgs a1{F->fbuf.p, h->spec.p, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, h->cubic,
-                   h->plan_rho, tex ? F->tex.p : nullptr, F->ival.p, F->dlo, F->dhi};
-    CUDA_TRY(launch(h, K_FWD_C2LP, st, [&] { return launch_fwd_c2lp(a1, S0, st); }));
-    ThetaConvArgs a2{h->spec.p, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), F->dlo, F->dhi,
-                     F->lo & ~1, std::min(F->hi | 1, h->Nth - 1), 0, h->plan_th};
-    CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
-    FwdLP2PolarArgs a3{h->spec.p, R, F->thc.p, F->rhoc.p, F->rows[k].p, F->nrows[k], h->N, h->N0, h->Nth,
-                       h->Nrho, h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho};
-    CUDA_TRY(launch(h, K_FWD_LP2POLAR, st, [&] { return launch_fwd_lp2polar(a3, S0, st); }));
-  }
-  return LP_OK;
+  return run_chunks(h, (cudaStream_t)stream, S0, h->fwd_chunk, h->fwd_streams,
+                    [&](int s0, int n, cudaStream_t st) { return fwd_slices(h, R, f, s0, n, st); });
 }
 
 int lp_fwd_transpose(lp_handle* h, float* f, const float* R, int S0, void* stream) {
@@ -944,38 +1043,93 @@ int lp_adj(lp_handle* h, float* f, const float* R, int S0, void* stream) {
   if (S0 == 0) return LP_OK;
   if (!R || !f) return set_err(LP_ERR_ARG, "lp_adj: null data pointer");
   DeviceGuard g(h->device);
-  cudaStream_t st = (cudaStream_t)stream;
-  AdjDev* A = h->adj;
-  AdjIngestArgs ia{R, A->rbuf.p, A->filter ? A->H.p : nullptr, h->N, h->N0, h->Nproj, h->Nproj0, h->os,
-                   h->N / 2 - h->cor, h->cubic, h->plan_filt};
-  CUDA_TRY(launch(h, K_ADJ_INGEST, st, [&] { return launch_adj_ingest(ia, S0, st); }));
-  if (h->cubic) {
-    ColPrefilterArgs ca{A->rbuf.p, h->Nproj, h->N};
-    CUDA_TRY(launch(h, K_COL_PREFILTER, st, [&] { return launch_col_prefilter(ca, S0, st); }));
-  }
-  for (int k = 0; k < 3; ++k) {
-    if (A->chi[k] < A->clo[k]) {
-      if (!A->tex_h[k].empty())
-        return set_err(LP_ERR_UNSUPPORTED, "lp_adj: span %d has no log-polar points", k);
-      CUDA_TRY(cudaMemsetAsync(A->G[k].p, 0, A->G[k].n * sizeof(float), st));
-      continue;
+  return run_chunks(h, (cudaStream_t)stream, S0, h->adj_chunk, h->adj_streams,
+                    [&](int s0, int n, cudaStream_t st) { return adj_slices(h, f, R, s0, n, st); });
+}
+
+int lp_set_schedule(lp_handle* h, int fwd_chunk, int fwd_streams, int adj_chunk, int adj_streams) {
+  if (!h) return set_err(LP_ERR_ARG, "lp_set_schedule: null handle");
+  if (fwd_chunk < 0 || adj_chunk < 0 || fwd_streams < 1 || fwd_streams > 2 || adj_streams < 1 || adj_streams > 2)
+    return set_err(LP_ERR_ARG, "lp_set_schedule: chunk >= 0 and streams in {1, 2} required");
+  h->fwd_chunk = fwd_chunk;
+  h->fwd_streams = fwd_streams;
+  h->adj_chunk = adj_chunk;
+  h->adj_streams = adj_streams;
+  return LP_OK;
+}
+
+int lp_get_schedule(const lp_handle* h, int32_t out[4]) {
+  if (!h || !out) return set_err(LP_ERR_ARG, "lp_get_schedule: null pointer");
+  out[0] = h->fwd_chunk;
+  out[1] = h->fwd_streams;
+  out[2] = h->adj_chunk;
+  out[3] = h->adj_streams;
+  return LP_OK;
+}
+
+// Time every candidate schedule of one direction on the caller's buffers and
+// keep the fastest (ties go to the earlier, simpler candidate).
+static int tune_one(lp_handle* h, bool fwd, float* R, float* f, int S0, cudaStream_t st, int reps,
+                    int* best_chunk, int* best_streams, float* best_ms) {
+  const int chunks[] = {0, 64, 32, 16, 8};
+  cudaEvent_t a = nullptr, b = nullptr;
+  CUDA_TRY(cudaEventCreate(&a));
+  CUDA_TRY(cudaEventCreate(&b));
+  const bool prof = h->profiling;
+  h->profiling = false;
+  float best = 1e30f;
+  int rc = LP_OK;
+  for (int ci = 0; ci < 5 && rc == LP_OK; ++ci) {
+    const int c = chunks[ci];
+    if (c != 0 && c >= S0) continue;
+    for (int ns = 1; ns <= 2 && rc == LP_OK; ++ns) {
+      if (ns == 2 && (c == 0 || (S0 + c - 1) / c < 2)) continue;
+      auto one = [&] {
+        return run_chunks(h, st, S0, c, ns, [&](int s0, int n, cudaStream_t s2) {
+          return fwd ? fwd_slices(h, R, f, s0, n, s2) : adj_slices(h, f, R, s0, n, s2);
+        });
+      };
+      rc = one();  // warm-up
+      if (rc != LP_OK) break;
+      cudaEventRecord(a, st);
+      for (int r = 0; r < reps && rc == LP_OK; ++r) rc = one();
+      cudaEventRecord(b, st);
+      if (cudaEventSynchronize(b) != cudaSuccess) rc = set_err(LP_ERR_CUDA, "lp_autotune: timing failed");
+      float ms = 0.f;
+      if (rc == LP_OK) cudaEventElapsedTime(&ms, a, b);
+      if (rc == LP_OK && ms / reps < 0.98f * best) {
+        best = ms / reps;
+        *best_chunk = c;
+        *best_streams = ns;
+      }
     }
-    AdjPolar2LPArgs a1{A->rbuf.p, h->spec.p, A->ta[k].p, A->sx[k].p, A->woff[k].p, A->wpt[k].p, h->N, h->Nth,
-                       h->Nrho, h->Nk, h->Nproj, h->cubic, A->clo[k], A->chi[k], h->plan_rho};
-    CUDA_TRY(launch(h, K_ADJ_POLAR2LP, st, [&] { return launch_adj_polar2lp(a1, S0, st); }));
-    ThetaConvArgs a2{h->spec.p, A->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), A->clo[k],
-                     A->chi[k], A->lo2, A->hi2, 0, h->plan_th};
-    CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
-    const bool tex = !A->tex_h[k].empty();
-    AdjLPColsArgs a3{h->spec.p, A->G[k].p, h->Nth, h->Nrho, h->Nk, A->lo2, A->hi2, A->W2, h->plan_rho,
-                     tex ? A->surf[k].p : nullptr};
-    CUDA_TRY(launch(h, K_ADJ_LPCOLS, st, [&] { return launch_adj_lpcols(a3, S0, st); }));
   }
-  const bool tex = !A->tex_h[0].empty();
-  AdjLP2CartArgs a4{A->G[0].p, A->G[1].p, A->G[2].p, A->c2lp[0].p, A->c2lp[1].p, A->c2lp[2].p, f,
-                    h->N0, h->Nth, h->Nrho, A->lo2, A->W2, h->cubic, h->N0 * h->N0,
-                    tex ? A->tex[0].p : nullptr, tex ? A->tex[1].p : nullptr, tex ? A->tex[2].p : nullptr};
-  CUDA_TRY(launch(h, K_ADJ_LP2CART, st, [&] { return launch_adj_lp2cart(a4, S0, st); }));
+  h->profiling = prof;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *best_ms = best;
+  return rc;
+}
+
+int lp_autotune(lp_handle* h, float* R, float* f, int S0, void* stream, float out_ms[2]) {
+  if (!h) return set_err(LP_ERR_ARG, "lp_autotune: null handle");
+  if (S0 < 1 || S0 > h->Nslices) return set_err(LP_ERR_ARG, "lp_autotune: S0=%d outside [1, %d]", S0, h->Nslices);
+  if (!R || !f) return set_err(LP_ERR_ARG, "lp_autotune: null data pointer");
+  DeviceGuard g(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  float ms[2] = {0.f, 0.f};
+  if (h->fwd) {
+    int rc = tune_one(h, true, R, f, S0, st, 2, &h->fwd_chunk, &h->fwd_streams, &ms[0]);
+    if (rc != LP_OK) return rc;
+  }
+  if (h->adj) {
+    int rc = tune_one(h, false, R, f, S0, st, 2, &h->adj_chunk, &h->adj_streams, &ms[1]);
+    if (rc != LP_OK) return rc;
+  }
+  if (out_ms) {
+    out_ms[0] = ms[0];
+    out_ms[1] = ms[1];
+  }
   return LP_OK;
 }
 

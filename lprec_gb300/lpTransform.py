@@ -147,6 +147,25 @@ class lpTransform:
                              % (h.Nproj, h.N0, h.N0, h.N0, Rs, fs))
         h.fwd_transpose(fp, Rp, S0, _stream(gpu))
 
+    # ---- batch schedule (not in the reference) ------------------------------
+    def autotune(self, gpu, S0=None):
+        """Time the candidate batch schedules (slice chunks, one or two streams) of
+        fwdp and adjp on S0 slices (default Nslices) of scratch tensors and keep the
+        fastest for this handle; returns the chosen schedule."""
+        import torch
+        h = self._handle(gpu)
+        S0 = int(S0 or self.Nslices)
+        dev = torch.device("cuda", gpu)
+        with torch.cuda.device(gpu):
+            f = torch.rand((S0, h.N0, h.N0), device=dev)
+            R = torch.rand((S0, h.Nproj, h.N0), device=dev)
+            h.autotune(R.data_ptr(), f.data_ptr(), S0, _stream(gpu))
+        del f, R
+        return h.schedule()
+
+    def set_schedule(self, gpu, fwd_chunk=0, fwd_streams=1, adj_chunk=0, adj_streams=1):
+        self._handle(gpu).set_schedule(fwd_chunk, fwd_streams, adj_chunk, adj_streams)
+
     # ---- host arrays, pipelined ---------------------------------------------
     def _host_op(self, op, x, out, gpu, chunk):
         """Run fwdp/adjp over host arrays in slice chunks, overlapping the

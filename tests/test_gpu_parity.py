@@ -155,6 +155,35 @@ def test_deterministic(torch_cuda):
     assert np.array_equal(_adj(torch_cuda, h, R), _adj(torch_cuda, h, R))
 
 
+@pytest.mark.parametrize("interp", ['cubic', 'linear'])
+def test_schedules_bit_identical(torch_cuda, interp):
+    """Chunked and two-stream batch schedules (and the autotuner's pick) give the
+    same bits as one whole-batch launch sequence."""
+    torch = torch_cuda
+    from lprec_gb300 import _lib
+    S = 7
+    packed = _lib.precompute(128, 192, S, 64, interp, 'shepp-logan', precision='fp64')
+    h = _handle(packed)
+    G = O.create_geometry(128, 192, S, 64, interp)
+    f, R = _inputs(G, S, 23)
+    Rc, fc = _fwd(torch, h, f), _adj(torch, h, R)
+    for sched in ((3, 2, 2, 2), (2, 1, 3, 1), (1, 2, 1, 2), (4, 2, 0, 1)):
+        h.set_schedule(*sched)
+        assert h.schedule() == dict(zip(('fwd_chunk', 'fwd_streams', 'adj_chunk', 'adj_streams'), sched))
+        assert np.array_equal(_fwd(torch, h, f), Rc), sched
+        assert np.array_equal(_adj(torch, h, R), fc), sched
+    Rt = torch.zeros((S, 192, 128), device='cuda')
+    ft = torch.zeros((S, 128, 128), device='cuda')
+    ms = h.autotune(Rt.data_ptr(), ft.data_ptr(), S, torch.cuda.current_stream().cuda_stream)
+    assert ms[0] > 0 and ms[1] > 0
+    sc = h.schedule()
+    assert sc['fwd_streams'] in (1, 2) and sc['adj_streams'] in (1, 2)
+    assert np.array_equal(_fwd(torch, h, f), Rc), sc
+    assert np.array_equal(_adj(torch, h, R), fc), sc
+    with pytest.raises(_lib.LprecError):
+        h.set_schedule(1, 3, 0, 1)
+
+
 @pytest.mark.parametrize("args", [(128, 192, 64, 'cubic', 'ramp'), (96, 144, 45, 'cubic', 'none'),
                                   (256, 384, 128, 'linear', 'hann'), (64, 96, 32, 'cubic', 'shepp-logan')])
 def test_scratch_poison_invariant(torch_cuda, args):

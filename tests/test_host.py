@@ -1,0 +1,142 @@
+"""Host side of the library, no GPU: the C ABI exports, the C++ precompute
+against the oracle and the reference's own tables, argument checking."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import lprec_oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+NAMES = ['glpars', 'fwdparsi', 'fwdparamsf', 'adjparsi', 'adjparamsf']
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from lprec_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        from lprec_gb300 import build
+        build.build()
+    return _lib
+
+
+def _declared():
+    names = []
+    for hdr in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(hdr).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+char\s*\*|int|long long|int64_t|void)\s*\*?\s*(lp_\w+)\s*\(",
+                            text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = _declared()
+    assert len(names) >= 20, names
+    so = ctypes.CDLL(lib.LIB_PATH)
+    missing = [n for n in names if not hasattr(so, n)]
+    assert not missing, missing
+    # the Python binding declares a signature for each of them
+    assert set(names) <= set(lib.EXPORTS), sorted(set(names) - set(lib.EXPORTS))
+
+
+def test_version_and_kernel_names(lib):
+    L = lib.lib()
+    assert L.lp_version() >= 100
+    n = L.lp_kernel_count()
+    names = [L.lp_kernel_name(i).decode() for i in range(n)]
+    for k in ("fwd_c2lp", "theta_conv", "fwd_lp2polar", "adj_polar2lp", "adj_lp2cart"):
+        assert k in names
+    assert L.lp_kernel_name(n) == b""
+
+
+@pytest.mark.parametrize("args", [(64, 96, 1, 32, 'cubic', 'ramp'), (48, 72, 2, 21, 'cubic', 'shepp-logan'),
+                                  (32, 24, 1, 16, 'linear', 'hann'), (64, 96, 3, 32, 'cubic', 'none'),
+                                  (80, 60, 1, 37, 'linear', 'parzen')])
+def test_precompute_fp64_equals_oracle(lib, args):
+    """C++ float64 precompute against the oracle's float64 tables rounded once: index
+    arrays, geometry, e^rho and every interpolation coordinate bit for bit; the FFT-made
+    kernels fZ to 1e-6 of their maximum (FFT round-off moves the last bit of small
+    entries); the FBP filter to 1e-5 (its quadrature weights invert an ill-conditioned
+    12x12 moment matrix, initsadj.py:128-144, by LAPACK in one and Gauss-Jordan in the
+    other)."""
+    N0, Nproj, S, cor, interp, filt = args
+    mine = lib.precompute(N0, Nproj, S, cor, interp, filt, precision='fp64')
+    tr = O.Transform(N0, Nproj, S, filt, cor, interp, mode='fp64', rounded=True)
+    ref = tr.packed()
+    for name, a, b in zip(NAMES, mine, ref):
+        assert a.shape == b.shape, name
+        if name.endswith('i') or name == 'glpars':
+            assert np.array_equal(a, b), name
+    _, Tf_a, Ta_a, _ = O.unpack_params(*mine)
+    _, Tf_b, Ta_b, _ = O.unpack_params(*ref)
+    for Ta, Tb in ((Tf_a, Tf_b), (Ta_a, Ta_b)):
+        for key in Tb:
+            x, y = Ta[key], Tb[key]
+            if key == 'fZ':
+                assert np.max(np.abs(x - y)) <= 1e-6 * np.max(np.abs(y)), key
+            elif key == 'filter':
+                assert (x is None) == (y is None)
+                if y is not None:
+                    assert np.linalg.norm(x - y) <= 1e-5 * np.linalg.norm(y), key
+            else:
+                for u, v in zip(np.atleast_1d(x) if not isinstance(x, list) else x,
+                                np.atleast_1d(y) if not isinstance(y, list) else y):
+                    assert np.array_equal(u, v), key
+
+
+def test_precompute_reference_mode_against_reference_tables(lib, golden_dir):
+    """C++ reference-precision precompute against the reference's own packed arrays:
+    identical integer arrays (index sets, sizes); float arrays within a few ulp except
+    fZ, whose float32 cos (NumPy's, not correctly rounded) leaves ~1e-5 relative."""
+    files = sorted(glob.glob(os.path.join(golden_dir, 'packed_*.npz')))
+    assert files
+    for fn in files:
+        z = np.load(fn)
+        N0, Nproj, S, cor = z['args']
+        mine = lib.precompute(int(N0), int(Nproj), int(S), float(cor), str(z['interp']), str(z['filter']),
+                              precision='reference')
+        for name, a in zip(NAMES, mine):
+            ref = z[name]
+            assert a.shape == ref.shape, (fn, name)
+            if name.endswith('i'):
+                assert np.array_equal(a, ref), (fn, name)
+            else:
+                err = np.linalg.norm(a.astype(np.float64) - ref) / np.linalg.norm(ref)
+                assert err < 5e-5, (fn, name, err)
+
+
+def test_precompute_rejects_bad_arguments(lib):
+    with pytest.raises(lib.LprecError, match="filter"):
+        lib.precompute(64, 96, 1, 32, 'cubic', 'no-such-filter')
+    with pytest.raises(lib.LprecError):
+        lib.precompute(0, 96, 1, 32, 'cubic', 'ramp')
+    with pytest.raises(lib.LprecError):
+        lib.precompute(64, 0, 1, 32, 'cubic', 'ramp')
+
+
+def test_create_rejects_malformed_glpars(lib):
+    """Validation happens before any device work, so it runs without a GPU."""
+    gl = lib.precompute(64, 96, 1, 32, 'cubic', 'ramp')[0].copy()
+    with pytest.raises(lib.LprecError):
+        lib.Handle(gl[:5], 0)
+    bad = gl.copy()
+    bad[4] = 4  # Nspan other than 3
+    with pytest.raises(lib.LprecError, match="Nspan"):
+        lib.Handle(bad, 0)
+    bad = gl.copy()
+    bad[0] = 72  # N not a power of the layout rules / inconsistent Ntheta
+    with pytest.raises(lib.LprecError):
+        lib.Handle(bad, 0)
+
+
+def test_null_handle_calls_return_errors(lib):
+    L = lib.lib()
+    assert L.lp_fwd(None, None, None, 1, None) == 1
+    assert L.lp_adj(None, None, None, 1, None) == 1
+    assert L.lp_set_schedule(None, 0, 1, 0, 1) == 1
+    assert b"null" in L.lp_last_error()
+    assert L.lp_destroy(None) == 0
