@@ -219,6 +219,22 @@ def cpu_baseline(packed, nproc, steps):
     return 1.0 / statistics.median(times), sum(times)
 
 
+def cpu_side_configs():
+    """Oracle fwd+adj of one slice at the two smaller workloads (single process)."""
+    sys.path.insert(0, ROOT)
+    from oracle import lprec_oracle as O
+    out = {}
+    for N, Nproj, filt, n_ell in ((256, 384, "ramp", 10), (1024, 1536, "shepp-logan", 20)):
+        tr = O.Transform(N, Nproj, 1, filt, N / 2, "cubic", mode="fp64")
+        f = O.ellipse_phantom(N, n_ell, np.random.default_rng(0))[None]
+        R = tr.fwd(f)
+        t0 = time.perf_counter()
+        R = tr.fwd(f)
+        tr.adj(R)
+        out["n%d_slices_per_s" % N] = 1.0 / (time.perf_counter() - t0)
+    return out
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
@@ -261,8 +277,10 @@ def per_kernel_bytes(h, S, prof):
     b = {
         "fwd_ingest": S * (N0 * N0 + N * N) * 4,
         "col_prefilter": S * (2 * N * N + 2 * P * N) * 4 / 2,      # mean of the fwd and adj launches
-        "fwd_c2lp": S * (N * N * 4 + Nk * Nth * 8) + Nth * Nrho * 8 / 1,
-        "theta_conv": S * (Nk * Nth * 8 + Nk * half * 8) + Nk * Nth * 8,
+        # image read once, spectrum columns holding disk points written once, coordinate table
+        "fwd_c2lp": S * (N * N * 4 + Nk * half * 8) + Nth * Nrho * 8 / 2,
+        # columns in use read and written once, fZ once per launch
+        "theta_conv": S * (Nk * half * 8 + Nk * half * 8) + Nk * Nth * 8,
         "fwd_lp2polar": S * (Nk * half * 8 + P0 // 3 * N0 * 4),
         "adj_ingest": S * (P0 * N0 + P * N) * 4,
         "adj_polar2lp": S * (P // 3 * N * 4 + Nk * half * 8),
@@ -491,11 +509,11 @@ def run_ours(args):
         lp.fwd(fh, dev, out=Rh_out)
         lp.adj(Rh, dev, out=fh_out)
 
-    for _ in range(max(1, args.warmup // 2)):
+    for _ in range(max(2, args.warmup // 2)):
         e2e_step()
     torch.cuda.synchronize()
     q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ke = max(2, args.steps // 2)
+    ke = max(3, args.steps)
     q0.record(stream)
     for _ in range(ke):
         e2e_step()
@@ -552,6 +570,8 @@ def run_ours(args):
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nproc, "kind": "port",
                                 "sample": "3 steps of 1 slice fwd+adj N=%d (%.1f s), float64 oracle, spans in %d "
                                           "processes" % (N, busy, nproc)}
+        if not args.small:
+            line["cpu_baseline"]["single_process"] = cpu_side_configs()
     if dist:
         tdist.barrier()
         tdist.destroy_process_group()
