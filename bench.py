@@ -471,7 +471,7 @@ def run_ours(args):
     ms = e0.elapsed_time(e1)
     # per-kernel times: the same steps with the whole batch in one chunk on one
     # stream (launches do not overlap), CUDA events around every launch
-    h.set_schedule()
+    h.set_schedule(fwd_theta_block=sched["fwd_theta_block"], adj_theta_block=sched["adj_theta_block"])
     step()
     torch.cuda.synchronize()
     h.set_profiling(True)

@@ -146,21 +146,26 @@ int lp_set_profiling(lp_handle* h, int enable);
 int lp_profile_collect(lp_handle* h, double* ms, int64_t* launches);
 
 /*
- * Batch schedule (no reference counterpart; the reference runs every kernel
- * once over the whole batch on the legacy stream).  lp_fwd / lp_adj split a
- * call's S0 slices into chunks of `chunk` slices (0: one chunk) processed in
- * turn, alternating between the caller's stream and a second stream owned by
- * the handle when `streams` is 2 (forked from and joined back into the
- * caller's stream with events).  Results do not depend on the schedule.
- * Defaults: chunk 0, streams 1.  out[4] = {fwd_chunk, fwd_streams,
- * adj_chunk, adj_streams}.
+ * Batch schedule and kernel shapes (no reference counterpart; the reference
+ * runs every kernel once over the whole batch on the legacy stream).
+ * sched[LP_SCHEDULE_LEN] = {fwd_chunk, fwd_streams, fwd_theta_block,
+ *                           adj_chunk, adj_streams, adj_theta_block}:
+ * lp_fwd / lp_adj split a call's S0 slices into chunks of `chunk` slices
+ * (0: one chunk) processed in turn, alternating between the caller's stream
+ * and a second stream owned by the handle when `streams` is 2 (forked from
+ * and joined back into the caller's stream with events); `theta_block` is the
+ * thread count (256 or 512) of the theta-convolution blocks.  Results do not
+ * depend on the schedule.  lp_set_schedule takes the first n entries (the
+ * rest get the defaults {0, 1, 256, 0, 1, 256}); lp_get_schedule writes n.
  */
-int lp_set_schedule(lp_handle* h, int fwd_chunk, int fwd_streams, int adj_chunk, int adj_streams);
-int lp_get_schedule(const lp_handle* h, int32_t out[4]);
+#define LP_SCHEDULE_LEN 6
+int lp_set_schedule(lp_handle* h, const int32_t* sched, int n);
+int lp_get_schedule(const lp_handle* h, int32_t* out, int n);
 
 /*
  * Autotuner (no reference counterpart): time every candidate schedule (chunks
- * of 64, 32, 16, 8 slices or none; one or two streams) of lp_fwd and lp_adj on
+ * of 64, 32, 16, 8 slices or none; one or two streams; theta-convolution
+ * blocks of 256 or 512 threads) of lp_fwd and lp_adj on
  * S0 slices, using the caller's device buffers R[S0][Nproj][N0] and
  * f[S0][N0][N0] as scratch input/output (their contents are overwritten), and
  * keep the fastest for this handle.  Synchronises `stream`; do not call it

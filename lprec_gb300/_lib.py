@@ -71,8 +71,8 @@ def lib():
         "lp_set_profiling": (c_int, [c_void_p, c_int]),
         "lp_profile_collect": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_double), P_i64]),
         "lp_debug_fill_scratch": (c_int, [c_void_p, ctypes.c_float, c_void_p]),
-        "lp_set_schedule": (c_int, [c_void_p, c_int, c_int, c_int, c_int]),
-        "lp_get_schedule": (c_int, [c_void_p, P_i32]),
+        "lp_set_schedule": (c_int, [c_void_p, P_i32, c_int]),
+        "lp_get_schedule": (c_int, [c_void_p, P_i32, c_int]),
         "lp_autotune": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, P_f32]),
     }
     for name, (res, args) in sig.items():
@@ -169,13 +169,17 @@ class Handle:
         check(lib().lp_device_bytes(self._h, _ptr(b, ctypes.c_int64)))
         return int(b[0])
 
-    def set_schedule(self, fwd_chunk=0, fwd_streams=1, adj_chunk=0, adj_streams=1):
-        check(lib().lp_set_schedule(self._h, int(fwd_chunk), int(fwd_streams), int(adj_chunk), int(adj_streams)))
+    SCHEDULE_KEYS = ("fwd_chunk", "fwd_streams", "fwd_theta_block", "adj_chunk", "adj_streams", "adj_theta_block")
+
+    def set_schedule(self, fwd_chunk=0, fwd_streams=1, fwd_theta_block=256, adj_chunk=0, adj_streams=1,
+                     adj_theta_block=256):
+        v = np.array([fwd_chunk, fwd_streams, fwd_theta_block, adj_chunk, adj_streams, adj_theta_block], np.int32)
+        check(lib().lp_set_schedule(self._h, _ptr(v, ctypes.c_int32), len(v)))
 
     def schedule(self):
-        out = np.zeros(4, np.int32)
-        check(lib().lp_get_schedule(self._h, _ptr(out, ctypes.c_int32)))
-        return dict(fwd_chunk=int(out[0]), fwd_streams=int(out[1]), adj_chunk=int(out[2]), adj_streams=int(out[3]))
+        out = np.zeros(len(self.SCHEDULE_KEYS), np.int32)
+        check(lib().lp_get_schedule(self._h, _ptr(out, ctypes.c_int32), len(out)))
+        return dict(zip(self.SCHEDULE_KEYS, (int(x) for x in out)))
 
     def autotune(self, R, f, S0, stream):
         """Pick the fastest batch schedule on S0 slices of the device buffers R, f (overwritten)."""

@@ -101,7 +101,7 @@ struct FwdDev {
   DevBuf<float> rhoc;      // [Nproj][N]
   DevBuf<int> rows[3];     // internal rows per span (multiples of os only)
   int nrows[3] = {0, 0, 0};
-  DevBuf<float2> fz;       // [Nk][Nth]
+  DevBuf<float2> fz;       // Hermitian-extended kernel, tiled spectrum layout
   int lo = 0, hi = 0;      // theta columns the polar gather reads
   DevBuf<float> fbuf;      // [Nslices][N][N]
   // cubic mode: the prefiltered image of each slice as a 2-D CUDA array that
@@ -128,7 +128,7 @@ struct AdjDev {
   DevBuf<float2> c2lp[3];  // [N0][N0]
   int clo[3], chi[3];
   int lo2 = 0, hi2 = 0, W2 = 1;
-  DevBuf<float2> fz;       // [Nk][Nth]
+  DevBuf<float2> fz;       // Hermitian-extended kernel, tiled spectrum layout
   DevBuf<float> H;         // [4N] or empty
   bool filter = false;
   DevBuf<float> rbuf;      // [Nslices][Nproj][N]
@@ -189,6 +189,7 @@ struct lp_handle {
   // one chunk) and streams the chunks alternate on (1 or 2); set by
   // lp_set_schedule or lp_autotune
   int fwd_chunk = 0, fwd_streams = 1, adj_chunk = 0, adj_streams = 1;
+  int fwd_tblock = 256, adj_tblock = 256;  // threads per block of the theta convolution
   cudaStream_t side = nullptr;        // second stream of a 2-stream schedule
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
@@ -247,7 +248,7 @@ static std::vector<float2> extend_kernel(const float* v, int Nrho, int Nth) {
     const size_t i = 2 * ((size_t)kr * nh + kt);
     return std::make_pair((double)v[i], (double)v[i + 1]);
   };
-  std::vector<float2> out((size_t)Nk * Nth);
+  std::vector<float2> out(spec_slice(Nk, Nth), make_float2(0.f, 0.f));
   for (int kr = 0; kr < Nk; ++kr) {
     const int mr = (Nrho - kr) % Nrho;
     for (int kt = 0; kt < Nth; ++kt) {
@@ -266,7 +267,7 @@ static std::vector<float2> extend_kernel(const float* v, int Nrho, int Nth) {
         re = b.first;
         im = -b.second;
       }
-      out[(size_t)kr * Nth + kt] = make_float2((float)re, (float)im);
+      out[sidx(kr, kt, Nth)] = make_float2((float)re, (float)im);
     }
   }
   return out;
@@ -481,7 +482,7 @@ int lp_create(const float* glpars, int64_t n, int device, lp_handle** out) {
   if (e == cudaSuccess) e = dev_upload(h->erho, h->erho_h);
   if (e == cudaSuccess) e = dev_upload(h->tw_rho, twiddles(h->Nrho));
   if (e == cudaSuccess) e = dev_upload(h->tw_th, twiddles(h->Nth));
-  if (e == cudaSuccess) e = dev_alloc(h->spec, (size_t)h->Nslices * h->Nk * h->Nth);
+  if (e == cudaSuccess) e = dev_alloc(h->spec, (size_t)h->Nslices * spec_slice(h->Nk, h->Nth));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
@@ -921,7 +922,7 @@ static int fwd_slices(lp_handle* h, float* R, const float* f, int s0, int n, cud
   f += (size_t)s0 * h->N0 * h->N0;
   R += (size_t)s0 * h->Nproj0 * h->N0;
   float* fbuf = F->fbuf.p + (size_t)s0 * h->N * h->N;
-  float2* spec = h->spec.p + (size_t)s0 * h->Nk * h->Nth;
+  float2* spec = h->spec.p + (size_t)s0 * spec_slice(h->Nk, h->Nth);
   const cudaTextureObject_t* tx = tex ? F->tex.p + s0 : nullptr;
   const cudaSurfaceObject_t* sf = tex ? F->surf.p + s0 : nullptr;
   FwdIngestArgs ia{f, fbuf, h->N, h->N0, h->N / 2 - h->N0 / 2, h->cubic};
@@ -935,7 +936,7 @@ static int fwd_slices(lp_handle* h, float* R, const float* f, int s0, int n, cud
                    h->plan_rho, tx, F->ival.p, F->dlo, F->dhi};
     CUDA_TRY(launch(h, K_FWD_C2LP, st, [&] { return launch_fwd_c2lp(a1, n, st); }));
     ThetaConvArgs a2{spec, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), F->dlo, F->dhi,
-                     F->lo & ~1, std::min(F->hi | 1, h->Nth - 1), 0, h->plan_th};
+                     F->lo & ~1, std::min(F->hi | 1, h->Nth - 1), 0, h->plan_th, h->fwd_tblock};
     CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, n, st); }));
     FwdLP2PolarArgs a3{spec, R, F->thc.p, F->rhoc.p, F->rows[k].p, F->nrows[k], h->N, h->N0, h->Nth,
                        h->Nrho, h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho};
@@ -950,7 +951,7 @@ static int adj_slices(lp_handle* h, float* f, const float* R, int s0, int n, cud
   R += (size_t)s0 * h->Nproj0 * h->N0;
   f += (size_t)s0 * h->N0 * h->N0;
   float* rbuf = A->rbuf.p + (size_t)s0 * h->Nproj * h->N;
-  float2* spec = h->spec.p + (size_t)s0 * h->Nk * h->Nth;
+  float2* spec = h->spec.p + (size_t)s0 * spec_slice(h->Nk, h->Nth);
   const size_t gstride = (size_t)A->W2 * h->Nrho;
   AdjIngestArgs ia{R, rbuf, A->filter ? A->H.p : nullptr, h->N, h->N0, h->Nproj, h->Nproj0, h->os,
                    h->N / 2 - h->cor, h->cubic, h->plan_filt};
@@ -972,7 +973,7 @@ static int adj_slices(lp_handle* h, float* f, const float* R, int s0, int n, cud
                        h->Nrho, h->Nk, h->Nproj, h->cubic, A->clo[k], A->chi[k], h->plan_rho};
     CUDA_TRY(launch(h, K_ADJ_POLAR2LP, st, [&] { return launch_adj_polar2lp(a1, n, st); }));
     ThetaConvArgs a2{spec, A->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), A->clo[k],
-                     A->chi[k], A->lo2, A->hi2, 0, h->plan_th};
+                     A->chi[k], A->lo2, A->hi2, 0, h->plan_th, h->adj_tblock};
     CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, n, st); }));
     AdjLPColsArgs a3{spec, G[k], h->Nth, h->Nrho, h->Nk, A->lo2, A->hi2, A->W2, h->plan_rho,
                      tex ? A->surf[k].p + s0 : nullptr};
@@ -1013,12 +1014,12 @@ int lp_fwd_transpose(lp_handle* h, float* f, const float* R, int S0, void* strea
   float* acc = F->fbuf.p;
   CUDA_TRY(cudaMemsetAsync(acc, 0, (size_t)S0 * h->N * h->N * sizeof(float), st));
   for (int k = 0; k < 3; ++k) {
-    CUDA_TRY(cudaMemsetAsync(h->spec.p, 0, (size_t)S0 * h->Nk * h->Nth * sizeof(float2), st));
+    CUDA_TRY(cudaMemsetAsync(h->spec.p, 0, (size_t)S0 * spec_slice(h->Nk, h->Nth) * sizeof(float2), st));
     FwdTPolarArgs a1{R, h->spec.p, F->thc.p, F->rhoc.p, F->rows[k].p, F->blk[k].p, h->N, h->N0, h->Nth, h->Nrho,
                      h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, F->lo, kTransposeCW, h->plan_rho};
     CUDA_TRY(launch(h, K_FWDT_POLAR, st, [&] { return launch_fwdT_polar(a1, S0, F->nblk[k], st); }));
     ThetaConvArgs a2{h->spec.p, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), F->lo, F->hi,
-                     F->dlo, F->dhi, 1, h->plan_th};
+                     F->dlo, F->dhi, 1, h->plan_th, h->fwd_tblock};
     if (F->dhi >= F->dlo)
       CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
     FwdTCartArgs a3{h->spec.p, acc, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, F->dlo, F->dhi,
@@ -1047,30 +1048,37 @@ int lp_adj(lp_handle* h, float* f, const float* R, int S0, void* stream) {
                     [&](int s0, int n, cudaStream_t st) { return adj_slices(h, f, R, s0, n, st); });
 }
 
-int lp_set_schedule(lp_handle* h, int fwd_chunk, int fwd_streams, int adj_chunk, int adj_streams) {
-  if (!h) return set_err(LP_ERR_ARG, "lp_set_schedule: null handle");
-  if (fwd_chunk < 0 || adj_chunk < 0 || fwd_streams < 1 || fwd_streams > 2 || adj_streams < 1 || adj_streams > 2)
-    return set_err(LP_ERR_ARG, "lp_set_schedule: chunk >= 0 and streams in {1, 2} required");
-  h->fwd_chunk = fwd_chunk;
-  h->fwd_streams = fwd_streams;
-  h->adj_chunk = adj_chunk;
-  h->adj_streams = adj_streams;
+int lp_set_schedule(lp_handle* h, const int32_t* sched, int n) {
+  if (!h || (!sched && n > 0)) return set_err(LP_ERR_ARG, "lp_set_schedule: null pointer");
+  if (n < 0 || n > LP_SCHEDULE_LEN) return set_err(LP_ERR_ARG, "lp_set_schedule: n=%d outside [0, %d]", n, LP_SCHEDULE_LEN);
+  int v[LP_SCHEDULE_LEN] = {0, 1, 256, 0, 1, 256};
+  for (int i = 0; i < n; ++i) v[i] = sched[i];
+  for (int d = 0; d < 2; ++d) {
+    const int* q = v + 3 * d;
+    if (q[0] < 0 || q[1] < 1 || q[1] > 2 || (q[2] != 256 && q[2] != 512))
+      return set_err(LP_ERR_ARG, "lp_set_schedule: chunk >= 0, streams in {1, 2}, theta block in {256, 512}");
+  }
+  h->fwd_chunk = v[0];
+  h->fwd_streams = v[1];
+  h->fwd_tblock = v[2];
+  h->adj_chunk = v[3];
+  h->adj_streams = v[4];
+  h->adj_tblock = v[5];
   return LP_OK;
 }
 
-int lp_get_schedule(const lp_handle* h, int32_t out[4]) {
-  if (!h || !out) return set_err(LP_ERR_ARG, "lp_get_schedule: null pointer");
-  out[0] = h->fwd_chunk;
-  out[1] = h->fwd_streams;
-  out[2] = h->adj_chunk;
-  out[3] = h->adj_streams;
+int lp_get_schedule(const lp_handle* h, int32_t* out, int n) {
+  if (!h || (!out && n > 0)) return set_err(LP_ERR_ARG, "lp_get_schedule: null pointer");
+  const int v[LP_SCHEDULE_LEN] = {h->fwd_chunk, h->fwd_streams, h->fwd_tblock,
+                                  h->adj_chunk, h->adj_streams, h->adj_tblock};
+  for (int i = 0; i < n && i < LP_SCHEDULE_LEN; ++i) out[i] = v[i];
   return LP_OK;
 }
 
 // Time every candidate schedule of one direction on the caller's buffers and
 // keep the fastest (ties go to the earlier, simpler candidate).
 static int tune_one(lp_handle* h, bool fwd, float* R, float* f, int S0, cudaStream_t st, int reps,
-                    int* best_chunk, int* best_streams, float* best_ms) {
+                    int* best_chunk, int* best_streams, int* best_tblock, float* best_ms) {
   const int chunks[] = {0, 64, 32, 16, 8};
   cudaEvent_t a = nullptr, b = nullptr;
   CUDA_TRY(cudaEventCreate(&a));
@@ -1079,9 +1087,12 @@ static int tune_one(lp_handle* h, bool fwd, float* R, float* f, int S0, cudaStre
   h->profiling = false;
   float best = 1e30f;
   int rc = LP_OK;
+  int* tblock = fwd ? &h->fwd_tblock : &h->adj_tblock;
+  for (int tb = 256; tb <= 512 && rc == LP_OK; tb += 256)
   for (int ci = 0; ci < 5 && rc == LP_OK; ++ci) {
     const int c = chunks[ci];
     if (c != 0 && c >= S0) continue;
+    *tblock = tb;
     for (int ns = 1; ns <= 2 && rc == LP_OK; ++ns) {
       if (ns == 2 && (c == 0 || (S0 + c - 1) / c < 2)) continue;
       auto one = [&] {
@@ -1101,10 +1112,12 @@ static int tune_one(lp_handle* h, bool fwd, float* R, float* f, int S0, cudaStre
         best = ms / reps;
         *best_chunk = c;
         *best_streams = ns;
+        *best_tblock = tb;
       }
     }
   }
   h->profiling = prof;
+  *tblock = *best_tblock;
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   *best_ms = best;
@@ -1119,11 +1132,19 @@ int lp_autotune(lp_handle* h, float* R, float* f, int S0, void* stream, float ou
   cudaStream_t st = (cudaStream_t)stream;
   float ms[2] = {0.f, 0.f};
   if (h->fwd) {
-    int rc = tune_one(h, true, R, f, S0, st, 2, &h->fwd_chunk, &h->fwd_streams, &ms[0]);
+    int c = 0, ns = 1, tb = 256;
+    int rc = tune_one(h, true, R, f, S0, st, 2, &c, &ns, &tb, &ms[0]);
+    h->fwd_chunk = c;
+    h->fwd_streams = ns;
+    h->fwd_tblock = tb;
     if (rc != LP_OK) return rc;
   }
   if (h->adj) {
-    int rc = tune_one(h, false, R, f, S0, st, 2, &h->adj_chunk, &h->adj_streams, &ms[1]);
+    int c = 0, ns = 1, tb = 256;
+    int rc = tune_one(h, false, R, f, S0, st, 2, &c, &ns, &tb, &ms[1]);
+    h->adj_chunk = c;
+    h->adj_streams = ns;
+    h->adj_tblock = tb;
     if (rc != LP_OK) return rc;
   }
   if (out_ms) {
@@ -1184,7 +1205,7 @@ static inline size_t round256(size_t b) { return (b + 255) / 256 * 256; }
 extern "C" int lp_noalloc_scratch_bytes(const lp_handle* h, int S0, int64_t* bytes) {
   if (!h || !bytes) return set_err(LP_ERR_ARG, "lp_noalloc_scratch_bytes: null pointer");
   *bytes = (int64_t)(round256((size_t)S0 * h->N * h->N * sizeof(float)) +
-                     round256((size_t)S0 * h->Nk * h->Nth * sizeof(float2)));
+                     round256((size_t)S0 * spec_slice(h->Nk, h->Nth) * sizeof(float2)));
   return LP_OK;
 }
 
@@ -1196,7 +1217,7 @@ extern "C" int lp_fwd_noalloc(lp_handle* h, float* R, const float* f, int S0, vo
   if (S0 == 0) return LP_OK;
   if (!R || !f) return set_err(LP_ERR_ARG, "lp_fwd_noalloc: null data pointer");
   const size_t fbytes = round256((size_t)S0 * h->N * h->N * sizeof(float));
-  const size_t sbytes = round256((size_t)S0 * h->Nk * h->Nth * sizeof(float2));
+  const size_t sbytes = round256((size_t)S0 * spec_slice(h->Nk, h->Nth) * sizeof(float2));
   if (fbytes + sbytes > (size_t)LP_NOALLOC_SCRATCH_BYTES)
     return set_err(LP_ERR_UNSUPPORTED,
                    "lp_fwd_noalloc: %d slices of N=%d need %zu bytes of scratch, more than the fixed %lld; "
@@ -1221,7 +1242,7 @@ extern "C" int lp_fwd_noalloc(lp_handle* h, float* R, const float* f, int S0, vo
                    nullptr, F->ival.p, F->dlo, F->dhi};
     CUDA_TRY(launch(h, K_FWD_C2LP, st, [&] { return launch_fwd_c2lp(a1, S0, st); }));
     ThetaConvArgs a2{spec, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), F->dlo, F->dhi,
-                     F->lo & ~1, std::min(F->hi | 1, h->Nth - 1), 0, h->plan_th};
+                     F->lo & ~1, std::min(F->hi | 1, h->Nth - 1), 0, h->plan_th, h->fwd_tblock};
     CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
     FwdLP2PolarArgs a3{spec, R, F->thc.p, F->rhoc.p, F->rows[k].p, F->nrows[k], h->N, h->N0, h->Nth,
                        h->Nrho, h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho};

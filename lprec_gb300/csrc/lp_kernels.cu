@@ -389,12 +389,12 @@ __global__ void __launch_bounds__(256, 2) k_fwd_c2lp(FwdC2LPArgs a) {
   }
   __syncthreads();
   const CBuf Z = fft_block<-1>(A, B, a.plan, 1, 0);
-  float2* out = a.spec + (size_t)s * a.Nk * a.Nth;
+  float2* out = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
   for (int k = threadIdx.x; k < a.Nk; k += blockDim.x) {
     const float2 z1 = Z.get(k);
     const float2 z2 = Z.get(k == 0 ? 0 : a.Nrho - k);
-    out[(size_t)k * a.Nth + th] = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
-    if (thb >= 0) out[(size_t)k * a.Nth + thb] = make_float2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
+    out[sidx(k, th, a.Nth)] = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+    if (thb >= 0) out[sidx(k, thb, a.Nth)] = make_float2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
   }
 }
 
@@ -410,19 +410,18 @@ __global__ void __launch_bounds__(256, 2) k_theta_conv(ThetaConvArgs a) {
   const int s = blockIdx.x;
   const int k0 = 2 * blockIdx.y;
   const int nrow = (k0 + 1 < a.Nk) ? 2 : 1;
-  float2* rows = a.spec + ((size_t)s * a.Nk + k0) * a.Nth;
+  float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
   const int ps = fft_plane_floats(a.Nth);  // plane stride between the two rows
   for (int i = threadIdx.x; i < 2 * a.Nth; i += blockDim.x) {
     const int r = i / a.Nth, t = i - r * a.Nth;
     const bool in = r < nrow && t >= a.in_lo && t <= a.in_hi;
-    A.offset(r * ps).set(t, in ? rows[i] : make_float2(0.f, 0.f));
+    A.offset(r * ps).set(t, in ? sp[sidx(k0 + r, t, a.Nth)] : make_float2(0.f, 0.f));
   }
   __syncthreads();
   const CBuf X = fft_block<-1>(A, B, a.plan, 2, ps);
-  const float2* fz = a.fz + (size_t)k0 * a.Nth;
   for (int i = threadIdx.x; i < nrow * a.Nth; i += blockDim.x) {
     const int r = i / a.Nth, t = i - r * a.Nth;
-    float2 w = __ldg(fz + i);
+    float2 w = __ldg(a.fz + sidx(k0 + r, t, a.Nth));
     if (a.conj_fz) w.y = -w.y;
     const CBuf Xr = X.offset(r * ps);
     Xr.set(t, cscale(cmul(Xr.get(t), w), a.scale));
@@ -432,7 +431,7 @@ __global__ void __launch_bounds__(256, 2) k_theta_conv(ThetaConvArgs a) {
   const int w = a.out_hi - a.out_lo + 1;
   for (int i = threadIdx.x; i < nrow * w; i += blockDim.x) {
     const int r = i / w, t = a.out_lo + (i - r * w);
-    rows[(size_t)r * a.Nth + t] = Y.offset(r * ps).get(t);
+    sp[sidx(k0 + r, t, a.Nth)] = Y.offset(r * ps).get(t);
   }
 }
 
@@ -479,17 +478,18 @@ __global__ void __launch_bounds__(256, 2) k_fwd_lp2polar(FwdLP2PolarArgs a) {
     t1[j] = wrapi(c1 + j, a.Nth);
   }
   const int ntap = a.cubic ? 4 : 2;
-  const float2* sp = a.spec + (size_t)s * a.Nk * a.Nth;
+  const float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
   for (int k = threadIdx.x; k < a.Nk; k += blockDim.x) {
-    const float2* row = sp + (size_t)k * a.Nth;
     float2 v0 = make_float2(0.f, 0.f), v1 = make_float2(0.f, 0.f);
     for (int j = 0; j < ntap; ++j) {
-      const float2 q0 = row[t0[j]];
+      const float2 q0 = sp[sidx(k, t0[j], a.Nth)];
       v0.x += w0[j] * q0.x;
       v0.y += w0[j] * q0.y;
-      const float2 q1 = row[t1[j]];
-      v1.x += w1[j] * q1.x;
-      v1.y += w1[j] * q1.y;
+      if (r1 >= 0) {
+        const float2 q1 = sp[sidx(k, t1[j], a.Nth)];
+        v1.x += w1[j] * q1.x;
+        v1.y += w1[j] * q1.y;
+      }
     }
     put_pair(A, k, a.Nrho, v0, v1);
   }
@@ -640,12 +640,12 @@ __global__ void __launch_bounds__(256, 2) k_adj_polar2lp(AdjPolar2LPArgs a) {
     __syncthreads();
   }
   const CBuf Z = fft_block<-1>(A, B, a.plan, 1, 0);
-  float2* out = a.spec + (size_t)s * a.Nk * a.Nth;
+  float2* out = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
   for (int k = threadIdx.x; k < a.Nk; k += blockDim.x) {
     const float2 z1 = Z.get(k);
     const float2 z2 = Z.get(k == 0 ? 0 : a.Nrho - k);
-    out[(size_t)k * a.Nth + th0] = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
-    if (th1 >= 0) out[(size_t)k * a.Nth + th1] = make_float2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
+    out[sidx(k, th0, a.Nth)] = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+    if (th1 >= 0) out[sidx(k, th1, a.Nth)] = make_float2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
   }
 }
 
@@ -660,10 +660,10 @@ __global__ void __launch_bounds__(256, 2) k_adj_lpcols(AdjLPColsArgs a) {
   const int s = blockIdx.x;
   const int th0 = a.lo2 + 2 * blockIdx.y;
   const int th1 = th0 + 1 <= a.hi2 ? th0 + 1 : -1;
-  const float2* sp = a.spec + (size_t)s * a.Nk * a.Nth;
+  const float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
   for (int k = threadIdx.x; k < a.Nk; k += blockDim.x) {
-    const float2 v0 = sp[(size_t)k * a.Nth + th0];
-    const float2 v1 = th1 >= 0 ? sp[(size_t)k * a.Nth + th1] : make_float2(0.f, 0.f);
+    const float2 v0 = sp[sidx(k, th0, a.Nth)];
+    const float2 v1 = th1 >= 0 ? sp[sidx(k, th1, a.Nth)] : make_float2(0.f, 0.f);
     put_pair(A, k, a.Nrho, v0, v1);
   }
   __syncthreads();
@@ -954,47 +954,69 @@ __global__ void __launch_bounds__(256, 3) k_fwd_c2lp_p2(FwdC2LPArgs a) {
   __syncthreads();
   reg_fft<L, -1>(v, sm, t);
   if (!live) return;
-  float2* out = a.spec + (size_t)s * a.Nk * a.Nth;
-  for (int k = t; k < a.Nk; k += T) {
-    const float2 z1 = sm[spad(k)];
-    const float2 z2 = sm[spad((L - k) & (L - 1))];
-    const float4 pr = make_float4(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y), 0.5f * (z1.y + z2.y),
-                                  0.5f * (z2.x - z1.x));
-    if (has_b) *reinterpret_cast<float4*>(out + (size_t)k * a.Nth + th) = pr;
-    else out[(size_t)k * a.Nth + th] = make_float2(pr.x, pr.y);
+  float2* out = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
+  // two consecutive rho frequencies per thread and column: 16-byte stores (the
+  // pair k, k+1 of a column is adjacent in the tiled layout; k + 1 = Nk lands
+  // in the tile's padding)
+  for (int k = 2 * t; k < a.Nk; k += 2 * T) {
+    const float2 z1 = sm[spad(k)], z2 = sm[spad((L - k) & (L - 1))];
+    const float2 y1 = sm[spad(k + 1)], y2 = sm[spad(L - k - 1)];
+    *reinterpret_cast<float4*>(out + sidx(k, th, a.Nth)) =
+        make_float4(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y), 0.5f * (y1.x + y2.x), 0.5f * (y1.y - y2.y));
+    if (has_b)
+      *reinterpret_cast<float4*>(out + sidx(k, th + 1, a.Nth)) =
+          make_float4(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x), 0.5f * (y1.y + y2.y), 0.5f * (y2.x - y1.x));
   }
 }
 
+// Theta convolution launch shape: BLK threads (256 or 512, picked per
+// geometry by the autotuner) carry NSIG = BLK / T rows (rho frequencies).  Threads are assigned so that the KT = min(4, NSIG) rows of one
+// spectrum tile alternate fastest: lane l works on row (l % KT) of the tile and
+// theta position t = l / KT, so a warp access covers 32 / KT consecutive theta
+// columns of all KT rows -- one contiguous run in the tiled layout.  The rows'
+// shared buffers are spaced by 32 / KT extra banks so that the KT rows' accesses
+// of one half-warp fall in distinct banks.
+template <int L, int BLK>
+struct TC {
+  static constexpr int T = L / 16;
+  static constexpr int BLOCK = BLK > T ? BLK : T;
+  static constexpr int NSIG = BLOCK / T;
+  static constexpr int KT = NSIG < kSpecTile ? NSIG : kSpecTile;
+  static constexpr int SLOTS = reg_fft_slots(L) + (KT > 1 ? 16 / KT : 0);
+};
+
 // per rho frequency: FFT along theta, multiply by the kernel, inverse; NSIG rows per block
-template <int L>
-__global__ void __launch_bounds__(256, 2) k_theta_conv_p2(ThetaConvArgs a) {
+template <int L, int BLK>
+__global__ void __launch_bounds__(TC<L, BLK>::BLOCK, 512 / TC<L, BLK>::BLOCK) k_theta_conv_p2(ThetaConvArgs a) {
   extern __shared__ float2 sm2[];
-  constexpr int T = P2<L>::T;
-  const int sig = threadIdx.x / T, t = threadIdx.x % T;
-  float2* sm = sm2 + sig * P2<L>::SLOTS;
+  using C = TC<L, BLK>;
+  constexpr int T = C::T, KT = C::KT;
+  const int g = threadIdx.x / (KT * T), r = threadIdx.x % (KT * T);
+  const int sig = g * KT + r % KT, t = r / KT;
+  float2* sm = sm2 + sig * C::SLOTS;
   const int s = blockIdx.x;
-  const int k = blockIdx.y * P2<L>::NSIG + sig;
+  const int k = blockIdx.y * C::NSIG + sig;
   const bool live = k < a.Nk;
-  float2* row = a.spec + ((size_t)s * a.Nk + (live ? k : 0)) * L;
+  float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, L);
   float2 v[16];
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
     const int c = t + i * T;
-    v[i] = (live && c >= a.in_lo && c <= a.in_hi) ? row[c] : make_float2(0.f, 0.f);
+    v[i] = (live && c >= a.in_lo && c <= a.in_hi) ? sp[sidx(k, c, L)] : make_float2(0.f, 0.f);
   }
   reg_fft<L, -1>(v, sm, t);
-  const float2* fz = a.fz + (size_t)(live ? k : 0) * L;
+  const int kf = live ? k : 0;
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
     const int c = t + i * T;
-    float2 w = __ldg(fz + c);
+    float2 w = __ldg(a.fz + sidx(kf, c, L));
     if (a.conj_fz) w.y = -w.y;
     v[i] = cscale(cmul(sm[spad(c)], w), a.scale);
   }
   __syncthreads();
   reg_fft<L, 1>(v, sm, t);
   if (!live) return;
-  for (int c = a.out_lo + t; c <= a.out_hi; c += T) row[c] = sm[spad(c)];
+  for (int c = a.out_lo + t; c <= a.out_hi; c += T) sp[sidx(k, c, L)] = sm[spad(c)];
 }
 
 // element p of the complex signal whose inverse FFT gives two real profiles
@@ -1035,51 +1057,50 @@ __global__ void __launch_bounds__(256, 3) k_fwd_lp2polar_p2(FwdLP2PolarArgs a) {
     t1[j] = wrapi(c1 + j, a.Nth);
   }
   const int ntap = a.cubic ? 4 : 2;
-  const float2* sp = a.spec + (size_t)s * a.Nk * a.Nth;
+  const float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
   // both rows' taps as offsets into one run of consecutive columns starting at cu
   const int cu = min(c0, r1 >= 0 ? c1 : c0);
   const int nu = max(c0, r1 >= 0 ? c1 : c0) - cu + ntap;
   const bool run = nu <= 8 && cu >= 0 && cu + nu <= a.Nth;
-  // the run read as 16-byte pairs of columns from an even column cu2 (Nth is even);
-  // the theta convolution writes whole even-aligned column pairs around the
-  // taps, so the extra column of a pair holds finite data (its weight is 0)
-  const int cu2 = cu & ~1;
-  const int nq = (cu + nu - cu2 + 1) >> 1;
-  float u0[10], u1[10];
+  float u0[8], u1[8];
 #pragma unroll
-  for (int q = 0; q < 10; ++q) {
-    const int j0 = cu2 + q - c0, j1 = cu2 + q - c1;
+  for (int q = 0; q < 8; ++q) {
+    const int j0 = cu + q - c0, j1 = cu + q - c1;
     u0[q] = (j0 >= 0 && j0 < ntap) ? w0[j0] : 0.f;
     u1[q] = (r1 >= 0 && j1 >= 0 && j1 < ntap) ? w1[j1] : 0.f;
   }
-#pragma unroll 3
-  for (int kk = t; kk <= L / 2; kk += T) {
-    const float2* row = sp + (size_t)kk * a.Nth;
-    float2 v0 = make_float2(0.f, 0.f), v1 = make_float2(0.f, 0.f);
+  // two consecutive rho frequencies per thread: one 16-byte load per column
+  // (frequencies kk, kk+1 of a column are adjacent in the tiled layout)
+#pragma unroll 1
+  for (int kk = 2 * t; kk <= L / 2; kk += 2 * T) {
+    float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = make_float4(0.f, 0.f, 0.f, 0.f);
     if (run) {
-      const float4* row4 = reinterpret_cast<const float4*>(row + cu2);
 #pragma unroll
-      for (int q = 0; q < 5; ++q) {
-        if (q < nq) {
-          const float4 z = row4[q];
-          v0.x += u0[2 * q] * z.x + u0[2 * q + 1] * z.z;
-          v0.y += u0[2 * q] * z.y + u0[2 * q + 1] * z.w;
-          v1.x += u1[2 * q] * z.x + u1[2 * q + 1] * z.z;
-          v1.y += u1[2 * q] * z.y + u1[2 * q + 1] * z.w;
+      for (int q = 0; q < 8; ++q) {
+        if (q < nu) {
+          const float4 z = *reinterpret_cast<const float4*>(sp + sidx(kk, cu + q, a.Nth));
+          v0.x += u0[q] * z.x; v0.y += u0[q] * z.y; v0.z += u0[q] * z.z; v0.w += u0[q] * z.w;
+          v1.x += u1[q] * z.x; v1.y += u1[q] * z.y; v1.z += u1[q] * z.z; v1.w += u1[q] * z.w;
         }
       }
     } else {
       for (int j = 0; j < ntap; ++j) {
-        const float2 q0 = row[t0[j]];
-        v0.x += w0[j] * q0.x;
-        v0.y += w0[j] * q0.y;
-        const float2 q1 = row[t1[j]];
-        v1.x += w1[j] * q1.x;
-        v1.y += w1[j] * q1.y;
+        const float4 q0 = *reinterpret_cast<const float4*>(sp + sidx(kk, t0[j], a.Nth));
+        v0.x += w0[j] * q0.x; v0.y += w0[j] * q0.y; v0.z += w0[j] * q0.z; v0.w += w0[j] * q0.w;
+        if (r1 >= 0) {
+          const float4 q1 = *reinterpret_cast<const float4*>(sp + sidx(kk, t1[j], a.Nth));
+          v1.x += w1[j] * q1.x; v1.y += w1[j] * q1.y; v1.z += w1[j] * q1.z; v1.w += w1[j] * q1.w;
+        }
       }
     }
-    sm[spad(kk)] = pair_elem(kk, L, v0, v1);
-    if (kk > 0 && kk < L / 2) sm[spad(L - kk)] = pair_elem(L - kk, L, v0, v1);
+    const float2 a0 = make_float2(v0.x, v0.y), a1 = make_float2(v1.x, v1.y);
+    sm[spad(kk)] = pair_elem(kk, L, a0, a1);
+    if (kk > 0) sm[spad(L - kk)] = pair_elem(L - kk, L, a0, a1);
+    if (kk + 1 <= L / 2) {  // kk + 1 < L / 2 here since kk is even and L / 2 is even
+      const float2 b0 = make_float2(v0.z, v0.w), b1 = make_float2(v1.z, v1.w);
+      sm[spad(kk + 1)] = pair_elem(kk + 1, L, b0, b1);
+      sm[spad(L - kk - 1)] = pair_elem(L - kk - 1, L, b0, b1);
+    }
   }
   __syncthreads();
   float2 v[16];
@@ -1255,19 +1276,16 @@ __global__ void __launch_bounds__(256, 3) k_adj_polar2lp_p2(AdjPolar2LPArgs a) {
   __syncthreads();
   reg_fft<L, -1>(v, sm, t);
   if (!live) return;
-  float2* out = a.spec + (size_t)s * a.Nk * a.Nth;
-  const bool al = ((th0 & 1) == 0) && th1 >= 0;  // 16-byte aligned pair
-  for (int k = t; k < a.Nk; k += T) {
-    const float2 z1 = sm[spad(k)];
-    const float2 z2 = sm[spad((L - k) & (L - 1))];
-    const float4 pr = make_float4(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y), 0.5f * (z1.y + z2.y),
-                                  0.5f * (z2.x - z1.x));
-    if (al) {
-      *reinterpret_cast<float4*>(out + (size_t)k * a.Nth + th0) = pr;
-    } else {
-      out[(size_t)k * a.Nth + th0] = make_float2(pr.x, pr.y);
-      if (th1 >= 0) out[(size_t)k * a.Nth + th1] = make_float2(pr.z, pr.w);
-    }
+  float2* out = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
+  // frequencies k, k+1 of a column in one 16-byte store (k + 1 = Nk: tile padding)
+  for (int k = 2 * t; k < a.Nk; k += 2 * T) {
+    const float2 z1 = sm[spad(k)], z2 = sm[spad((L - k) & (L - 1))];
+    const float2 y1 = sm[spad(k + 1)], y2 = sm[spad(L - k - 1)];
+    *reinterpret_cast<float4*>(out + sidx(k, th0, a.Nth)) =
+        make_float4(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y), 0.5f * (y1.x + y2.x), 0.5f * (y1.y - y2.y));
+    if (th1 >= 0)
+      *reinterpret_cast<float4*>(out + sidx(k, th1, a.Nth)) =
+          make_float4(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x), 0.5f * (y1.y + y2.y), 0.5f * (y2.x - y1.x));
   }
 }
 
@@ -1282,23 +1300,23 @@ __global__ void __launch_bounds__(256, 3) k_adj_lpcols_p2(AdjLPColsArgs a) {
   const int th0 = a.lo2 + 2 * (blockIdx.y * P2<L>::NSIG + sig);
   const bool live = th0 <= a.hi2;
   const int th1 = (live && th0 + 1 <= a.hi2) ? th0 + 1 : -1;
-  const float2* sp = a.spec + (size_t)s * a.Nk * a.Nth;
-  const bool al = ((th0 & 1) == 0) && th1 >= 0;
+  const float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
+  // frequencies kk, kk+1 of each column in one 16-byte load (kk even)
 #pragma unroll
-  for (int m = 0; m <= L / 2 / T; ++m) {
-    const int kk = t + m * T;
+  for (int m = 0; m <= L / 4 / T; ++m) {
+    const int kk = 2 * (t + m * T);
     if (kk > L / 2) break;
-    float2 v0 = make_float2(0.f, 0.f), v1 = make_float2(0.f, 0.f);
-    if (al) {
-      const float4 q = *reinterpret_cast<const float4*>(sp + (size_t)kk * a.Nth + th0);
-      v0 = make_float2(q.x, q.y);
-      v1 = make_float2(q.z, q.w);
-    } else if (live) {
-      v0 = sp[(size_t)kk * a.Nth + th0];
-      if (th1 >= 0) v1 = sp[(size_t)kk * a.Nth + th1];
+    float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (live) q0 = *reinterpret_cast<const float4*>(sp + sidx(kk, th0, a.Nth));
+    if (th1 >= 0) q1 = *reinterpret_cast<const float4*>(sp + sidx(kk, th1, a.Nth));
+    const float2 a0 = make_float2(q0.x, q0.y), a1 = make_float2(q1.x, q1.y);
+    sm[spad(kk)] = pair_elem(kk, L, a0, a1);
+    if (kk > 0) sm[spad(L - kk)] = pair_elem(L - kk, L, a0, a1);
+    if (kk + 1 <= L / 2) {
+      const float2 b0 = make_float2(q0.z, q0.w), b1 = make_float2(q1.z, q1.w);
+      sm[spad(kk + 1)] = pair_elem(kk + 1, L, b0, b1);
+      sm[spad(L - kk - 1)] = pair_elem(L - kk - 1, L, b0, b1);
     }
-    sm[spad(kk)] = pair_elem(kk, L, v0, v1);
-    if (kk > 0 && kk < L / 2) sm[spad(L - kk)] = pair_elem(L - kk, L, v0, v1);
   }
   __syncthreads();
   float2 v[16];
@@ -1326,7 +1344,8 @@ static bool p2_ok(int L) { return L >= 256 && L <= 8192 && (L & (L - 1)) == 0; }
 template <int L>
 static void set_p2_attrs(int optin) {
   cudaFuncSetAttribute(k_fwd_c2lp_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-  cudaFuncSetAttribute(k_theta_conv_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  cudaFuncSetAttribute(k_theta_conv_p2<L, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  cudaFuncSetAttribute(k_theta_conv_p2<L, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_fwd_lp2polar_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_adj_ingest_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_adj_polar2lp_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -1368,10 +1387,19 @@ bool p2_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st, cudaError_t* 
   if (!p2_ok(L)) return false;
 #define CALL(LL)                                                                              \
   {                                                                                           \
-    const size_t sm = (size_t)P2<LL>::NSIG * P2<LL>::SLOTS * sizeof(float2);                 \
-    if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; }   \
-    dim3 grid(S, (a.Nk + P2<LL>::NSIG - 1) / P2<LL>::NSIG);                                    \
-    k_theta_conv_p2<LL><<<grid, P2<LL>::BLOCK, sm, st>>>(a);                                  \
+    if (a.block == 512) {                                                                     \
+      using C = TC<LL, 512>;                                                                  \
+      const size_t sm = (size_t)C::NSIG * C::SLOTS * sizeof(float2);                          \
+      if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; } \
+      dim3 grid(S, (a.Nk + C::NSIG - 1) / C::NSIG);                                           \
+      k_theta_conv_p2<LL, 512><<<grid, C::BLOCK, sm, st>>>(a);                                \
+    } else {                                                                                  \
+      using C = TC<LL, 256>;                                                                  \
+      const size_t sm = (size_t)C::NSIG * C::SLOTS * sizeof(float2);                          \
+      if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; } \
+      dim3 grid(S, (a.Nk + C::NSIG - 1) / C::NSIG);                                           \
+      k_theta_conv_p2<LL, 256><<<grid, C::BLOCK, sm, st>>>(a);                                \
+    }                                                                                         \
   }
   switch (L) { case 256: CALL(256) break; case 512: CALL(512) break; case 1024: CALL(1024) break;
                case 2048: CALL(2048) break; case 4096: CALL(4096) break; case 8192: CALL(8192) break; }
@@ -1474,7 +1502,7 @@ __global__ void __launch_bounds__(256) k_fwdT_polar(FwdTPolarArgs a) {
   const int c0 = a.lo + b * a.CW;
   const int2 rr = __ldg(a.blk + b);
   const int ntap = a.cubic ? 4 : 2;
-  float2* sp = a.spec + (size_t)s * a.Nk * a.Nth;
+  float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
   const int L = a.Nrho;
   for (int i0 = rr.x; i0 < rr.y; i0 += 2) {
     const int r0 = a.rows[i0];
@@ -1515,22 +1543,19 @@ __global__ void __launch_bounds__(256) k_fwdT_polar(FwdTPolarArgs a) {
       }
       va = cscale(va, ak);
       vb = cscale(vb, ak);
-      float2* rowk = sp + (size_t)k * a.Nth;
       for (int j = 0; j < ntap; ++j) {
         const int ca = wrapi(t0 + j, a.Nth);
         if (ca >= c0 && ca < c0 + a.CW) {
-          float2 o = rowk[ca];
+          float2& o = sp[sidx(k, ca, a.Nth)];
           o.x += w0[j] * va.x;
           o.y += w0[j] * va.y;
-          rowk[ca] = o;
         }
         if (r1 >= 0) {
           const int cb = wrapi(t1 + j, a.Nth);
           if (cb >= c0 && cb < c0 + a.CW) {
-            float2 o = rowk[cb];
+            float2& o = sp[sidx(k, cb, a.Nth)];
             o.x += w1[j] * vb.x;
             o.y += w1[j] * vb.y;
-            rowk[cb] = o;
           }
         }
       }
@@ -1569,12 +1594,12 @@ __global__ void __launch_bounds__(256) k_fwdT_cart(FwdTCartArgs a) {
   const int s = blockIdx.x;
   const int th0 = a.dlo + 2 * blockIdx.y;
   const int th1 = th0 + 1 <= a.dhi ? th0 + 1 : -1;
-  const float2* sp = a.spec + (size_t)s * a.Nk * a.Nth;
+  const float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
   const int L = a.Nrho;
   for (int k = threadIdx.x; k < a.Nk; k += blockDim.x) {
     const float bk = (k == 0 || k == L / 2) ? 1.f : 0.5f;
-    const float2 v0 = cscale(sp[(size_t)k * a.Nth + th0], bk);
-    const float2 v1 = th1 >= 0 ? cscale(sp[(size_t)k * a.Nth + th1], bk) : make_float2(0.f, 0.f);
+    const float2 v0 = cscale(sp[sidx(k, th0, a.Nth)], bk);
+    const float2 v1 = th1 >= 0 ? cscale(sp[sidx(k, th1, a.Nth)], bk) : make_float2(0.f, 0.f);
     put_pair(A, k, L, v0, v1);
   }
   __syncthreads();

@@ -7,6 +7,22 @@
 
 namespace lpgb {
 
+// ---- spectrum layout ------------------------------------------------------
+// The log-polar spectrum of one slice (Nk rho frequencies x Ntheta columns,
+// complex) is stored in tiles of kSpecTile consecutive rho frequencies:
+// element (kk, th) sits at ((kk / 4) * Ntheta + th) * 4 + kk % 4.  A theta
+// column is then contiguous in runs of 4 frequencies (32 bytes) and a tile
+// row of 4 frequencies is contiguous across theta, so the column kernels
+// (one column per signal, frequencies across lanes) and the theta
+// convolution (4 frequencies per block, theta across lanes) both touch few
+// lines per warp access.  fZ uses the same layout.
+constexpr int kSpecTile = 4;
+__host__ __device__ inline int spec_rows(int Nk) { return (Nk + kSpecTile - 1) / kSpecTile * kSpecTile; }
+__host__ __device__ inline size_t spec_slice(int Nk, int Nth) { return (size_t)spec_rows(Nk) * Nth; }
+__host__ __device__ __forceinline__ size_t sidx(int kk, int th, int Nth) {
+  return ((size_t)(kk >> 2) * Nth + th) * 4 + (kk & 3);
+}
+
 // ---- forward ----------------------------------------------------------------
 struct FwdIngestArgs {        // centre f into the padded grid, prefilter rows
   const float* fin;           // [S][N0][N0] caller's image
@@ -22,7 +38,7 @@ struct ColPrefilterArgs {     // prefilter along the slow axis, in place
 
 struct FwdC2LPArgs {          // Cartesian -> log-polar gather, e^rho, FFT along rho
   const float* fbuf;          // [S][N][N] prefiltered image
-  float2* spec;               // [S][Nk][Nth] spectrum (Nk = N+1 rho frequencies)
+  float2* spec;               // [S] spectra (Nk = N+1 rho frequencies), tiled layout (sidx)
   const float2* c2lp;         // [Nth][Nrho] texel coordinates (x, y); x = NaN outside the disk
   const float* erho;          // [Nrho]
   int N, Nth, Nrho, Nk, cubic;
@@ -33,18 +49,19 @@ struct FwdC2LPArgs {          // Cartesian -> log-polar gather, e^rho, FFT along
 };
 
 struct ThetaConvArgs {        // FFT along theta, multiply by the kernel, inverse
-  float2* spec;               // [S][Nk][Nth]
-  const float2* fz;           // [Nk][Nth] Hermitian-extended kernel
+  float2* spec;               // [S] spectra, tiled layout
+  const float2* fz;           // Hermitian-extended kernel, tiled layout
   int Nth, Nk;
   float scale;
   int in_lo, in_hi;           // columns outside [in_lo, in_hi] are read as 0
   int out_lo, out_hi;         // only these columns are written back
   int conj_fz;
   FFTPlan plan;               // length Nth
+  int block;                  // power-of-two kernels: threads per block (256 or 512; 0 = 256)
 };
 
 struct FwdLP2PolarArgs {      // inverse FFT along rho of theta-combined columns, polar gather
-  const float2* spec;         // [S][Nk][Nth]
+  const float2* spec;         // [S] spectra, tiled layout
   float* Rout;                // [S][Nproj0][N0] caller's sinogram
   const float* thc;           // [Nproj] theta texel coordinate per internal angle row
   const float* rhoc;          // [Nproj][N] rho texel coordinate per polar point

@@ -163,8 +163,10 @@ class lpTransform:
         del f, R
         return h.schedule()
 
-    def set_schedule(self, gpu, fwd_chunk=0, fwd_streams=1, adj_chunk=0, adj_streams=1):
-        self._handle(gpu).set_schedule(fwd_chunk, fwd_streams, adj_chunk, adj_streams)
+    def set_schedule(self, gpu, **sched):
+        """Batch schedule by keyword (fwd_chunk, fwd_streams, fwd_theta_block, adj_chunk,
+        adj_streams, adj_theta_block); unnamed entries take their defaults."""
+        self._handle(gpu).set_schedule(**sched)
 
     # ---- host arrays, pipelined ---------------------------------------------
     def _host_op(self, op, x, out, gpu, chunk):

@@ -167,9 +167,9 @@ def test_schedules_bit_identical(torch_cuda, interp):
     G = O.create_geometry(128, 192, S, 64, interp)
     f, R = _inputs(G, S, 23)
     Rc, fc = _fwd(torch, h, f), _adj(torch, h, R)
-    for sched in ((3, 2, 2, 2), (2, 1, 3, 1), (1, 2, 1, 2), (4, 2, 0, 1)):
+    for sched in ((3, 2, 512, 2, 2, 256), (2, 1, 256, 3, 1, 512), (1, 2, 512, 1, 2, 512), (4, 2, 256, 0, 1, 256)):
         h.set_schedule(*sched)
-        assert h.schedule() == dict(zip(('fwd_chunk', 'fwd_streams', 'adj_chunk', 'adj_streams'), sched))
+        assert h.schedule() == dict(zip(h.SCHEDULE_KEYS, sched))
         assert np.array_equal(_fwd(torch, h, f), Rc), sched
         assert np.array_equal(_adj(torch, h, R), fc), sched
     Rt = torch.zeros((S, 192, 128), device='cuda')
@@ -181,7 +181,9 @@ def test_schedules_bit_identical(torch_cuda, interp):
     assert np.array_equal(_fwd(torch, h, f), Rc), sc
     assert np.array_equal(_adj(torch, h, R), fc), sc
     with pytest.raises(_lib.LprecError):
-        h.set_schedule(1, 3, 0, 1)
+        h.set_schedule(1, 3)
+    with pytest.raises(_lib.LprecError):
+        h.set_schedule(fwd_theta_block=384)
 
 
 @pytest.mark.parametrize("args", [(128, 192, 64, 'cubic', 'ramp'), (96, 144, 45, 'cubic', 'none'),

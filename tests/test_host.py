@@ -137,6 +137,6 @@ def test_null_handle_calls_return_errors(lib):
     L = lib.lib()
     assert L.lp_fwd(None, None, None, 1, None) == 1
     assert L.lp_adj(None, None, None, 1, None) == 1
-    assert L.lp_set_schedule(None, 0, 1, 0, 1) == 1
+    assert L.lp_set_schedule(None, None, 0) == 1
     assert b"null" in L.lp_last_error()
     assert L.lp_destroy(None) == 0
