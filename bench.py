@@ -565,7 +565,7 @@ def run_ours(args):
     if rank == 0 and not args.no_cpu:
         cores = len(os.sched_getaffinity(0))
         nproc = max(1, min(cores, 6))
-        packed = (lp.glpars, lp.fwdparsi, lp.fwdparamsf, lp.adjparsi, lp.adjparamsf)
+        packed = lp.tables()
         v, busy = cpu_baseline(packed, nproc, 3)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nproc, "kind": "port",
                                 "sample": "3 steps of 1 slice fwd+adj N=%d (%.1f s), float64 oracle, spans in %d "
@@ -656,7 +656,7 @@ def run_report(args):
     loss.backward()
     grad = x0.grad.cpu().double().numpy()
     # finite differences with the float64 oracle on 2 slices (same float32 tables)
-    tr2 = O.Transform.from_packed(lp16.glpars, lp16.fwdparsi, lp16.fwdparamsf, lp16.adjparsi, lp16.adjparamsf)
+    tr2 = O.Transform.from_packed(*lp16.tables())
     xx = ph[:2].astype(np.float64) * 0.5
 
     def L(v):

@@ -65,6 +65,16 @@ int lp_precompute(int N0, int Nproj, int Nslices, double cor, int cubic, const c
                   int32_t* adjparsi, float* adjparamsf);
 
 /*
+ * The same with the float arrays (fwdparamsf, adjparamsf) in float64: every
+ * value rounded once from the float64 computation to double instead of to
+ * float32 (no reference counterpart; the reference's format is float32).
+ * Feed them to lp_init_fwd_f64 / lp_init_adj_f64.
+ */
+int lp_precompute_f64(int N0, int Nproj, int Nslices, double cor, int cubic, const char* filter, int precision,
+                      int with_fwd, int nthreads, float* glpars, int32_t* fwdparsi, double* fwdparamsf,
+                      int32_t* adjparsi, double* adjparamsf);
+
+/*
  * Create a handle on `device` from glpars (replaces lpRgpu::lpRgpu(size_t
  * params, int gpu), src/cuda/lpRgpu.cu:7-39).  n = number of floats.
  */
@@ -75,6 +85,16 @@ int lp_init_fwd(lp_handle* h, const int32_t* parsi, int64_t ni, const float* par
 
 /* Upload adjoint tables and filter (replaces lpRgpu::initAdj, src/cuda/lpRgpu.cu:98-133). */
 int lp_init_adj(lp_handle* h, const int32_t* parsi, int64_t ni, const float* parsf, int64_t nf);
+
+/*
+ * lp_init_fwd / lp_init_adj with the float arrays in float64 (same layout as
+ * the packed float32 arrays; no reference counterpart).  Interpolation
+ * coordinates are kept on the device as 32-bit fixed point with F fraction
+ * bits (F = 17 at N = 2048, steps of 7.6e-6 texel), so float64 tables carry
+ * about 60 times less coordinate rounding than float32 ones near 4096.
+ */
+int lp_init_fwd_f64(lp_handle* h, const int32_t* parsi, int64_t ni, const double* parsf, int64_t nf);
+int lp_init_adj_f64(lp_handle* h, const int32_t* parsi, int64_t ni, const double* parsf, int64_t nf);
 
 /* Free everything the handle owns (replaces lpRgpu::~lpRgpu, src/cuda/lpRgpu.cu:41-58). */
 int lp_destroy(lp_handle* h);

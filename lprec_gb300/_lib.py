@@ -24,7 +24,8 @@ EXPORTS = ("lp_last_error", "lp_version", "lp_precompute_sizes", "lp_precompute"
            "lp_init_adj", "lp_destroy", "lp_fwd", "lp_adj", "lp_get_geometry", "lp_device_bytes",
            "lp_launch_count", "lp_kernel_count", "lp_kernel_name", "lp_set_profiling", "lp_profile_collect",
            "lp_fwd_noalloc", "lp_noalloc_scratch_bytes", "lp_fwd_transpose", "lp_debug_fill_scratch",
-           "lp_set_schedule", "lp_get_schedule", "lp_autotune")
+           "lp_set_schedule", "lp_get_schedule", "lp_autotune",
+           "lp_precompute_f64", "lp_init_fwd_f64", "lp_init_adj_f64")
 
 
 class LprecError(RuntimeError):
@@ -39,6 +40,7 @@ c_int, c_int64, c_double, c_void_p, c_char_p = ctypes.c_int, ctypes.c_int64, cty
 P_i32 = ctypes.POINTER(ctypes.c_int32)
 P_f32 = ctypes.POINTER(ctypes.c_float)
 P_i64 = ctypes.POINTER(ctypes.c_int64)
+P_f64 = ctypes.POINTER(ctypes.c_double)
 
 
 def lib():
@@ -54,6 +56,10 @@ def lib():
         "lp_precompute_sizes": (c_int, [c_int, c_int, c_int, c_double, c_int, c_char_p, P_i64]),
         "lp_precompute": (c_int, [c_int, c_int, c_int, c_double, c_int, c_char_p, c_int, c_int, c_int,
                                   P_f32, P_i32, P_f32, P_i32, P_f32]),
+        "lp_precompute_f64": (c_int, [c_int, c_int, c_int, c_double, c_int, c_char_p, c_int, c_int, c_int,
+                                      P_f32, P_i32, P_f64, P_i32, P_f64]),
+        "lp_init_fwd_f64": (c_int, [c_void_p, P_i32, c_int64, P_f64, c_int64]),
+        "lp_init_adj_f64": (c_int, [c_void_p, P_i32, c_int64, P_f64, c_int64]),
         "lp_create": (c_int, [P_f32, c_int64, c_int, ctypes.POINTER(c_void_p)]),
         "lp_init_fwd": (c_int, [c_void_p, P_i32, c_int64, P_f32, c_int64]),
         "lp_init_adj": (c_int, [c_void_p, P_i32, c_int64, P_f32, c_int64]),
@@ -97,8 +103,9 @@ def launch_count():
 
 
 def precompute(N0, Nproj, Nslices, cor, interp_type, filter_type, precision="reference", with_fwd=True,
-               nthreads=0):
-    """Host precompute; returns (glpars, fwdparsi, fwdparamsf, adjparsi, adjparamsf)."""
+               nthreads=0, wide=False):
+    """Host precompute; returns (glpars, fwdparsi, fwdparamsf, adjparsi, adjparamsf).  With
+    wide=True the two float arrays are float64 (same layout; for Handle.init_fwd/init_adj)."""
     L = lib()
     cubic = 1 if interp_type == "cubic" else 0
     filt = (filter_type or "none").encode()
@@ -106,12 +113,18 @@ def precompute(N0, Nproj, Nslices, cor, interp_type, filter_type, precision="ref
     check(L.lp_precompute_sizes(int(N0), int(Nproj), int(Nslices), float(cor), cubic, filt, _ptr(sizes, ctypes.c_int64)))
     gl = np.empty(sizes[0], np.float32)
     fi = np.empty(sizes[1] if with_fwd else 1, np.int32)
-    ff = np.empty(sizes[2] if with_fwd else 1, np.float32)
     ai = np.empty(sizes[3], np.int32)
-    af = np.empty(sizes[4], np.float32)
-    check(L.lp_precompute(int(N0), int(Nproj), int(Nslices), float(cor), cubic, filt, PRECISION[precision],
-                          1 if with_fwd else 0, int(nthreads), _ptr(gl, ctypes.c_float), _ptr(fi, ctypes.c_int32),
-                          _ptr(ff, ctypes.c_float), _ptr(ai, ctypes.c_int32), _ptr(af, ctypes.c_float)))
+    if wide:
+        ff = np.empty(sizes[2] if with_fwd else 1, np.float64)
+        af = np.empty(sizes[4], np.float64)
+        fn, ct = L.lp_precompute_f64, ctypes.c_double
+    else:
+        ff = np.empty(sizes[2] if with_fwd else 1, np.float32)
+        af = np.empty(sizes[4], np.float32)
+        fn, ct = L.lp_precompute, ctypes.c_float
+    check(fn(int(N0), int(Nproj), int(Nslices), float(cor), cubic, filt, PRECISION[precision],
+             1 if with_fwd else 0, int(nthreads), _ptr(gl, ctypes.c_float), _ptr(fi, ctypes.c_int32),
+             _ptr(ff, ct), _ptr(ai, ctypes.c_int32), _ptr(af, ct)))
     if not with_fwd:
         fi = ff = None
     return gl, fi, ff, ai, af
@@ -135,16 +148,25 @@ class Handle:
         self.has_fwd = False
         self.has_adj = False
 
+    @staticmethod
+    def _parsf(parsf):
+        """float64 arrays go to the *_f64 entry points, anything else as float32."""
+        if np.asarray(parsf).dtype == np.float64:
+            return np.ascontiguousarray(parsf), ctypes.c_double, "_f64"
+        return np.ascontiguousarray(parsf, dtype=np.float32), ctypes.c_float, ""
+
     def init_fwd(self, parsi, parsf):
         pi = np.ascontiguousarray(parsi, dtype=np.int32)
-        pf = np.ascontiguousarray(parsf, dtype=np.float32)
-        check(lib().lp_init_fwd(self._h, _ptr(pi, ctypes.c_int32), pi.size, _ptr(pf, ctypes.c_float), pf.size))
+        pf, ct, sfx = self._parsf(parsf)
+        fn = getattr(lib(), "lp_init_fwd" + sfx)
+        check(fn(self._h, _ptr(pi, ctypes.c_int32), pi.size, _ptr(pf, ct), pf.size))
         self.has_fwd = True
 
     def init_adj(self, parsi, parsf):
         pi = np.ascontiguousarray(parsi, dtype=np.int32)
-        pf = np.ascontiguousarray(parsf, dtype=np.float32)
-        check(lib().lp_init_adj(self._h, _ptr(pi, ctypes.c_int32), pi.size, _ptr(pf, ctypes.c_float), pf.size))
+        pf, ct, sfx = self._parsf(parsf)
+        fn = getattr(lib(), "lp_init_adj" + sfx)
+        check(fn(self._h, _ptr(pi, ctypes.c_int32), pi.size, _ptr(pf, ct), pf.size))
         self.has_adj = True
 
     def fwd(self, R_ptr, f_ptr, S0, stream):

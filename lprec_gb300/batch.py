@@ -13,9 +13,22 @@ measured slower: the large groups already fill the GPU and the branches only
 compete for L2).  The graph records an event when each group finishes, which
 gives per-request latencies measured from the start of the launch.
 """
+import time
+
 import torch
 
 from .lpTransform import lpTransform
+
+
+def wait_event(ev, timeout_s, poll_s=0.001, clock=time.monotonic, sleep=time.sleep):
+    """Host-side watchdog: poll `ev.query()` until it reports completion or `timeout_s`
+    seconds pass; raise TimeoutError in the second case (the GPU work is not cancelled,
+    the caller learns of the stall without blocking in a synchronize)."""
+    deadline = clock() + timeout_s
+    while not ev.query():
+        if clock() >= deadline:
+            raise TimeoutError("graph launch not finished after %.3f s" % timeout_s)
+        sleep(poll_s)
 
 
 class UnevenBatch:
@@ -91,10 +104,20 @@ class UnevenBatch:
                     ev.record(main)
         self._main = main
 
-    def run(self):
+    def run(self, timeout_s=None):
+        """One graph launch; with timeout_s, wait for it (host-side watchdog, see wait())."""
         if self.graph is None:
             self.capture()
         self.graph.replay()
+        if timeout_s is not None:
+            self.wait(timeout_s)
+
+    def wait(self, timeout_s):
+        """Wait for the last launch without blocking in cudaDeviceSynchronize; raises
+        TimeoutError when it has not finished within timeout_s seconds."""
+        ev = torch.cuda.Event()
+        ev.record(self._main)
+        wait_event(ev, timeout_s)
 
     def latencies_ms(self):
         """Per-request latency of the last run: start of the launch to its group's end."""

@@ -91,14 +91,15 @@ static cudaError_t dev_upload(DevBuf<T>& b, const std::vector<T>& v) {
   return cudaMemcpy(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
 }
 
-static inline float qnan() { return nanf(""); }
 
 }  // namespace
 
 struct FwdDev {
-  DevBuf<float2> c2lp[3];  // [Nth][Nrho]
-  DevBuf<float> thc;       // [Nproj]
-  DevBuf<float> rhoc;      // [Nproj][N]
+  int F = 16;              // fixed-point fraction bits of every coordinate table below
+  float fsc = 1.f / 65536.f;
+  DevBuf<int2> c2lp[3];    // [Nth][Nrho]
+  DevBuf<int> thc;         // [Nproj]
+  DevBuf<int> rhoc;        // [Nproj][N]
   DevBuf<int> rows[3];     // internal rows per span (multiples of os only)
   int nrows[3] = {0, 0, 0};
   DevBuf<float2> fz;       // Hermitian-extended kernel, tiled spectrum layout
@@ -121,11 +122,13 @@ struct FwdDev {
 static const int kTransposeCW = 8;
 
 struct AdjDev {
-  DevBuf<float> ta[3];     // [Nth]
-  DevBuf<float> sx[3];     // [Nth][Nrho]
+  int F = 16;              // fixed-point fraction bits of every coordinate table below
+  float fsc = 1.f / 65536.f;
+  DevBuf<int> ta[3];       // [Nth]
+  DevBuf<int> sx[3];       // [Nth][Nrho]
   DevBuf<int> woff[3];     // [Nth+1]
-  DevBuf<float4> wpt[3];
-  DevBuf<float2> c2lp[3];  // [N0][N0]
+  DevBuf<int4> wpt[3];
+  DevBuf<int2> c2lp[3];    // [N0][N0]
   int clo[3], chi[3];
   int lo2 = 0, hi2 = 0, W2 = 1;
   DevBuf<float2> fz;       // Hermitian-extended kernel, tiled spectrum layout
@@ -241,7 +244,8 @@ static void free_adj(AdjDev* a) {
 // lpRgpu.cu:28-34) to the rho-half / theta-full layout [Nrho/2+1][Nth].  Only
 // the Hermitian part of the kernel affects C2R output, so the kt = 0 and
 // kt = Nth/2 columns are symmetrised.
-static std::vector<float2> extend_kernel(const float* v, int Nrho, int Nth) {
+template <typename Real>
+static std::vector<float2> extend_kernel(const Real* v, int Nrho, int Nth) {
   const int nh = Nth / 2 + 1;
   const int Nk = Nrho / 2 + 1;
   auto at = [&](int kr, int kt) {
@@ -273,7 +277,7 @@ static std::vector<float2> extend_kernel(const float* v, int Nrho, int Nth) {
   return out;
 }
 
-static bool finite_coord(float v, float lim) { return isfinite(v) && fabsf(v) < lim; }
+static bool finite_coord(double v, double lim) { return std::isfinite(v) && std::fabs(v) < lim; }
 
 // A W x H float array with a gather texture (normalised, wrap) and a surface.
 static cudaError_t make_gather_array(int W, int H, std::vector<cudaArray_t>& arrs, cudaTextureObject_t* tex,
@@ -355,7 +359,8 @@ static std::vector<float2> twiddles(int L) {
 // h[d] for |d| < N matters and a circular convolution of length 2N with the
 // folded kernel gives the same result.  Returns its spectrum divided by 2N
 // (real: the filter is symmetric), or an empty vector if it is not symmetric.
-static std::vector<float> fbp_kernel_2n(const float* filt, int N) {
+template <typename Real>
+static std::vector<float> fbp_kernel_2n(const Real* filt, int N) {
   using lpgb_host::cd;
   const int M = 4 * N, L2 = 2 * N;
   std::vector<cd> H(M), tmp(M);
@@ -376,7 +381,22 @@ static std::vector<float> fbp_kernel_2n(const float* filt, int N) {
 }
 
 // taps of one axis for coordinate t: first index and count
-static inline int first_tap(float t, int cubic) { return (int)floorf(t) - (cubic ? 1 : 0); }
+// Fixed-point coordinates (value = v * 2^-F): F is the largest number of fraction
+// bits that keeps (max |coordinate| + 2) * 2^F below 2^30, so sums of a
+// coordinate and a table offset stay inside int32.
+static int fixed_bits(double maxabs) {
+  int F = 0;
+  while (F < 24 && std::ldexp(maxabs + 2.0, F + 1) < 1073741824.0) ++F;
+  return F;
+}
+static inline int to_fixed(double x, int F) { return std::isnan(x) ? LP_FX_NONE : (int)std::llrint(std::ldexp(x, F)); }
+static std::vector<int> to_fixed(const std::vector<double>& v, int F) {
+  std::vector<int> out(v.size());
+  for (size_t i = 0; i < v.size(); ++i) out[i] = to_fixed(v[i], F);
+  return out;
+}
+// first interpolation tap of a fixed-point coordinate (the kernels' v >> F)
+static inline int first_tap(int v, int F, int cubic) { return (v >> F) - (cubic ? 1 : 0); }
 
 static cudaEvent_t take_event(lp_handle* h) {
   if (!h->evpool.empty()) {
@@ -505,7 +525,10 @@ int lp_create(const float* glpars, int64_t n, int device, lp_handle** out) {
   return LP_OK;
 }
 
-int lp_init_fwd(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, int64_t nf) {
+}  // extern "C"
+
+template <typename Real>
+static int init_fwd_impl(lp_handle* h, const int32_t* pi, int64_t ni, const Real* pf, int64_t nf) {
   if (!h || !pi || !pf) return set_err(LP_ERR_ARG, "lp_init_fwd: null pointer");
   const int N = h->N, Nth = h->Nth, Nrho = h->Nrho, Nproj = h->Nproj;
   // layout: Npids[3], pids[k]..., Ncids, cids  |  lp2C1[3], lp2C2[3], p2lp1[3], p2lp2[3], fZ
@@ -531,28 +554,41 @@ int lp_init_fwd(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
   const int64_t nh = Nth / 2 + 1;
   if (nf != 6 * ncids + 2 * sum_p + 2 * (int64_t)Nrho * nh)
     return set_err(LP_ERR_ARG, "lp_init_fwd: parsf size %lld inconsistent", (long long)nf);
-  const float* lp2C1 = pf;
-  const float* lp2C2 = pf + 3 * ncids;
-  const float* p2lp1 = pf + 6 * ncids;
-  const float* p2lp2 = p2lp1 + sum_p;
-  const float* fzv = p2lp2 + sum_p;
+  const Real* lp2C1 = pf;
+  const Real* lp2C2 = pf + 3 * ncids;
+  const Real* p2lp1 = pf + 6 * ncids;
+  const Real* p2lp2 = p2lp1 + sum_p;
+  const Real* fzv = p2lp2 + sum_p;
 
   FwdDev* F = new FwdDev();
-  const float lim = 8.0f * (float)Nrho;
+  const double lim = 8.0 * Nrho;
+  // fixed-point format from the largest coordinate
+  double maxabs = 0.0;
+  for (int64_t i = 0; i < 6 * ncids + 2 * sum_p; ++i) {
+    const double v = (double)pf[i];
+    if (!finite_coord(v, lim)) {
+      free_fwd(F);
+      return set_err(LP_ERR_ARG, "lp_init_fwd: coordinate %lld not finite or out of range", (long long)i);
+    }
+    maxabs = std::max(maxabs, std::fabs(v));
+  }
+  F->F = fixed_bits(maxabs);
+  F->fsc = (float)std::ldexp(1.0, -F->F);
+  const int FB = F->F;
   std::vector<int2> ival(Nth, make_int2(1, 0));
   // dense column-major Cartesian coordinates of every log-polar point
-  std::vector<float2> c2lp((size_t)Nth * Nrho);
+  std::vector<int2> c2lp((size_t)Nth * Nrho);
   for (int k = 0; k < 3; ++k) {
-    std::fill(c2lp.begin(), c2lp.end(), make_float2(qnan(), qnan()));
+    std::fill(c2lp.begin(), c2lp.end(), make_int2(LP_FX_NONE, LP_FX_NONE));
     for (int64_t i = 0; i < ncids; ++i) {
       const int idx = cids[i];
-      const float x = lp2C1[k * ncids + i], y = lp2C2[k * ncids + i];
-      if (idx < 0 || idx >= Nrho * Nth || !finite_coord(x, lim) || !finite_coord(y, lim)) {
+      if (idx < 0 || idx >= Nrho * Nth) {
         free_fwd(F);
-        return set_err(LP_ERR_ARG, "lp_init_fwd: bad cids/lp2C entry %lld", (long long)i);
+        return set_err(LP_ERR_ARG, "lp_init_fwd: bad cids entry %lld", (long long)i);
       }
       const int r = idx / Nth, t = idx % Nth;
-      c2lp[(size_t)t * Nrho + r] = make_float2(x, y);
+      c2lp[(size_t)t * Nrho + r] = make_int2(to_fixed((double)lp2C1[k * ncids + i], FB),
+                                             to_fixed((double)lp2C2[k * ncids + i], FB));
       int2& iv = ival[t];
       if (iv.y < iv.x) iv = make_int2(r, r);
       else iv = make_int2(std::min(iv.x, r), std::max(iv.y, r));
@@ -573,8 +609,8 @@ int lp_init_fwd(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
     }
   }
   // polar points: every span must own whole sinogram rows with one theta coordinate
-  std::vector<float> thc(Nproj, qnan());
-  std::vector<float> rhoc((size_t)Nproj * N, 0.f);
+  std::vector<int> thc(Nproj, LP_FX_NONE);
+  std::vector<int> rhoc((size_t)Nproj * N, 0);
   std::vector<int> owner(Nproj, -1);
   std::vector<int> cnt(Nproj, 0);
   int64_t off = 0;
@@ -583,8 +619,8 @@ int lp_init_fwd(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
   for (int k = 0; k < 3; ++k) {
     for (int64_t i = 0; i < npids[k]; ++i) {
       const int idx = pids[k][i];
-      const float t = p2lp1[off + i], rr = p2lp2[off + i];
-      if (idx < 0 || idx >= Nproj * N || !finite_coord(t, lim) || !finite_coord(rr, lim)) {
+      const int t = to_fixed((double)p2lp1[off + i], FB), rr = to_fixed((double)p2lp2[off + i], FB);
+      if (idx < 0 || idx >= Nproj * N) {
         free_fwd(F);
         return set_err(LP_ERR_ARG, "lp_init_fwd: bad pids/p2lp entry");
       }
@@ -609,7 +645,7 @@ int lp_init_fwd(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
       return set_err(LP_ERR_UNSUPPORTED, "lp_init_fwd: sinogram row %d not covered exactly once", row);
     }
     if (row % h->os == 0) rows[owner[row]].push_back(row);
-    const int c = first_tap(thc[row], h->cubic);
+    const int c = first_tap(thc[row], FB, h->cubic);
     const int n = h->cubic ? 4 : 2;
     if (c < 0 || c + n - 1 >= Nth) wraps = true;
     lo = std::min(lo, c);
@@ -631,7 +667,7 @@ int lp_init_fwd(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
         const int c0 = lo + b * kTransposeCW, c1 = std::min(c0 + kTransposeCW, hi + 1);
         int first = -1, last = -1;
         for (int i = 0; i < (int)rows[k].size(); ++i) {
-          const int c = first_tap(thc[rows[k][i]], h->cubic);
+          const int c = first_tap(thc[rows[k][i]], FB, h->cubic);
           bool touch = false;
           for (int j = 0; j < ntap && !touch; ++j) {
             int cc = (c + j) % Nth;
@@ -671,7 +707,20 @@ int lp_init_fwd(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
   return LP_OK;
 }
 
-int lp_init_adj(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, int64_t nf) {
+extern "C" {
+
+int lp_init_fwd(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, int64_t nf) {
+  return init_fwd_impl(h, pi, ni, pf, nf);
+}
+
+int lp_init_fwd_f64(lp_handle* h, const int32_t* pi, int64_t ni, const double* pf, int64_t nf) {
+  return init_fwd_impl(h, pi, ni, pf, nf);
+}
+
+}  // extern "C"
+
+template <typename Real>
+static int init_adj_impl(lp_handle* h, const int32_t* pi, int64_t ni, const Real* pf, int64_t nf) {
   if (!h || !pi || !pf) return set_err(LP_ERR_ARG, "lp_init_adj: null pointer");
   const int N = h->N, N0 = h->N0, Nth = h->Nth, Nrho = h->Nrho, Nproj = h->Nproj;
   // layout: Ncids, Nlpids, Nwids, cids, lpids, wids, flag |
@@ -689,35 +738,44 @@ int lp_init_adj(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
   const int64_t nbase = 6 * nc + 6 * nl + 6 * nw + 2 * (int64_t)Nrho * nh;
   if (nf != nbase + (flag == 1 ? 4 * (int64_t)N : 0))
     return set_err(LP_ERR_ARG, "lp_init_adj: parsf size %lld inconsistent", (long long)nf);
-  const float* C2lp1 = pf;
-  const float* C2lp2 = C2lp1 + 3 * nc;
-  const float* lp2p1 = C2lp2 + 3 * nc;
-  const float* lp2p2 = lp2p1 + 3 * nl;
-  const float* lp2p1w = lp2p2 + 3 * nl;
-  const float* lp2p2w = lp2p1w + 3 * nw;
-  const float* fzv = lp2p2w + 3 * nw;
-  const float* filt = fzv + 2 * (size_t)Nrho * nh;
-  const float lim = 8.0f * (float)std::max(Nrho, Nproj);
+  const Real* C2lp1 = pf;
+  const Real* C2lp2 = C2lp1 + 3 * nc;
+  const Real* lp2p1 = C2lp2 + 3 * nc;
+  const Real* lp2p2 = lp2p1 + 3 * nl;
+  const Real* lp2p1w = lp2p2 + 3 * nl;
+  const Real* lp2p2w = lp2p1w + 3 * nw;
+  const Real* fzv = lp2p2w + 3 * nw;
+  const Real* filt = fzv + 2 * (size_t)Nrho * nh;
+  const double lim = 8.0 * std::max(Nrho, Nproj);
 
   AdjDev* A = new AdjDev();
   auto fail = [&](int code, const char* msg) {
     free_adj(A);
     return set_err(code, "lp_init_adj: %s", msg);
   };
+  // fixed-point format from the largest coordinate
+  double maxabs = 0.0;
+  for (int64_t i = 0; i < 6 * (nc + nl + nw); ++i) {
+    const double v = (double)pf[i];
+    if (!finite_coord(v, lim)) return fail(LP_ERR_ARG, "coordinate not finite or out of range");
+    maxabs = std::max(maxabs, std::fabs(v));
+  }
+  A->F = fixed_bits(maxabs);
+  A->fsc = (float)std::ldexp(1.0, -A->F);
+  const int FB = A->F;
   DeviceGuard g(h->device);
   const int off = N / 2 - N0 / 2;
   int lo2 = Nth, hi2 = -1;
   bool wraps = false;
   for (int k = 0; k < 3; ++k) {
-    std::vector<float> ta(Nth, qnan());
-    std::vector<float> sx((size_t)Nth * Nrho, qnan());
+    std::vector<int> ta(Nth, LP_FX_NONE);
+    std::vector<int> sx((size_t)Nth * Nrho, LP_FX_NONE);
     for (int64_t i = 0; i < nl; ++i) {
       const int idx = lpids[i];
-      const float s = lp2p2[k * nl + i], a = lp2p1[k * nl + i];
-      if (idx < 0 || idx >= Nrho * Nth || !finite_coord(s, lim) || !finite_coord(a, lim))
-        return fail(LP_ERR_ARG, "bad lpids/lp2p entry");
+      const int s = to_fixed((double)lp2p2[k * nl + i], FB), a = to_fixed((double)lp2p1[k * nl + i], FB);
+      if (idx < 0 || idx >= Nrho * Nth) return fail(LP_ERR_ARG, "bad lpids entry");
       const int r = idx / Nth, t = idx % Nth;
-      if (isnan(ta[t])) ta[t] = a;
+      if (ta[t] == LP_FX_NONE) ta[t] = a;
       else if (ta[t] != a) return fail(LP_ERR_UNSUPPORTED, "log-polar column with more than one angle coordinate");
       sx[(size_t)t * Nrho + r] = s;
     }
@@ -726,21 +784,19 @@ int lp_init_adj(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
     for (int64_t i = 0; i < nw; ++i) {
       const int idx = wids[i];
       if (idx < 0 || idx >= Nrho * Nth) return fail(LP_ERR_ARG, "bad wids entry");
-      if (!finite_coord(lp2p2w[k * nw + i], lim) || !finite_coord(lp2p1w[k * nw + i], lim))
-        return fail(LP_ERR_ARG, "bad wrap coordinate");
       woff[idx % Nth + 1]++;
     }
     for (int t = 0; t < Nth; ++t) woff[t + 1] += woff[t];
-    std::vector<float4> wpt(std::max<int64_t>(nw, 1));
+    std::vector<int4> wpt(std::max<int64_t>(nw, 1), make_int4(0, 0, 0, 0));
     std::vector<int> fillp(woff.begin(), woff.end() - 1);
     for (int64_t i = 0; i < nw; ++i) {
       const int idx = wids[i];
       const int r = idx / Nth, t = idx % Nth;
-      wpt[fillp[t]++] = make_float4((float)r, lp2p2w[k * nw + i], lp2p1w[k * nw + i], 0.f);
+      wpt[fillp[t]++] = make_int4(r, to_fixed((double)lp2p2w[k * nw + i], FB), to_fixed((double)lp2p1w[k * nw + i], FB), 0);
     }
     int clo = Nth, chi = -1;
     for (int t = 0; t < Nth; ++t) {
-      if (!isnan(ta[t]) || woff[t + 1] > woff[t]) {
+      if (ta[t] != LP_FX_NONE || woff[t + 1] > woff[t]) {
         clo = std::min(clo, t);
         chi = std::max(chi, t);
       }
@@ -748,16 +804,15 @@ int lp_init_adj(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
     A->clo[k] = clo;
     A->chi[k] = chi;
     // Cartesian pixels of the output window
-    std::vector<float2> c2((size_t)N0 * N0, make_float2(qnan(), qnan()));
+    std::vector<int2> c2((size_t)N0 * N0, make_int2(LP_FX_NONE, LP_FX_NONE));
     for (int64_t i = 0; i < nc; ++i) {
       const int idx = cids[i];
-      const float tt = C2lp1[k * nc + i], tr = C2lp2[k * nc + i];
-      if (idx < 0 || idx >= N * N || !finite_coord(tt, lim) || !finite_coord(tr, lim))
-        return fail(LP_ERR_ARG, "bad cids/C2lp entry");
+      const int tt = to_fixed((double)C2lp1[k * nc + i], FB), tr = to_fixed((double)C2lp2[k * nc + i], FB);
+      if (idx < 0 || idx >= N * N) return fail(LP_ERR_ARG, "bad cids entry");
       const int Y = idx / N - off, X = idx % N - off;
       if (Y < 0 || Y >= N0 || X < 0 || X >= N0) continue;
-      c2[(size_t)Y * N0 + X] = make_float2(tt, tr);
-      const int c = first_tap(tt, h->cubic);
+      c2[(size_t)Y * N0 + X] = make_int2(tt, tr);
+      const int c = first_tap(tt, FB, h->cubic);
       const int n = h->cubic ? 4 : 2;
       if (c < 0 || c + n - 1 >= Nth) wraps = true;
       lo2 = std::min(lo2, c);
@@ -812,6 +867,16 @@ int lp_init_adj(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, in
   free_adj(h->adj);
   h->adj = A;
   return LP_OK;
+}
+
+extern "C" {
+
+int lp_init_adj(lp_handle* h, const int32_t* pi, int64_t ni, const float* pf, int64_t nf) {
+  return init_adj_impl(h, pi, ni, pf, nf);
+}
+
+int lp_init_adj_f64(lp_handle* h, const int32_t* pi, int64_t ni, const double* pf, int64_t nf) {
+  return init_adj_impl(h, pi, ni, pf, nf);
 }
 
 int lp_destroy(lp_handle* h) {
@@ -933,13 +998,13 @@ static int fwd_slices(lp_handle* h, float* R, const float* f, int s0, int n, cud
   }
   for (int k = 0; k < 3; ++k) {
     FwdC2LPArgs a1{fbuf, spec, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, h->cubic,
-                   h->plan_rho, tx, F->ival.p, F->dlo, F->dhi};
+                   h->plan_rho, tx, F->ival.p, F->dlo, F->dhi, F->F, F->fsc};
     CUDA_TRY(launch(h, K_FWD_C2LP, st, [&] { return launch_fwd_c2lp(a1, n, st); }));
     ThetaConvArgs a2{spec, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), F->dlo, F->dhi,
                      F->lo & ~1, std::min(F->hi | 1, h->Nth - 1), 0, h->plan_th, h->fwd_tblock};
     CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, n, st); }));
     FwdLP2PolarArgs a3{spec, R, F->thc.p, F->rhoc.p, F->rows[k].p, F->nrows[k], h->N, h->N0, h->Nth,
-                       h->Nrho, h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho};
+                       h->Nrho, h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho, F->F, F->fsc};
     CUDA_TRY(launch(h, K_FWD_LP2POLAR, st, [&] { return launch_fwd_lp2polar(a3, n, st); }));
   }
   return LP_OK;
@@ -970,7 +1035,7 @@ static int adj_slices(lp_handle* h, float* f, const float* R, int s0, int n, cud
       continue;
     }
     AdjPolar2LPArgs a1{rbuf, spec, A->ta[k].p, A->sx[k].p, A->woff[k].p, A->wpt[k].p, h->N, h->Nth,
-                       h->Nrho, h->Nk, h->Nproj, h->cubic, A->clo[k], A->chi[k], h->plan_rho};
+                       h->Nrho, h->Nk, h->Nproj, h->cubic, A->clo[k], A->chi[k], h->plan_rho, A->F, A->fsc};
     CUDA_TRY(launch(h, K_ADJ_POLAR2LP, st, [&] { return launch_adj_polar2lp(a1, n, st); }));
     ThetaConvArgs a2{spec, A->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), A->clo[k],
                      A->chi[k], A->lo2, A->hi2, 0, h->plan_th, h->adj_tblock};
@@ -983,7 +1048,7 @@ static int adj_slices(lp_handle* h, float* f, const float* R, int s0, int n, cud
   AdjLP2CartArgs a4{G[0], G[1], G[2], A->c2lp[0].p, A->c2lp[1].p, A->c2lp[2].p, f,
                     h->N0, h->Nth, h->Nrho, A->lo2, A->W2, h->cubic, h->N0 * h->N0,
                     tex ? A->tex[0].p + s0 : nullptr, tex ? A->tex[1].p + s0 : nullptr,
-                    tex ? A->tex[2].p + s0 : nullptr};
+                    tex ? A->tex[2].p + s0 : nullptr, A->F, A->fsc};
   CUDA_TRY(launch(h, K_ADJ_LP2CART, st, [&] { return launch_adj_lp2cart(a4, n, st); }));
   return LP_OK;
 }
@@ -1016,14 +1081,15 @@ int lp_fwd_transpose(lp_handle* h, float* f, const float* R, int S0, void* strea
   for (int k = 0; k < 3; ++k) {
     CUDA_TRY(cudaMemsetAsync(h->spec.p, 0, (size_t)S0 * spec_slice(h->Nk, h->Nth) * sizeof(float2), st));
     FwdTPolarArgs a1{R, h->spec.p, F->thc.p, F->rhoc.p, F->rows[k].p, F->blk[k].p, h->N, h->N0, h->Nth, h->Nrho,
-                     h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, F->lo, kTransposeCW, h->plan_rho};
+                     h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, F->lo, kTransposeCW, h->plan_rho,
+                     F->F, F->fsc};
     CUDA_TRY(launch(h, K_FWDT_POLAR, st, [&] { return launch_fwdT_polar(a1, S0, F->nblk[k], st); }));
     ThetaConvArgs a2{h->spec.p, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), F->lo, F->hi,
                      F->dlo, F->dhi, 1, h->plan_th, h->fwd_tblock};
     if (F->dhi >= F->dlo)
       CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
     FwdTCartArgs a3{h->spec.p, acc, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, F->dlo, F->dhi,
-                    h->cubic, h->plan_rho};
+                    h->cubic, h->plan_rho, F->F, F->fsc};
     CUDA_TRY(launch(h, K_FWDT_CART, st, [&] { return launch_fwdT_cart(a3, S0, st); }));
   }
   if (h->cubic) {
@@ -1239,13 +1305,13 @@ extern "C" int lp_fwd_noalloc(lp_handle* h, float* R, const float* f, int S0, vo
   }
   for (int k = 0; k < 3; ++k) {
     FwdC2LPArgs a1{fbuf, spec, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, h->cubic, h->plan_rho,
-                   nullptr, F->ival.p, F->dlo, F->dhi};
+                   nullptr, F->ival.p, F->dlo, F->dhi, F->F, F->fsc};
     CUDA_TRY(launch(h, K_FWD_C2LP, st, [&] { return launch_fwd_c2lp(a1, S0, st); }));
     ThetaConvArgs a2{spec, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), F->dlo, F->dhi,
                      F->lo & ~1, std::min(F->hi | 1, h->Nth - 1), 0, h->plan_th, h->fwd_tblock};
     CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
     FwdLP2PolarArgs a3{spec, R, F->thc.p, F->rhoc.p, F->rows[k].p, F->nrows[k], h->N, h->N0, h->Nth,
-                       h->Nrho, h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho};
+                       h->Nrho, h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho, F->F, F->fsc};
     CUDA_TRY(launch(h, K_FWD_LP2POLAR, st, [&] { return launch_fwd_lp2polar(a3, S0, st); }));
   }
   return LP_OK;

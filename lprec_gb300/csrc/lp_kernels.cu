@@ -31,6 +31,17 @@ __device__ __forceinline__ int wrapi(int i, int n) {
   return i < 0 ? i + n : i;
 }
 
+// ---------------------------------------------------------------------------
+// Interpolation coordinates are stored as 32-bit fixed point: value = v * 2^-F
+// with F chosen per handle from the largest coordinate (F = 17 at N = 2048:
+// steps of 7.6e-6 texel, where float32 near 4096 steps by 4.9e-4).  The
+// integer tap position is v >> F (an arithmetic shift, i.e. floor) and the
+// fraction (v & (2^F - 1)) * 2^-F is exact in float32.  LP_FX_NONE marks a
+// table entry without a point.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int fx_int(int v, int F) { return v >> F; }
+__device__ __forceinline__ float fx_frac(int v, int F, float fsc) { return (float)(v & ((1 << F) - 1)) * fsc; }
+
 // cubic B-spline weights for taps i-1, i, i+1, i+2 at fraction f
 __device__ __forceinline__ void bspline_w(float f, float* w) {
   const float one = 1.0f - f;
@@ -44,11 +55,8 @@ __device__ __forceinline__ void bspline_w(float f, float* w) {
 
 // 2-D interpolation of a row-major image (W columns, H rows) at index position
 // (x, y) with wrap addressing.
-__device__ __forceinline__ float interp2d(const float* __restrict__ img, int W, int H, float x, float y,
-                                          int cubic) {
-  const float fx = floorf(x), fy = floorf(y);
-  const int ix = (int)fx, iy = (int)fy;
-  const float ax = x - fx, ay = y - fy;
+__device__ __forceinline__ float interp2d_split(const float* __restrict__ img, int W, int H, int ix, float ax,
+                                                int iy, float ay, int cubic) {
   if (cubic) {
     float wx[4], wy[4];
     bspline_w(ax, wx);
@@ -78,6 +86,13 @@ __device__ __forceinline__ float interp2d(const float* __restrict__ img, int W, 
          ay * ((1.f - ax) * __ldg(r1 + x0) + ax * __ldg(r1 + x1));
 }
 
+// 2-D interpolation at fixed-point index position (x, y)
+__device__ __forceinline__ float interp2d_fx(const float* __restrict__ img, int W, int H, int vx, int vy, int F,
+                                             float fsc, int cubic) {
+  return interp2d_split(img, W, H, fx_int(vx, F), fx_frac(vx, F, fsc), fx_int(vy, F), fx_frac(vy, F, fsc), cubic);
+}
+
+
 // Cubic B-spline sample of a 2-D texture (N x N texels, normalised
 // coordinates, wrap addressing) at index position (x, y) from four 2x2
 // texel gathers.  A gather at integer texel coordinate (i, j) returns the
@@ -86,12 +101,12 @@ __device__ __forceinline__ float interp2d(const float* __restrict__ img, int W, 
 // margin of the integer position makes the quad selection insensitive to
 // coordinate rounding.  Gather component order: w (i-1, j-1), z (i, j-1),
 // x (i-1, j), y (i, j).
-__device__ __forceinline__ float interp_tex_cubic(cudaTextureObject_t tx, float invW, float invH, float x,
-                                                 float y) {
-  const float fx = floorf(x), fy = floorf(y);
+__device__ __forceinline__ float interp_tex_cubic_split(cudaTextureObject_t tx, float invW, float invH, int ix,
+                                                       float ax, int iy, float ay) {
   float wx[4], wy[4];
-  bspline_w(x - fx, wx);
-  bspline_w(y - fy, wy);
+  bspline_w(ax, wx);
+  bspline_w(ay, wy);
+  const float fx = (float)ix, fy = (float)iy;
   const float u0 = fx * invW, u1 = (fx + 2.0f) * invW;
   const float v0 = fy * invH, v1 = (fy + 2.0f) * invH;
   const float4 q00 = tex2Dgather<float4>(tx, u0, v0, 0);
@@ -105,12 +120,16 @@ __device__ __forceinline__ float interp_tex_cubic(cudaTextureObject_t tx, float 
   return wy[0] * r0 + wy[1] * r1 + wy[2] * r2 + wy[3] * r3;
 }
 
+// the same at fixed-point texel coordinates (x, y)
+__device__ __forceinline__ float interp_tex_cubic_fx(cudaTextureObject_t tx, float invW, float invH, int vx, int vy,
+                                                    int F, float fsc) {
+  return interp_tex_cubic_split(tx, invW, invH, fx_int(vx, F), fx_frac(vx, F, fsc), fx_int(vy, F),
+                                fx_frac(vy, F, fsc));
+}
+
 // 1-D interpolation along a shared-memory line of length L (wrap).
 template <typename Get>
-__device__ __forceinline__ float interp1d(Get get, int L, float x, int cubic) {
-  const float fx = floorf(x);
-  const int ix = (int)fx;
-  const float ax = x - fx;
+__device__ __forceinline__ float interp1d_split(Get get, int L, int ix, float ax, int cubic) {
   if (cubic) {
     float w[4];
     bspline_w(ax, w);
@@ -127,16 +146,22 @@ __device__ __forceinline__ float interp1d(Get get, int L, float x, int cubic) {
   return (1.f - ax) * get(wrapi(ix, L)) + ax * get(wrapi(ix + 1, L));
 }
 
-// Interpolation weights along one axis at coordinate t: taps start at *first.
-__device__ __forceinline__ int axis_weights(float t, int cubic, float* w) {
-  const float ft = floorf(t);
-  const int it = (int)ft;
+// 1-D interpolation at fixed-point position v
+template <typename Get>
+__device__ __forceinline__ float interp1d_fx(Get get, int L, int v, int F, float fsc, int cubic) {
+  return interp1d_split(get, L, fx_int(v, F), fx_frac(v, F, fsc), cubic);
+}
+
+// Interpolation weights along one axis at fixed-point coordinate v: returns the first tap.
+__device__ __forceinline__ int axis_weights_fx(int v, int F, float fsc, int cubic, float* w) {
+  const int it = fx_int(v, F);
+  const float a = fx_frac(v, F, fsc);
   if (cubic) {
-    bspline_w(t - ft, w);
+    bspline_w(a, w);
     return it - 1;
   }
-  w[0] = 1.f - (t - ft);
-  w[1] = t - ft;
+  w[0] = 1.f - a;
+  w[1] = a;
   w[2] = 0.f;
   w[3] = 0.f;
   return it;
@@ -369,21 +394,23 @@ __global__ void __launch_bounds__(256, 2) k_fwd_c2lp(FwdC2LPArgs a) {
   const int th = 2 * blockIdx.y;
   const int thb = th + 1 < a.Nth ? th + 1 : -1;
   const float* img = a.fbuf + (size_t)s * a.N * a.N;
-  const float2* ca = a.c2lp + (size_t)th * a.Nrho;
-  const float2* cb = a.c2lp + (size_t)max(thb, 0) * a.Nrho;
+  const int2* ca = a.c2lp + (size_t)th * a.Nrho;
+  const int2* cb = a.c2lp + (size_t)max(thb, 0) * a.Nrho;
   const bool use_tex = a.tex != nullptr;
   const cudaTextureObject_t tx = use_tex ? a.tex[s] : 0;
   const float invN = 1.0f / (float)a.N;
   for (int r = threadIdx.x; r < a.Nrho; r += blockDim.x) {
     const float e = __ldg(a.erho + r);
-    const float2 pa = __ldg(ca + r);
+    const int2 pa = __ldg(ca + r);
     float va = 0.f, vb = 0.f;
-    if (!isnan(pa.x))
-      va = e * (use_tex ? interp_tex_cubic(tx, invN, invN, pa.x, pa.y) : interp2d(img, a.N, a.N, pa.x, pa.y, a.cubic));
+    if (pa.x != LP_FX_NONE)
+      va = e * (use_tex ? interp_tex_cubic_fx(tx, invN, invN, pa.x, pa.y, a.F, a.fsc)
+                        : interp2d_fx(img, a.N, a.N, pa.x, pa.y, a.F, a.fsc, a.cubic));
     if (thb >= 0) {
-      const float2 pb = __ldg(cb + r);
-      if (!isnan(pb.x))
-        vb = e * (use_tex ? interp_tex_cubic(tx, invN, invN, pb.x, pb.y) : interp2d(img, a.N, a.N, pb.x, pb.y, a.cubic));
+      const int2 pb = __ldg(cb + r);
+      if (pb.x != LP_FX_NONE)
+        vb = e * (use_tex ? interp_tex_cubic_fx(tx, invN, invN, pb.x, pb.y, a.F, a.fsc)
+                          : interp2d_fx(img, a.N, a.N, pb.x, pb.y, a.F, a.fsc, a.cubic));
     }
     A.set(r, make_float2(va, vb));
   }
@@ -464,10 +491,10 @@ __global__ void __launch_bounds__(256, 2) k_fwd_lp2polar(FwdLP2PolarArgs a) {
   const int r0 = a.rows[i0];
   const int r1 = (i0 + 1 < a.nrows) ? a.rows[i0 + 1] : -1;
   float w0[4], w1[4];
-  const int c0 = axis_weights(__ldg(a.thc + r0), a.cubic, w0);
+  const int c0 = axis_weights_fx(__ldg(a.thc + r0), a.F, a.fsc, a.cubic, w0);
   int c1 = 0;
   if (r1 >= 0) {
-    c1 = axis_weights(__ldg(a.thc + r1), a.cubic, w1);
+    c1 = axis_weights_fx(__ldg(a.thc + r1), a.F, a.fsc, a.cubic, w1);
   } else {
     w1[0] = w1[1] = w1[2] = w1[3] = 0.f;
   }
@@ -500,13 +527,13 @@ __global__ void __launch_bounds__(256, 2) k_fwd_lp2polar(FwdLP2PolarArgs a) {
     const int xo = x - a.cor_off;
     if (xo < 0 || xo >= a.N0) continue;
     if (r0 % a.os == 0) {
-      const float t = __ldg(a.rhoc + (size_t)r0 * a.N + x);
-      const float v = interp1d([&](int i) { return zr.re[fpad(i)]; }, Nrho, t, a.cubic);
+      const int t = __ldg(a.rhoc + (size_t)r0 * a.N + x);
+      const float v = interp1d_fx([&](int i) { return zr.re[fpad(i)]; }, Nrho, t, a.F, a.fsc, a.cubic);
       a.Rout[((size_t)s * a.Nproj0 + r0 / a.os) * a.N0 + xo] = v;
     }
     if (r1 >= 0 && r1 % a.os == 0) {
-      const float t = __ldg(a.rhoc + (size_t)r1 * a.N + x);
-      const float v = interp1d([&](int i) { return zr.im[fpad(i)]; }, Nrho, t, a.cubic);
+      const int t = __ldg(a.rhoc + (size_t)r1 * a.N + x);
+      const float v = interp1d_fx([&](int i) { return zr.im[fpad(i)]; }, Nrho, t, a.F, a.fsc, a.cubic);
       a.Rout[((size_t)s * a.Nproj0 + r1 / a.os) * a.N0 + xo] = v;
     }
   }
@@ -587,15 +614,15 @@ __global__ void __launch_bounds__(256, 2) k_adj_polar2lp(AdjPolar2LPArgs a) {
   const int th0 = a.clo + 2 * blockIdx.y;
   const int th1 = th0 + 1 <= a.chi ? th0 + 1 : -1;
   const float* img = a.rbuf + (size_t)s * a.Nproj * a.N;
-  const float ta0 = __ldg(a.ta + th0);
-  const float ta1 = th1 >= 0 ? __ldg(a.ta + th1) : __int_as_float(0x7fc00000);
+  const int ta0 = __ldg(a.ta + th0);
+  const int ta1 = th1 >= 0 ? __ldg(a.ta + th1) : LP_FX_NONE;
   float w0[4], w1[4];
   int rw0[4], rw1[4];
-  const bool has0 = !isnan(ta0), has1 = !isnan(ta1);
+  const bool has0 = ta0 != LP_FX_NONE, has1 = ta1 != LP_FX_NONE;
   const int ntap = a.cubic ? 4 : 2;
   {
-    const int c0 = has0 ? axis_weights(ta0, a.cubic, w0) : 0;
-    const int c1 = has1 ? axis_weights(ta1, a.cubic, w1) : 0;
+    const int c0 = has0 ? axis_weights_fx(ta0, a.F, a.fsc, a.cubic, w0) : 0;
+    const int c1 = has1 ? axis_weights_fx(ta1, a.F, a.fsc, a.cubic, w1) : 0;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       rw0[j] = wrapi(c0 + j, a.Nproj);
@@ -612,15 +639,15 @@ __global__ void __launch_bounds__(256, 2) k_adj_polar2lp(AdjPolar2LPArgs a) {
     prof[a.N + x] = p1;
   }
   __syncthreads();
-  const float* sx0 = a.sx + (size_t)th0 * a.Nrho;
-  const float* sx1 = a.sx + (size_t)max(th1, 0) * a.Nrho;
+  const int* sx0 = a.sx + (size_t)th0 * a.Nrho;
+  const int* sx1 = a.sx + (size_t)max(th1, 0) * a.Nrho;
   for (int r = threadIdx.x; r < a.Nrho; r += blockDim.x) {
     float v0 = 0.f, v1 = 0.f;
-    const float x0 = __ldg(sx0 + r);
-    if (!isnan(x0)) v0 = interp1d([&](int i) { return prof[i]; }, a.N, x0, a.cubic);
+    const int x0 = __ldg(sx0 + r);
+    if (x0 != LP_FX_NONE) v0 = interp1d_fx([&](int i) { return prof[i]; }, a.N, x0, a.F, a.fsc, a.cubic);
     if (th1 >= 0) {
-      const float x1 = __ldg(sx1 + r);
-      if (!isnan(x1)) v1 = interp1d([&](int i) { return prof[a.N + i]; }, a.N, x1, a.cubic);
+      const int x1 = __ldg(sx1 + r);
+      if (x1 != LP_FX_NONE) v1 = interp1d_fx([&](int i) { return prof[a.N + i]; }, a.N, x1, a.F, a.fsc, a.cubic);
     }
     A.set(r, make_float2(v0, v1));
   }
@@ -631,9 +658,9 @@ __global__ void __launch_bounds__(256, 2) k_adj_polar2lp(AdjPolar2LPArgs a) {
     if (th < 0) break;
     const int w_begin = __ldg(a.woff + th), w_end = __ldg(a.woff + th + 1);
     for (int w = w_begin + threadIdx.x; w < w_end; w += blockDim.x) {
-      const float4 p = __ldg(a.wpt + w);
-      const int r = (int)p.x;
-      const float v = interp2d(img, a.N, a.Nproj, p.y, p.z, a.cubic);
+      const int4 p = __ldg(a.wpt + w);
+      const int r = p.x;
+      const float v = interp2d_fx(img, a.N, a.Nproj, p.y, p.z, a.F, a.fsc, a.cubic);
       if (c == 0) A.re[fpad(r)] += v;
       else A.im[fpad(r)] += v;
     }
@@ -687,10 +714,10 @@ __global__ void __launch_bounds__(256, 2) k_adj_lpcols(AdjLPColsArgs a) {
 // copy3Dshifted :206).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float interp_cols(const float* __restrict__ G, int Nrho, int Nth, int lo2, int W2,
-                                             float2 t, int cubic) {
+                                             int2 t, int F, float fsc, int cubic) {
   float wt[4], wr[4];
-  const int ct = axis_weights(t.x, cubic, wt);
-  const int cr = axis_weights(t.y, cubic, wr);
+  const int ct = axis_weights_fx(t.x, F, fsc, cubic, wt);
+  const int cr = axis_weights_fx(t.y, F, fsc, cubic, wr);
   const int nt = cubic ? 4 : 2;
   int rr[4];
   const bool inner = (cr >= 0 && cr + 3 < Nrho);
@@ -717,30 +744,31 @@ __global__ void k_adj_lp2cart(AdjLP2CartArgs a) {
   if (p >= a.npix) return;
   const size_t gs = (size_t)s * a.W2 * a.Nrho;
   float acc = 0.f;
-  const float2 t0 = __ldg(a.c2lp0 + p);
+  const int2 t0 = __ldg(a.c2lp0 + p);
   if (a.tex0) {
     // texture x = rho (wrap over Nrho), y = theta - lo2 (taps stay inside the stored band).
     // Straight-line: the three spans' twelve gathers are in flight together; pixels
     // outside the disk sample (0, 0) and are discarded, warps entirely outside skip.
-    const bool ok = !isnan(t0.x);
+    const bool ok = t0.x != LP_FX_NONE;
     if (__any_sync(__activemask(), ok)) {
-      const float iw = 1.0f / (float)a.Nrho, ih = 1.0f / (float)a.W2, l2 = (float)a.lo2;
-      float2 t1 = __ldg(a.c2lp1 + p), t2 = __ldg(a.c2lp2 + p);
-      const float2 q0 = ok ? make_float2(t0.y, t0.x - l2) : make_float2(0.f, 0.f);
-      const float2 q1 = ok ? make_float2(t1.y, t1.x - l2) : make_float2(0.f, 0.f);
-      const float2 q2 = ok ? make_float2(t2.y, t2.x - l2) : make_float2(0.f, 0.f);
-      const float v = interp_tex_cubic(a.tex0[s], iw, ih, q0.x, q0.y) +
-                      interp_tex_cubic(a.tex1[s], iw, ih, q1.x, q1.y) +
-                      interp_tex_cubic(a.tex2[s], iw, ih, q2.x, q2.y);
+      const float iw = 1.0f / (float)a.Nrho, ih = 1.0f / (float)a.W2;
+      const int l2 = a.lo2 << a.F;
+      const int2 t1 = __ldg(a.c2lp1 + p), t2 = __ldg(a.c2lp2 + p);
+      const int2 q0 = ok ? make_int2(t0.y, t0.x - l2) : make_int2(0, 0);
+      const int2 q1 = ok ? make_int2(t1.y, t1.x - l2) : make_int2(0, 0);
+      const int2 q2 = ok ? make_int2(t2.y, t2.x - l2) : make_int2(0, 0);
+      const float v = interp_tex_cubic_fx(a.tex0[s], iw, ih, q0.x, q0.y, a.F, a.fsc) +
+                      interp_tex_cubic_fx(a.tex1[s], iw, ih, q1.x, q1.y, a.F, a.fsc) +
+                      interp_tex_cubic_fx(a.tex2[s], iw, ih, q2.x, q2.y, a.F, a.fsc);
       acc = ok ? v : 0.f;
     }
     a.fout[(size_t)s * a.npix + p] = acc;
     return;
   }
-  if (!isnan(t0.x)) {
-    acc += interp_cols(a.G0 + gs, a.Nrho, a.Nth, a.lo2, a.W2, t0, a.cubic);
-    acc += interp_cols(a.G1 + gs, a.Nrho, a.Nth, a.lo2, a.W2, __ldg(a.c2lp1 + p), a.cubic);
-    acc += interp_cols(a.G2 + gs, a.Nrho, a.Nth, a.lo2, a.W2, __ldg(a.c2lp2 + p), a.cubic);
+  if (t0.x != LP_FX_NONE) {
+    acc += interp_cols(a.G0 + gs, a.Nrho, a.Nth, a.lo2, a.W2, t0, a.F, a.fsc, a.cubic);
+    acc += interp_cols(a.G1 + gs, a.Nrho, a.Nth, a.lo2, a.W2, __ldg(a.c2lp1 + p), a.F, a.fsc, a.cubic);
+    acc += interp_cols(a.G2 + gs, a.Nrho, a.Nth, a.lo2, a.W2, __ldg(a.c2lp2 + p), a.F, a.fsc, a.cubic);
   }
   a.fout[(size_t)s * a.npix + p] = acc;
 }
@@ -935,11 +963,12 @@ __global__ void __launch_bounds__(256, 3) k_fwd_c2lp_p2(FwdC2LPArgs a) {
       const bool isa = j < na;
       const int r = inb ? (isa ? ia.x + j : ib.x + (j - na)) : 0;
       const int col = (inb && !isa) ? th + 1 : th;
-      float2 p = __ldg(a.c2lp + (size_t)col * L + r);
-      const bool ok = inb && !isnan(p.x);
-      if (!ok) p = make_float2(0.f, 0.f);
+      int2 p = __ldg(a.c2lp + (size_t)col * L + r);
+      const bool ok = inb && p.x != LP_FX_NONE;
+      if (!ok) p = make_int2(0, 0);
       const float e = __ldg(a.erho + r);
-      const float v = use_tex ? interp_tex_cubic(tx, invN, invN, p.x, p.y) : interp2d(img, a.N, a.N, p.x, p.y, a.cubic);
+      const float v = use_tex ? interp_tex_cubic_fx(tx, invN, invN, p.x, p.y, a.F, a.fsc)
+                              : interp2d_fx(img, a.N, a.N, p.x, p.y, a.F, a.fsc, a.cubic);
       val[u] = ok ? e * v : 0.f;
       pos[u] = inb ? 2 * spad(r) + (isa ? 0 : 1) : -1;
     }
@@ -1042,10 +1071,10 @@ __global__ void __launch_bounds__(256, 3) k_fwd_lp2polar_p2(FwdLP2PolarArgs a) {
   const int r0 = live ? a.rows[i0] : 0;
   const int r1 = (live && i0 + 1 < a.nrows) ? a.rows[i0 + 1] : -1;
   float w0[4], w1[4];
-  const int c0 = axis_weights(__ldg(a.thc + r0), a.cubic, w0);
+  const int c0 = axis_weights_fx(__ldg(a.thc + r0), a.F, a.fsc, a.cubic, w0);
   int c1 = 0;
   if (r1 >= 0) {
-    c1 = axis_weights(__ldg(a.thc + r1), a.cubic, w1);
+    c1 = axis_weights_fx(__ldg(a.thc + r1), a.F, a.fsc, a.cubic, w1);
   } else {
     w1[0] = w1[1] = w1[2] = w1[3] = 0.f;
   }
@@ -1108,7 +1137,7 @@ __global__ void __launch_bounds__(256, 3) k_fwd_lp2polar_p2(FwdLP2PolarArgs a) {
   for (int i = 0; i < 16; ++i) v[i] = sm[spad(t + i * T)];
   __syncthreads();
   // rho coordinates of both rows' N = 8 T polar points, loaded while the FFT runs
-  float tr0[8], tr1[8];
+  int tr0[8], tr1[8];
 #pragma unroll
   for (int m = 0; m < 8; ++m) {
     tr0[m] = __ldg(a.rhoc + (size_t)r0 * a.N + t + m * T);
@@ -1124,8 +1153,8 @@ __global__ void __launch_bounds__(256, 3) k_fwd_lp2polar_p2(FwdLP2PolarArgs a) {
     const int x = t + m * T;
     const int xo = x - a.cor_off;
     if (xo < 0 || xo >= a.N0) continue;
-    if (o0) out0[xo] = interp1d([&](int i) { return sm[spad(i)].x; }, L, tr0[m], a.cubic);
-    if (o1) out1[xo] = interp1d([&](int i) { return sm[spad(i)].y; }, L, tr1[m], a.cubic);
+    if (o0) out0[xo] = interp1d_fx([&](int i) { return sm[spad(i)].x; }, L, tr0[m], a.F, a.fsc, a.cubic);
+    if (o1) out1[xo] = interp1d_fx([&](int i) { return sm[spad(i)].y; }, L, tr1[m], a.F, a.fsc, a.cubic);
   }
 }
 
@@ -1205,16 +1234,15 @@ __global__ void __launch_bounds__(256, 3) k_adj_polar2lp_p2(AdjPolar2LPArgs a) {
   const bool live = th0 <= a.chi;
   const int th1 = (live && th0 + 1 <= a.chi) ? th0 + 1 : -1;
   const float* img = a.rbuf + (size_t)s * a.Nproj * N;
-  const float nanv = __int_as_float(0x7fc00000);
-  const float ta0 = live ? __ldg(a.ta + th0) : nanv;
-  const float ta1 = th1 >= 0 ? __ldg(a.ta + th1) : nanv;
+  const int ta0 = live ? __ldg(a.ta + th0) : LP_FX_NONE;
+  const int ta1 = th1 >= 0 ? __ldg(a.ta + th1) : LP_FX_NONE;
   float w0[4], w1[4];
   int rw0[4], rw1[4];
-  const bool has0 = !isnan(ta0), has1 = !isnan(ta1);
+  const bool has0 = ta0 != LP_FX_NONE, has1 = ta1 != LP_FX_NONE;
   const int ntap = a.cubic ? 4 : 2;
   {
-    const int c0 = has0 ? axis_weights(ta0, a.cubic, w0) : 0;
-    const int c1 = has1 ? axis_weights(ta1, a.cubic, w1) : 0;
+    const int c0 = has0 ? axis_weights_fx(ta0, a.F, a.fsc, a.cubic, w0) : 0;
+    const int c1 = has1 ? axis_weights_fx(ta1, a.F, a.fsc, a.cubic, w1) : 0;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       rw0[j] = wrapi(c0 + j, a.Nproj);
@@ -1240,19 +1268,19 @@ __global__ void __launch_bounds__(256, 3) k_adj_polar2lp_p2(AdjPolar2LPArgs a) {
     prof[N + x] = p1;
   }
   __syncthreads();
-  const float* sx0 = a.sx + (size_t)(live ? th0 : 0) * L;
-  const float* sx1 = a.sx + (size_t)max(th1, 0) * L;
-  float xs0[16], xs1[16];
+  const int* sx0 = a.sx + (size_t)(live ? th0 : 0) * L;
+  const int* sx1 = a.sx + (size_t)max(th1, 0) * L;
+  int xs0[16], xs1[16];
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
-    xs0[i] = live ? __ldg(sx0 + t + i * T) : nanv;
-    xs1[i] = th1 >= 0 ? __ldg(sx1 + t + i * T) : nanv;
+    xs0[i] = live ? __ldg(sx0 + t + i * T) : LP_FX_NONE;
+    xs1[i] = th1 >= 0 ? __ldg(sx1 + t + i * T) : LP_FX_NONE;
   }
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
-    const bool ok0 = !isnan(xs0[i]), ok1 = !isnan(xs1[i]);
-    const float v0 = interp1d([&](int q) { return prof[q]; }, N, ok0 ? xs0[i] : 0.f, a.cubic);
-    const float v1 = interp1d([&](int q) { return prof[N + q]; }, N, ok1 ? xs1[i] : 0.f, a.cubic);
+    const bool ok0 = xs0[i] != LP_FX_NONE, ok1 = xs1[i] != LP_FX_NONE;
+    const float v0 = interp1d_fx([&](int q) { return prof[q]; }, N, ok0 ? xs0[i] : 0, a.F, a.fsc, a.cubic);
+    const float v1 = interp1d_fx([&](int q) { return prof[N + q]; }, N, ok1 ? xs1[i] : 0, a.F, a.fsc, a.cubic);
     sm[spad(t + i * T)] = make_float2(ok0 ? v0 : 0.f, ok1 ? v1 : 0.f);
   }
   __syncthreads();
@@ -1262,9 +1290,9 @@ __global__ void __launch_bounds__(256, 3) k_adj_polar2lp_p2(AdjPolar2LPArgs a) {
     if (!live || th < 0) continue;
     const int wb = __ldg(a.woff + th), we = __ldg(a.woff + th + 1);
     for (int w = wb + t; w < we; w += T) {
-      const float4 p = __ldg(a.wpt + w);
-      const int r = (int)p.x;
-      const float val = interp2d(img, N, a.Nproj, p.y, p.z, a.cubic);
+      const int4 p = __ldg(a.wpt + w);
+      const int r = p.x;
+      const float val = interp2d_fx(img, N, a.Nproj, p.y, p.z, a.F, a.fsc, a.cubic);
       if (c == 0) sm[spad(r)].x += val;
       else sm[spad(r)].y += val;
     }
@@ -1519,7 +1547,7 @@ __global__ void __launch_bounds__(256) k_fwdT_polar(FwdTPolarArgs a) {
         if (xo < 0 || xo >= a.N0) continue;
         const float val = __ldg(row + xo);
         float w[4];
-        const int c = axis_weights(__ldg(a.rhoc + (size_t)r * a.N + x), a.cubic, w);
+        const int c = axis_weights_fx(__ldg(a.rhoc + (size_t)r * a.N + x), a.F, a.fsc, a.cubic, w);
         for (int j = 0; j < ntap; ++j) atomicAdd(u + q * L + wrapi(c + j, L), w[j] * val);
       }
     }
@@ -1528,9 +1556,9 @@ __global__ void __launch_bounds__(256) k_fwdT_polar(FwdTPolarArgs a) {
     __syncthreads();
     const CBuf Z = fft_block<-1>(A, B, a.plan, 1, 0);
     float w0[4], w1[4];
-    const int t0 = axis_weights(__ldg(a.thc + r0), a.cubic, w0);
+    const int t0 = axis_weights_fx(__ldg(a.thc + r0), a.F, a.fsc, a.cubic, w0);
     int t1 = 0;
-    if (r1 >= 0) t1 = axis_weights(__ldg(a.thc + r1), a.cubic, w1);
+    if (r1 >= 0) t1 = axis_weights_fx(__ldg(a.thc + r1), a.F, a.fsc, a.cubic, w1);
     for (int k = threadIdx.x; k < a.Nk; k += blockDim.x) {
       const float2 z1 = Z.get(k);
       const float2 z2 = Z.get(k == 0 ? 0 : L - k);
@@ -1564,20 +1592,22 @@ __global__ void __launch_bounds__(256) k_fwdT_polar(FwdTPolarArgs a) {
   }
 }
 
-__device__ __forceinline__ void scatter2d(float* img, int W, int H, float x, float y, float val, int cubic) {
-  const float fx = floorf(x), fy = floorf(y);
-  const int ix = (int)fx, iy = (int)fy;
+// transposed 2-D interpolation: scatter val with the weights of the sample at fixed-point (x, y)
+__device__ __forceinline__ void scatter2d_fx(float* img, int W, int H, int vx, int vy, int F, float fsc, float val,
+                                             int cubic) {
+  const int ix = fx_int(vx, F), iy = fx_int(vy, F);
+  const float ax = fx_frac(vx, F, fsc), ay = fx_frac(vy, F, fsc);
   float wx[4], wy[4];
   int nt;
   if (cubic) {
-    bspline_w(x - fx, wx);
-    bspline_w(y - fy, wy);
+    bspline_w(ax, wx);
+    bspline_w(ay, wy);
     nt = 4;
   } else {
-    wx[0] = 1.f - (x - fx);
-    wx[1] = x - fx;
-    wy[0] = 1.f - (y - fy);
-    wy[1] = y - fy;
+    wx[0] = 1.f - ax;
+    wx[1] = ax;
+    wy[0] = 1.f - ay;
+    wy[1] = ay;
     nt = 2;
   }
   const int ox = cubic ? 1 : 0;
@@ -1608,13 +1638,13 @@ __global__ void __launch_bounds__(256) k_fwdT_cart(FwdTCartArgs a) {
   for (int q = 0; q < 2; ++q) {
     const int th = q == 0 ? th0 : th1;
     if (th < 0) break;
-    const float2* cc = a.c2lp + (size_t)th * L;
+    const int2* cc = a.c2lp + (size_t)th * L;
     for (int r = threadIdx.x; r < L; r += blockDim.x) {
-      const float2 p = __ldg(cc + r);
-      if (isnan(p.x)) continue;
+      const int2 p = __ldg(cc + r);
+      if (p.x == LP_FX_NONE) continue;
       const float2 zv = z.get(r);
       const float val = __ldg(a.erho + r) * (q == 0 ? zv.x : zv.y);
-      scatter2d(img, a.N, a.N, p.x, p.y, val, a.cubic);
+      scatter2d_fx(img, a.N, a.N, p.x, p.y, a.F, a.fsc, val, a.cubic);
     }
   }
 }

@@ -7,6 +7,10 @@
 
 namespace lpgb {
 
+// Interpolation coordinates are 32-bit fixed point, value = v * 2^-F (F per
+// handle direction); LP_FX_NONE marks a table entry without a point.
+#define LP_FX_NONE ((int)0x80000000)
+
 // ---- spectrum layout ------------------------------------------------------
 // The log-polar spectrum of one slice (Nk rho frequencies x Ntheta columns,
 // complex) is stored in tiles of kSpecTile consecutive rho frequencies:
@@ -39,13 +43,15 @@ struct ColPrefilterArgs {     // prefilter along the slow axis, in place
 struct FwdC2LPArgs {          // Cartesian -> log-polar gather, e^rho, FFT along rho
   const float* fbuf;          // [S][N][N] prefiltered image
   float2* spec;               // [S] spectra (Nk = N+1 rho frequencies), tiled layout (sidx)
-  const float2* c2lp;         // [Nth][Nrho] texel coordinates (x, y); x = NaN outside the disk
+  const int2* c2lp;           // [Nth][Nrho] fixed-point texel coordinates (x, y); x = LP_FX_NONE outside the disk
   const float* erho;          // [Nrho]
   int N, Nth, Nrho, Nk, cubic;
   FFTPlan plan;               // length Nrho
   const cudaTextureObject_t* tex;  // if set: the prefiltered image per slice as a gather texture (cubic)
   const int2* ival;           // [Nth] rho interval [x, y] of a column's disk points (y < x: none); if set,
   int col_lo, col_hi;         //   only column pairs meeting [col_lo, col_hi] are launched (others untouched)
+  int F;                      // fixed-point fraction bits of the coordinates
+  float fsc;                  // 2^-F
 };
 
 struct ThetaConvArgs {        // FFT along theta, multiply by the kernel, inverse
@@ -63,12 +69,14 @@ struct ThetaConvArgs {        // FFT along theta, multiply by the kernel, invers
 struct FwdLP2PolarArgs {      // inverse FFT along rho of theta-combined columns, polar gather
   const float2* spec;         // [S] spectra, tiled layout
   float* Rout;                // [S][Nproj0][N0] caller's sinogram
-  const float* thc;           // [Nproj] theta texel coordinate per internal angle row
-  const float* rhoc;          // [Nproj][N] rho texel coordinate per polar point
+  const int* thc;             // [Nproj] theta texel coordinate per internal angle row (fixed point)
+  const int* rhoc;            // [Nproj][N] rho texel coordinate per polar point (fixed point)
   const int* rows;            // internal rows handled by this launch
   int nrows;
   int N, N0, Nth, Nrho, Nk, Nproj0, os, cor_off, cubic;
   FFTPlan plan;               // length Nrho
+  int F;
+  float fsc;
 };
 
 // ---- adjoint ----------------------------------------------------------------
@@ -83,13 +91,15 @@ struct AdjIngestArgs {        // cor shift, angle step, edge padding, FBP filter
 struct AdjPolar2LPArgs {      // polar -> log-polar gather (+ wrap points), FFT along rho
   const float* rbuf;          // [S][Nproj][N] prefiltered sinogram
   float2* spec;               // [S][Nk][Nth]
-  const float* ta;            // [Nth] angle texel coordinate per column (NaN: no points)
-  const float* sx;            // [Nth][Nrho] s texel coordinate (NaN: not a point)
+  const int* ta;              // [Nth] angle texel coordinate per column, fixed point (LP_FX_NONE: no points)
+  const int* sx;              // [Nth][Nrho] s texel coordinate, fixed point (LP_FX_NONE: not a point)
   const int* woff;            // [Nth+1] wrap-point offsets per column
-  const float4* wpt;          // wrap points: (rho, s coordinate, angle coordinate, 0)
+  const int4* wpt;            // wrap points: (rho index, s coordinate, angle coordinate, 0), fixed point
   int N, Nth, Nrho, Nk, Nproj, cubic;
   int clo, chi;
   FFTPlan plan;               // length Nrho
+  int F;
+  float fsc;
 };
 
 struct AdjLPColsArgs {        // inverse FFT along rho, write real log-polar columns
@@ -104,15 +114,17 @@ struct AdjLP2CartArgs {       // log-polar -> Cartesian gather summed over spans
   const float* G0;
   const float* G1;
   const float* G2;            // [S][W2][Nrho] per span
-  const float2* c2lp0;
-  const float2* c2lp1;
-  const float2* c2lp2;        // [N0][N0] (theta, rho) texel coordinates per span; NaN outside disk
+  const int2* c2lp0;
+  const int2* c2lp1;
+  const int2* c2lp2;          // [N0][N0] (theta, rho) texel coordinates per span, fixed point; LP_FX_NONE outside
   float* fout;                // [S][N0][N0]
   int N0, Nth, Nrho, lo2, W2, cubic;
   int npix;
   const cudaTextureObject_t* tex0;  // if set (cubic): the columns of each span and slice as gather textures
   const cudaTextureObject_t* tex1;
   const cudaTextureObject_t* tex2;
+  int F;
+  float fsc;
 };
 
 // launches (defined in lp_kernels.cu); return the launch error
@@ -136,21 +148,25 @@ namespace lpgb {
 struct FwdTPolarArgs {        // sinogram rows -> log-polar spectrum columns (transposed lp2polar)
   const float* Rin;           // [S][Nproj0][N0] caller's gradient
   float2* spec;               // [S][Nk][Nth], zeroed; block owns columns [c0, c0+CW)
-  const float* thc;           // [Nproj] theta coordinate per internal row
-  const float* rhoc;          // [Nproj][N] rho coordinate per polar point
+  const int* thc;             // [Nproj] theta coordinate per internal row (fixed point)
+  const int* rhoc;            // [Nproj][N] rho coordinate per polar point (fixed point)
   const int* rows;            // rows of the span (multiples of os), sorted
   const int2* blk;            // per column block: [first, last) into rows
   int N, N0, Nth, Nrho, Nk, Nproj0, os, cor_off, cubic, lo, CW;
   FFTPlan plan;               // length Nrho
+  int F;
+  float fsc;
 };
 
 struct FwdTCartArgs {         // spectrum columns -> real log-polar columns -> scatter to the image
   const float2* spec;         // [S][Nk][Nth]
   float* acc;                 // [S][N][N] accumulator (atomic adds)
-  const float2* c2lp;         // [Nth][Nrho] this span
+  const int2* c2lp;           // [Nth][Nrho] this span (fixed point)
   const float* erho;          // [Nrho]
   int N, Nth, Nrho, Nk, dlo, dhi, cubic;
   FFTPlan plan;
+  int F;
+  float fsc;
 };
 
 struct PrefilterTArgs {       // transposed prefilter along lines of length L, in place

@@ -649,9 +649,10 @@ extern "C" int lp_precompute_sizes(int N0, int Nproj, int Nslices, double cor, i
   return LP_OK;
 }
 
-extern "C" int lp_precompute(int N0, int Nproj, int Nslices, double cor, int cubic, const char* filter,
-                             int precision, int with_fwd, int nthreads, float* glpars, int32_t* fwdparsi,
-                             float* fwdparamsf, int32_t* adjparsi, float* adjparamsf) {
+template <typename Real>
+static int precompute_impl(int N0, int Nproj, int Nslices, double cor, int cubic, const char* filter,
+                           int precision, int with_fwd, int nthreads, float* glpars, int32_t* fwdparsi,
+                           Real* fwdparamsf, int32_t* adjparsi, Real* adjparamsf) {
   bool wf;
   int rc = check_args(N0, Nproj, Nslices, cor, filter, wf);
   if (rc) return rc;
@@ -676,10 +677,10 @@ extern "C" int lp_precompute(int N0, int Nproj, int Nslices, double cor, int cub
     for (int t = 0; t < G.Nth; ++t) glpars[10 + (size_t)r * G.Nth + t] = e;
   }
   const int nh = G.Nth / 2 + 1;
-  auto put_fz = [&](float* dst, const std::vector<cd>& fz) {
+  auto put_fz = [&](Real* dst, const std::vector<cd>& fz) {
     for (size_t i = 0; i < (size_t)G.Nrho * nh; ++i) {
-      dst[2 * i] = (float)fz[i].real();
-      dst[2 * i + 1] = (float)fz[i].imag();
+      dst[2 * i] = (Real)fz[i].real();
+      dst[2 * i + 1] = (Real)fz[i].imag();
     }
   };
   if (with_fwd) {
@@ -692,7 +693,7 @@ extern "C" int lp_precompute(int N0, int Nproj, int Nslices, double cor, int cub
     o = 0;
     for (auto* arr : {T.lp2C1, T.lp2C2, T.p2lp1, T.p2lp2})
       for (int k = 0; k < 3; ++k)
-        for (double v : arr[k]) fwdparamsf[o++] = (float)v;
+        for (double v : arr[k]) fwdparamsf[o++] = (Real)v;
     put_fz(fwdparamsf + o, kernel_half(G, false, ref, nthreads));
   }
   {
@@ -707,14 +708,28 @@ extern "C" int lp_precompute(int N0, int Nproj, int Nslices, double cor, int cub
     o = 0;
     for (auto* arr : {T.C2lp1, T.C2lp2, T.lp2p1, T.lp2p2, T.lp2p1w, T.lp2p2w})
       for (int k = 0; k < 3; ++k)
-        for (double v : arr[k]) adjparamsf[o++] = (float)v;
+        for (double v : arr[k]) adjparamsf[o++] = (Real)v;
     put_fz(adjparamsf + o, kernel_half(G, true, ref, nthreads));
     o += 2 * (int64_t)G.Nrho * nh;
     if (wf) {
       std::vector<double> fl;
       take_filter(G.N, filter, fl);
-      for (int i = 0; i < 4 * G.N; ++i) adjparamsf[o++] = (float)fl[i];
+      for (int i = 0; i < 4 * G.N; ++i) adjparamsf[o++] = (Real)fl[i];
     }
   }
   return LP_OK;
+}
+
+extern "C" int lp_precompute(int N0, int Nproj, int Nslices, double cor, int cubic, const char* filter,
+                             int precision, int with_fwd, int nthreads, float* glpars, int32_t* fwdparsi,
+                             float* fwdparamsf, int32_t* adjparsi, float* adjparamsf) {
+  return precompute_impl(N0, Nproj, Nslices, cor, cubic, filter, precision, with_fwd, nthreads, glpars, fwdparsi,
+                         fwdparamsf, adjparsi, adjparamsf);
+}
+
+extern "C" int lp_precompute_f64(int N0, int Nproj, int Nslices, double cor, int cubic, const char* filter,
+                                 int precision, int with_fwd, int nthreads, float* glpars, int32_t* fwdparsi,
+                                 double* fwdparamsf, int32_t* adjparsi, double* adjparamsf) {
+  return precompute_impl(N0, Nproj, Nslices, cor, cubic, filter, precision, with_fwd, nthreads, glpars, fwdparsi,
+                         fwdparamsf, adjparsi, adjparamsf);
 }

@@ -77,27 +77,47 @@ class lpTransform:
 
     # ---- precompute / init (lpTransform.py:19-40) -------------------------
     def precompute(self, flg):
-        """Parameters for the lp method (fwd ones too when flg), as packed arrays."""
-        (self.glpars, self.fwdparsi, self.fwdparamsf, self.adjparsi,
-         self.adjparamsf) = _lib.precompute(self.N, self.Nproj, self.Nslices, self.cor, self.interp_type,
-                                            self.filter_type, self.precision, with_fwd=bool(flg))
+        """Parameters for the lp method (fwd ones too when flg), as packed arrays.
+
+        With precision 'fp64' the float arrays are computed and kept in float64
+        (the handle then stores interpolation coordinates with ~60x less rounding
+        than the float32 format); `fwdparamsf`/`adjparamsf` hold their float32
+        rounding, the reference's packed format."""
+        wide = self.precision == "fp64"
+        (self.glpars, self.fwdparsi, ff, self.adjparsi, af) = _lib.precompute(
+            self.N, self.Nproj, self.Nslices, self.cor, self.interp_type, self.filter_type, self.precision,
+            with_fwd=bool(flg), wide=wide)
+        self._wide = (ff, af) if wide else None
+        self.fwdparamsf = None if ff is None else ff.astype(np.float32)
+        self.adjparamsf = af.astype(np.float32)
 
     def load_packed(self, glpars, fwdparsi, fwdparamsf, adjparsi, adjparamsf):
-        """Use packed arrays made elsewhere (e.g. by the reference's own precompute)."""
+        """Use packed arrays made elsewhere (e.g. by the reference's own precompute);
+        float64 float arrays are kept as the handle's tables."""
         self.glpars = np.asarray(glpars, np.float32)
         self.fwdparsi = None if fwdparsi is None else np.asarray(fwdparsi, np.int32)
-        self.fwdparamsf = None if fwdparamsf is None else np.asarray(fwdparamsf, np.float32)
         self.adjparsi = np.asarray(adjparsi, np.int32)
+        wide = np.asarray(adjparamsf).dtype == np.float64
+        self._wide = (None if fwdparamsf is None else np.asarray(fwdparamsf, np.float64),
+                      np.asarray(adjparamsf, np.float64)) if wide else None
+        self.fwdparamsf = None if fwdparamsf is None else np.asarray(fwdparamsf, np.float32)
         self.adjparamsf = np.asarray(adjparamsf, np.float32)
+
+    def tables(self):
+        """(glpars, fwdparsi, fwdparamsf, adjparsi, adjparamsf) as the handle receives them
+        (float64 float arrays with precision 'fp64')."""
+        ff, af = self._wide if getattr(self, "_wide", None) is not None else (self.fwdparamsf, self.adjparamsf)
+        return self.glpars, self.fwdparsi, ff, self.adjparsi, af
 
     def initcmem(self, flg, gpu):
         """Create the native handle for device `gpu` and upload the tables."""
         h = _lib.Handle(self.glpars, gpu)
+        _, fi, ff, ai, af = self.tables()
         if flg:
-            if self.fwdparsi is None:
+            if fi is None:
                 raise RuntimeError("precompute(1) is needed before initcmem(1, gpu)")
-            h.init_fwd(self.fwdparsi, self.fwdparamsf)
-        h.init_adj(self.adjparsi, self.adjparamsf)
+            h.init_fwd(fi, ff)
+        h.init_adj(ai, af)
         old = self.clphandle[gpu]
         self.clphandle[gpu] = h
         if old is not None:

@@ -105,6 +105,31 @@ def test_fp64_oracle_error_phantom(torch_cuda, args):
     assert O.rel_l2(_adj(torch_cuda, h, R), tr.adj(R)) < TOL
 
 
+@pytest.mark.parametrize("args", [(256, 384, 'cubic', 'shepp-logan', 128), (512, 768, 'cubic', 'ramp', 256),
+                                  (192, 288, 'linear', 'hann', 90), (2048, 3000, 'cubic', 'shepp-logan', 1024)])
+def test_float64_tables(torch_cuda, args):
+    """Handles fed float64 tables (fixed-point coordinates on the device): parity with the
+    oracle fed the same float64 tables, and FBP within 1e-6 of the unrounded float64
+    oracle (float32 tables leave 4.6e-6 at N=512 and 3.3e-5 at N=2048)."""
+    from lprec_gb300 import _lib
+    N0, Nproj, interp, filt, cor = args
+    wide = _lib.precompute(N0, Nproj, 1, cor, interp, filt, precision='fp64', wide=True)
+    assert wide[2].dtype == np.float64 and wide[4].dtype == np.float64
+    h = _handle(wide)
+    tr = O.Transform.from_packed(*wide)
+    rng = np.random.default_rng(11)
+    f = O.ellipse_phantom(N0, 10, rng)[None]
+    R = tr.fwd(f)
+    Rn = R + 0.01 * np.abs(R).max() * rng.standard_normal(R.shape)
+    Rn = np.float32(Rn).astype(np.float64)
+    assert O.rel_l2(_fwd(torch_cuda, h, f), R) < TOL
+    fb = _adj(torch_cuda, h, Rn)
+    assert O.rel_l2(fb, tr.adj(Rn)) < TOL
+    if N0 <= 512:
+        exact = O.Transform(N0, Nproj, 1, filt, cor, interp, mode='fp64', rounded=False)
+        assert O.rel_l2(fb, exact.adj(Rn)) < 1e-6, O.rel_l2(fb, exact.adj(Rn))
+
+
 def test_reference_pins_adj_many(torch_cuda, golden_dir):
     """tests/test_adj_many.py pins on the GPU: 8 slices scaled by (8-k)."""
     from lprec_gb300.lpTransform import lpTransform

@@ -19,7 +19,7 @@ def setup():
     lp = lpTransform.lpTransform(N, Nproj, S, 'none', N / 2, 'cubic')
     lp.precompute(1)
     lp.initcmem(1, 0)
-    tr = O.Transform.from_packed(lp.glpars, lp.fwdparsi, lp.fwdparamsf, lp.adjparsi, lp.adjparamsf)
+    tr = O.Transform.from_packed(*lp.tables())
     rng = np.random.default_rng(4)
     f = np.stack([O.ellipse_phantom(N, 10, rng) for _ in range(S)])
     tomo = tr.fwd(f).astype(np.float32)

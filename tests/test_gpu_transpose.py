@@ -39,7 +39,7 @@ def _fwdT(torch, lp, g):
 def test_transpose_matches_oracle(torch_cuda, args):
     N0, Nproj, cor, interp = args
     lp = _lp(N0, Nproj, 2, cor, interp)
-    tr = O.Transform.from_packed(lp.glpars, lp.fwdparsi, lp.fwdparamsf, lp.adjparsi, lp.adjparamsf)
+    tr = O.Transform.from_packed(*lp.tables())
     g = np.random.default_rng(5).standard_normal((2, Nproj, N0)).astype(np.float32).astype(np.float64)
     fg = _fwdT(torch_cuda, lp, g)
     fo = tr.fwd_T(g)
@@ -71,7 +71,7 @@ def test_autograd_finite_differences(torch_cuda):
     from lprec_gb300.autograd import radon
     N0, Nproj, S = 128, 192, 2
     lp = _lp(N0, Nproj, S, 64, 'cubic')
-    tr = O.Transform.from_packed(lp.glpars, lp.fwdparsi, lp.fwdparamsf, lp.adjparsi, lp.adjparamsf)
+    tr = O.Transform.from_packed(*lp.tables())
     rng = np.random.default_rng(2)
     f0 = np.stack([O.ellipse_phantom(N0, 10, rng) for _ in range(S)]).astype(np.float32)
     y = (tr.fwd(f0) * 1.1).astype(np.float32)
@@ -115,7 +115,7 @@ def test_cg_exact_matches_oracle(torch_cuda):
     from lprec_gb300 import lpmethods
     N0, Nproj = 64, 96
     lp = _lp(N0, Nproj, 2, 32, 'cubic')
-    tr = O.Transform.from_packed(lp.glpars, lp.fwdparsi, lp.fwdparamsf, lp.adjparsi, lp.adjparamsf)
+    tr = O.Transform.from_packed(*lp.tables())
     rng = np.random.default_rng(4)
     ph = np.stack([O.ellipse_phantom(N0, 5, rng) for _ in range(2)])
     tomo = np.float32(tr.fwd(ph)).astype(np.float64)
@@ -135,7 +135,7 @@ def test_tv_gd_decreases_objective(torch_cuda):
     from lprec_gb300 import lpmethods
     N0, Nproj = 64, 96
     lp = _lp(N0, Nproj, 2, 32, 'cubic')
-    tr = O.Transform.from_packed(lp.glpars, lp.fwdparsi, lp.fwdparamsf, lp.adjparsi, lp.adjparamsf)
+    tr = O.Transform.from_packed(*lp.tables())
     rng = np.random.default_rng(6)
     ph = np.stack([O.ellipse_phantom(N0, 5, rng) for _ in range(2)])
     tomo = tr.fwd(ph)

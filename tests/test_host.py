@@ -140,3 +140,34 @@ def test_null_handle_calls_return_errors(lib):
     assert L.lp_set_schedule(None, None, 0) == 1
     assert b"null" in L.lp_last_error()
     assert L.lp_destroy(None) == 0
+
+
+def test_graph_watchdog_times_out_on_host():
+    """The uneven-batch watchdog on a fake event that never completes (no GPU involved)."""
+    from lprec_gb300.batch import wait_event
+
+    class Never:
+        def query(self):
+            return False
+
+    class After:
+        def __init__(self, n):
+            self.n = n
+
+        def query(self):
+            self.n -= 1
+            return self.n <= 0
+
+    t = [0.0]
+
+    def clock():
+        return t[0]
+
+    def sleep(dt):
+        t[0] += dt
+    with pytest.raises(TimeoutError):
+        wait_event(Never(), 0.05, poll_s=0.01, clock=clock, sleep=sleep)
+    assert 0.05 <= t[0] < 0.07
+    t[0] = 0.0
+    wait_event(After(3), 1.0, poll_s=0.01, clock=clock, sleep=sleep)
+    assert t[0] < 0.05
