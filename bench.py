@@ -33,6 +33,17 @@ UNIT = "slices/s"
 WORKLOAD = dict(N=2048, Nproj=3000, S=128, filter="shepp-logan", interp="cubic", ellipses=30, seed=3, noise=0.01)
 # algorithmic HBM bytes per slice of one fwd+adj step (N=2048, Nproj=3000, batch 128)
 ALGO_BYTES_PER_SLICE = 1.541e9
+# DRAM bytes (read + write) per slice and launch measured by ncu on an 8-slice step of the
+# same geometry (profiles/ncu_full_step_n2048_s8.md: launch averages / 8); the traffic of a
+# 128-slice launch is taken as 128 times these (every term but the per-launch tables grows
+# with the slice count)
+NCU_DRAM_BYTES_PER_SLICE = {
+    "fwd_ingest": (134.2e6 + 85.9e6) / 8, "col_prefilter": (166.7e6 + 232.0e6) / 8,
+    "fwd_c2lp": (128.8e6 + 93.3e6) / 8, "theta_conv": (168.2e6 + 79.8e6) / 8,
+    "fwd_lp2polar": (143.8e6 + 44.2e6) / 8, "adj_ingest": (196.7e6 + 152.5e6) / 8,
+    "adj_polar2lp": (83.2e6 + 88.7e6) / 8, "adj_lpcols": (135.6e6 + 94.3e6) / 8,
+    "adj_lp2cart": (354.1e6 + 117.7e6) / 8,
+}
 
 
 def dist_env():
@@ -552,7 +563,10 @@ def run_ours(args):
                     "matches_device_result": e2e_ok},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": (NCU_DRAM_BYTES_PER_SLICE[name] * S
+                                     if (N, Nproj) == (2048, 3000) and name in NCU_DRAM_BYTES_PER_SLICE else None),
+                         "traffic_source": "ncu dram__bytes_read+write, 8-slice capture scaled to the launch's slices",
                          "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms},
             "step_roofline": {"algorithmic_bytes_per_slice": ALGO_BYTES_PER_SLICE, "achieved": step_gbs,
                               "peak": peak, "frac": step_gbs / peak},

@@ -66,10 +66,19 @@ __device__ __forceinline__ void twiddle_powers(float f, float2* w) {
   }
 }
 
-template <int L, int DIR, int R, int NS, bool LAST>
-__device__ __forceinline__ void reg_stage(float2 (&v)[16], float2* sm, int t) {
+// where the last stage leaves the transform
+enum RegFftOut { kOutSmem = 0, kOutPlanar = 1, kOutRegs = 2, kOutCall = 3 };
+
+struct NoSink {
+  __device__ __forceinline__ void operator()(int, float2) const {}
+};
+
+template <int L, int DIR, int R, int NS, bool LAST, int OUT = kOutSmem, class Sink = NoSink>
+__device__ __forceinline__ void reg_stage(float2 (&v)[16], float2* sm, int t, const Sink& sink = Sink()) {
   constexpr int T = L / 16;
   constexpr int NB = 16 / R;
+  static_assert((OUT != kOutRegs && OUT != kOutCall) || (LAST && NS * R == L),
+                "register or sink output only from a last stage spanning L");
 #pragma unroll
   for (int m = 0; m < NB; ++m) {
     const int jp = t + m * T;
@@ -85,10 +94,29 @@ __device__ __forceinline__ void reg_stage(float2 (&v)[16], float2* sm, int t) {
     }
     reg_bfly<R, DIR>(x);
     const int base = (jp - k) * R + k;
+    if constexpr (OUT == kOutRegs) {
+      // jp < NS here, so output i of this butterfly is element jp + i*NS = t + (m + i*NB)*T:
+      // back into the register it came from
 #pragma unroll
-    for (int i = 0; i < R; ++i) sm[spad(base + i * NS)] = x[i];
+      for (int i = 0; i < R; ++i) v[m + i * NB] = x[i];
+    } else if constexpr (OUT == kOutCall) {
+      // the same elements handed to the caller as soon as they exist
+#pragma unroll
+      for (int i = 0; i < R; ++i) sink(jp + i * NS, x[i]);
+    } else if constexpr (OUT == kOutPlanar) {
+      float* re = reinterpret_cast<float*>(sm);
+      float* im = re + reg_fft_slots(L);
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        re[spad(base + i * NS)] = x[i].x;
+        im[spad(base + i * NS)] = x[i].y;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < R; ++i) sm[spad(base + i * NS)] = x[i];
+    }
   }
-  __syncthreads();
+  if constexpr (OUT != kOutRegs && OUT != kOutCall) __syncthreads();
   if constexpr (!LAST) {
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = sm[spad(t + i * T)];
@@ -98,21 +126,31 @@ __device__ __forceinline__ void reg_stage(float2 (&v)[16], float2* sm, int t) {
 
 // Transform one signal.  v: this thread's 16 elements x[t + i*T]; sm: the
 // signal's shared buffer of reg_fft_slots(L) float2.  All threads of the
-// block must call it (it synchronises the block).
-template <int L, int DIR>
-__device__ __forceinline__ void reg_fft(float2 (&v)[16], float2* sm, int t) {
+// block must call it (it synchronises the block).  OUT:
+//   kOutSmem   -- the result in sm in natural order at spad(k), registers free;
+//   kOutPlanar -- the same as two float planes (real parts at ((float*)sm)[spad(k)],
+//                 imaginary parts reg_fft_slots(L) floats further), so that 4-byte
+//                 reads of one part by neighbouring threads fall in distinct banks;
+//   kOutRegs   -- the result in registers, v[q] = X[t + q*T]: the distribution the
+//                 input had, so a pointwise multiply and another transform (or
+//                 stores of a chosen range) follow without a shared-memory round
+//                 trip.  sm is free on return (no final barrier).
+//   kOutCall   -- the same elements X[t + q*T] passed to sink(t + q*T, value) as the
+//                 last stage produces them (registers are released as it goes).
+template <int L, int DIR, int OUT = kOutSmem, class Sink = NoSink>
+__device__ __forceinline__ void reg_fft(float2 (&v)[16], float2* sm, int t, const Sink& sink = Sink()) {
   static_assert(L == 256 || L == 512 || L == 1024 || L == 2048 || L == 4096 || L == 8192, "size");
   reg_stage<L, DIR, 16, 1, false>(v, sm, t);
   if constexpr (L == 256) {
-    reg_stage<L, DIR, 16, 16, true>(v, sm, t);
+    reg_stage<L, DIR, 16, 16, true, OUT>(v, sm, t, sink);
   } else if constexpr (L == 8192) {
     reg_stage<L, DIR, 16, 16, false>(v, sm, t);
     reg_stage<L, DIR, 16, 256, false>(v, sm, t);
-    reg_stage<L, DIR, 2, 4096, true>(v, sm, t);
+    reg_stage<L, DIR, 2, 4096, true, OUT>(v, sm, t, sink);
   } else {
     reg_stage<L, DIR, 16, 16, false>(v, sm, t);
     constexpr int R3 = L / 256;
-    reg_stage<L, DIR, R3, 256, true>(v, sm, t);
+    reg_stage<L, DIR, R3, 256, true, OUT>(v, sm, t, sink);
   }
 }
 

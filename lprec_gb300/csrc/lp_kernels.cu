@@ -346,15 +346,21 @@ __global__ void k_col_prefilter(ColPrefilterArgs a) {
     int n;
     const cudaSurfaceObject_t so = a.surf ? a.surf[s] : 0;
     if (e + nw >= H) {
-      // exact anticausal initialisation at H-1
-      float last = (nw > 0) ? wu[nw - 1] : col[(size_t)(H - 1) * W];
+      // exact anticausal initialisation at H-1 (static indices only, so wu stays in registers)
+      float last = 0.f;
+#pragma unroll
+      for (int i = 0; i < LP_WARM; ++i)
+        if (i == nw - 1) last = wu[i];
+      if (nw == 0) last = col[(size_t)(H - 1) * W];
       c = (z / (z - 1.0f)) * last;
       if (nw == 0) {
         if (a.surf) surf2Dwrite(c, so, x * (int)sizeof(float), H - 1);
         else col[(size_t)(H - 1) * W] = c;
         n = H - 2;
       } else {
-        for (int i = nw - 2; i >= 0; --i) c = z * (c - wu[i]);
+#pragma unroll
+        for (int i = LP_WARM - 2; i >= 0; --i)
+          if (i <= nw - 2) c = z * (c - wu[i]);
         n = e - 1;
       }
     } else {
@@ -1185,18 +1191,18 @@ __global__ void __launch_bounds__(256, 2) k_adj_ingest_p2(AdjIngestArgs a) {
       const int xi = min(max(x - a.cor_off, 0), a.N0 - 1);
       v[i] = x < N ? make_float2(__ldg(in0 + xi), q1 >= 0 ? __ldg(in1 + xi) : 0.f) : make_float2(0.f, 0.f);
     }
-    reg_fft<L, -1>(v, sm, t);
+    // filter spectrum multiply and line stores straight from registers (v[i] = X[t + i*T])
+    reg_fft<L, -1, kOutRegs>(v, sm, t);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = cscale(v[i], __ldg(a.H + t + i * T));
+    reg_fft<L, 1, kOutRegs>(v, sm, t);
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
-      const int k = t + i * T;
-      v[i] = cscale(sm[spad(k)], __ldg(a.H + k));
-    }
-    __syncthreads();
-    reg_fft<L, 1>(v, sm, t);
-    for (int x = t; x < N; x += T) {
-      const float2 y = sm[spad(x)];
-      lines[lpos(x, C)] = y.x;
-      lines[LF + lpos(x, C)] = y.y;
+      const int x = t + i * T;
+      if (x < N) {
+        lines[lpos(x, C)] = v[i].x;
+        lines[LF + lpos(x, C)] = v[i].y;
+      }
     }
   } else {
     for (int x = t; x < N; x += T) {
