@@ -1039,16 +1039,17 @@ __global__ void __launch_bounds__(TC<L, BLK>::BLOCK, 512 / TC<L, BLK>::BLOCK) k_
     const int c = t + i * T;
     v[i] = (live && c >= a.in_lo && c <= a.in_hi) ? sp[sidx(k, c, L)] : make_float2(0.f, 0.f);
   }
-  reg_fft<L, -1>(v, sm, t);
+  // the forward transform leaves X[t + i*T] in v[i]: the kernel multiply needs no
+  // shared-memory round trip
+  reg_fft<L, -1, kOutRegs>(v, sm, t);
   const int kf = live ? k : 0;
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
     const int c = t + i * T;
     float2 w = __ldg(a.fz + sidx(kf, c, L));
     if (a.conj_fz) w.y = -w.y;
-    v[i] = cscale(cmul(sm[spad(c)], w), a.scale);
+    v[i] = cscale(cmul(v[i], w), a.scale);
   }
-  __syncthreads();
   reg_fft<L, 1>(v, sm, t);
   if (!live) return;
   for (int c = a.out_lo + t; c <= a.out_hi; c += T) sp[sidx(k, c, L)] = sm[spad(c)];
