@@ -202,6 +202,31 @@ int lp_autotune(lp_handle* h, float* R, float* f, int S0, void* stream, float ou
  */
 int lp_debug_fill_scratch(lp_handle* h, float value, void* stream);
 
+/*
+ * Fused vector kernels of the iterative solvers (no single reference
+ * counterpart: they replace the CuPy elementwise updates and float32 sums of
+ * src/lprec/lpmethods.py:62-128).  Device pointers; float32 vectors, float64
+ * accumulation; scalars (num, den, results) are device float64 values, so an
+ * iteration needs no host round trip.  Reductions are deterministic (fixed
+ * grid and summation order).  `work` is caller-provided device scratch of
+ * lp_vec_work_doubles(S) doubles (lp_vec_work_doubles(1) for lp_cg_step);
+ * these calls allocate nothing.
+ *
+ *   lp_vec_dot:  out[s] = sum_i a[s*m + i] * b[s*m + i], s < S
+ *   lp_cg_step:  alpha = (float)(*num / *den); x += alpha p; r -= alpha q;
+ *                *rr = r.r (after the update)
+ *   lp_cg_dir:   p = r + (float)(*num / *den) * p
+ *   lp_em_ratio: g = tomo / (g + eps)
+ *   lp_em_step:  x *= upd / xi
+ */
+int64_t lp_vec_work_doubles(int S);
+int lp_vec_dot(const float* a, const float* b, int64_t m, int S, double* work, double* out, void* stream);
+int lp_cg_step(float* x, float* r, const float* p, const float* q, int64_t n, const double* num, const double* den,
+               double* work, double* rr, void* stream);
+int lp_cg_dir(float* p, const float* r, int64_t n, const double* num, const double* den, void* stream);
+int lp_em_ratio(float* g, const float* tomo, float eps, int64_t n, void* stream);
+int lp_em_step(float* x, const float* upd, const float* xi, int64_t n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

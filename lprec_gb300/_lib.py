@@ -25,7 +25,8 @@ EXPORTS = ("lp_last_error", "lp_version", "lp_precompute_sizes", "lp_precompute"
            "lp_launch_count", "lp_kernel_count", "lp_kernel_name", "lp_set_profiling", "lp_profile_collect",
            "lp_fwd_noalloc", "lp_noalloc_scratch_bytes", "lp_fwd_transpose", "lp_debug_fill_scratch",
            "lp_set_schedule", "lp_get_schedule", "lp_autotune",
-           "lp_precompute_f64", "lp_init_fwd_f64", "lp_init_adj_f64")
+           "lp_precompute_f64", "lp_init_fwd_f64", "lp_init_adj_f64",
+           "lp_vec_work_doubles", "lp_vec_dot", "lp_cg_step", "lp_cg_dir", "lp_em_ratio", "lp_em_step")
 
 
 class LprecError(RuntimeError):
@@ -60,6 +61,12 @@ def lib():
                                       P_f32, P_i32, P_f64, P_i32, P_f64]),
         "lp_init_fwd_f64": (c_int, [c_void_p, P_i32, c_int64, P_f64, c_int64]),
         "lp_init_adj_f64": (c_int, [c_void_p, P_i32, c_int64, P_f64, c_int64]),
+        "lp_vec_work_doubles": (c_int64, [c_int]),
+        "lp_vec_dot": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),
+        "lp_cg_step": (c_int, [c_void_p] * 4 + [c_int64] + [c_void_p] * 5),
+        "lp_cg_dir": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+        "lp_em_ratio": (c_int, [c_void_p, c_void_p, ctypes.c_float, c_int64, c_void_p]),
+        "lp_em_step": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]),
         "lp_create": (c_int, [P_f32, c_int64, c_int, ctypes.POINTER(c_void_p)]),
         "lp_init_fwd": (c_int, [c_void_p, P_i32, c_int64, P_f32, c_int64]),
         "lp_init_adj": (c_int, [c_void_p, P_i32, c_int64, P_f32, c_int64]),
@@ -235,3 +242,30 @@ class Handle:
             self.close()
         except Exception:
             pass
+
+
+# ---- fused solver vector kernels (device pointers; see include/lprec_gb300.h) ----
+def vec_work_doubles(S=1):
+    return int(lib().lp_vec_work_doubles(int(S)))
+
+
+def vec_dot(a, b, m, S, work, out, stream):
+    check(lib().lp_vec_dot(c_void_p(a), c_void_p(b), int(m), int(S), c_void_p(work), c_void_p(out),
+                           c_void_p(stream)))
+
+
+def cg_step(x, r, p, q, n, num, den, work, rr, stream):
+    check(lib().lp_cg_step(c_void_p(x), c_void_p(r), c_void_p(p), c_void_p(q), int(n), c_void_p(num),
+                           c_void_p(den), c_void_p(work), c_void_p(rr), c_void_p(stream)))
+
+
+def cg_dir(p, r, n, num, den, stream):
+    check(lib().lp_cg_dir(c_void_p(p), c_void_p(r), int(n), c_void_p(num), c_void_p(den), c_void_p(stream)))
+
+
+def em_ratio(g, tomo, eps, n, stream):
+    check(lib().lp_em_ratio(c_void_p(g), c_void_p(tomo), float(eps), int(n), c_void_p(stream)))
+
+
+def em_step(x, upd, xi, n, stream):
+    check(lib().lp_em_step(c_void_p(x), c_void_p(upd), c_void_p(xi), int(n), c_void_p(stream)))

@@ -8,8 +8,15 @@ with `init_recon` [S, N, N] and `tomo0` [S, Nproj, N] host arrays (or CUDA
 tensors).  Vectors stay float32 on the GPU, as in the reference; inner
 products and norms are accumulated in float64 (the reference sums float32).
 Work is enqueued on the current torch stream of device `gpu`.
+
+cg, cg_exact and em run their vector updates with the library's fused kernels
+(one pass per update, the inner product it needs in the same pass, float64
+scalars kept on the device, deterministic reductions); the other methods use
+torch elementwise ops.
 """
 import numpy as np
+
+from . import _lib
 
 C_TV = 0.35  # step of the primal-dual TV iterations (lpmethods.py:202)
 
@@ -37,6 +44,45 @@ def _dot_slices(a, b):
 
 def _out(x):
     return x.cpu().numpy()
+
+
+def _stream(x):
+    import torch
+    return torch.cuda.current_stream(x.device).cuda_stream
+
+
+def _cg(lp, init_recon, tomo0, num_iter, gpu, normal_op):
+    """CG on the normal equations A f = normal_op(tomo) with A = normal_op o fwdp; the
+    vector updates, step lengths and residual norms on the device (fused kernels)."""
+    torch = _torch()
+    with torch.cuda.device(gpu):
+        recon = _dev(init_recon, gpu)
+        tomo = _dev(tomo0, gpu)
+        n = recon.numel()
+        st = _stream(recon)
+        b = torch.zeros_like(recon)
+        q = torch.zeros_like(recon)
+        g = torch.zeros_like(tomo)
+        work = torch.empty(_lib.vec_work_doubles(1), dtype=torch.float64, device=recon.device)
+        sc = torch.zeros(3, dtype=torch.float64, device=recon.device)  # rs_old, <p, A p>, rs_new
+        normal_op(b, tomo)
+        lp.fwdp(g, recon, gpu)
+        normal_op(q, g)
+        r = b - q
+        p = r.clone()
+        ptr = [sc.data_ptr() + 8 * i for i in range(3)]
+        _lib.vec_dot(r.data_ptr(), r.data_ptr(), n, 1, work.data_ptr(), ptr[0], st)
+        for i in range(num_iter):
+            lp.fwdp(g, p, gpu)
+            normal_op(q, g)
+            _lib.vec_dot(p.data_ptr(), q.data_ptr(), n, 1, work.data_ptr(), ptr[1], st)
+            # alpha = rs_old / <p, A p>: recon += alpha p, r -= alpha A p, rs_new = <r, r>
+            _lib.cg_step(recon.data_ptr(), r.data_ptr(), p.data_ptr(), q.data_ptr(), n, ptr[0], ptr[1],
+                         work.data_ptr(), ptr[2], st)
+            # p = r + (rs_new / rs_old) p
+            _lib.cg_dir(p.data_ptr(), r.data_ptr(), n, ptr[2], ptr[0], st)
+            sc[0:1].copy_(sc[2:3])
+        return _out(recon)
 
 
 def fbp(lp, init_recon, tomo0, num_iter=0, reg_par=0, gpu=0):
@@ -81,29 +127,7 @@ def grad(lp, init_recon, tomo0, num_iter, reg_par, gpu=0):
 
 def cg(lp, init_recon, tomo0, num_iter, reg_par=0, gpu=0):
     """Conjugate gradients on the normal equations R*R f = R*g (lpmethods.py:62-97)."""
-    torch = _torch()
-    with torch.cuda.device(gpu):
-        recon = _dev(init_recon, gpu)
-        tomo = _dev(tomo0, gpu)
-        b = torch.zeros_like(recon)
-        f = torch.zeros_like(recon)
-        g = torch.zeros_like(tomo)
-        lp.adjp(b, tomo, gpu)
-        lp.fwdp(g, recon, gpu)
-        lp.adjp(f, g, gpu)
-        r = b - f
-        p = r.clone()
-        rsold = _dot(r, r)
-        for i in range(num_iter):
-            lp.fwdp(g, p, gpu)
-            lp.adjp(f, g, gpu)
-            alpha = (rsold / _dot(p, f)).float()
-            recon.add_(alpha * p)
-            r.sub_(alpha * f)
-            rsnew = _dot(r, r)
-            p.mul_((rsnew / rsold).float()).add_(r)
-            rsold = rsnew
-        return _out(recon)
+    return _cg(lp, init_recon, tomo0, num_iter, gpu, lambda out, x: lp.adjp(out, x, gpu))
 
 
 def em(lp, init_recon, tomo0, num_iter, reg_par, gpu=0):
@@ -118,10 +142,12 @@ def em(lp, init_recon, tomo0, num_iter, reg_par, gpu=0):
         lp.adjp(xi, torch.ones_like(tomo), gpu)
         xi.add_(1e-5)
         eps = float(np.float32(reg_par))
+        st = _stream(recon)
         for i in range(num_iter):
             lp.fwdp(g, recon, gpu)
-            lp.adjp(upd, tomo / (g + eps), gpu)
-            recon.mul_(upd / xi)
+            _lib.em_ratio(g.data_ptr(), tomo.data_ptr(), eps, g.numel(), st)   # g = tomo / (g + eps)
+            lp.adjp(upd, g, gpu)
+            _lib.em_step(recon.data_ptr(), upd.data_ptr(), xi.data_ptr(), recon.numel(), st)
         return _out(recon)
 
 
@@ -195,29 +221,7 @@ def tvl1(lp, init_recon, tomo0, num_iter, reg_par, gpu=0):
 # ---------------------------------------------------------------------------
 def cg_exact(lp, init_recon, tomo0, num_iter, reg_par=0, gpu=0):
     """CG on R^T R f = R^T g with R^T the exact transpose (lp.fwdp_T); float64 inner products."""
-    torch = _torch()
-    with torch.cuda.device(gpu):
-        recon = _dev(init_recon, gpu)
-        tomo = _dev(tomo0, gpu)
-        g = torch.zeros_like(tomo)
-        b = torch.zeros_like(recon)
-        q = torch.zeros_like(recon)
-        lp.fwdp_T(b, tomo, gpu)
-        lp.fwdp(g, recon, gpu)
-        lp.fwdp_T(q, g, gpu)
-        r = b - q
-        p = r.clone()
-        rsold = _dot(r, r)
-        for i in range(num_iter):
-            lp.fwdp(g, p, gpu)
-            lp.fwdp_T(q, g, gpu)
-            alpha = (rsold / _dot(p, q)).float()
-            recon.add_(alpha * p)
-            r.sub_(alpha * q)
-            rsnew = _dot(r, r)
-            p.mul_((rsnew / rsold).float()).add_(r)
-            rsold = rsnew
-        return _out(recon)
+    return _cg(lp, init_recon, tomo0, num_iter, gpu, lambda out, x: lp.fwdp_T(out, x, gpu))
 
 
 def tv_gd(lp, init_recon, tomo0, num_iter, reg_par, gpu=0, step=None, eps=1e-8):

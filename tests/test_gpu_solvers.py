@@ -70,3 +70,61 @@ def test_reference_pins_lpmethods(golden_dir):
         assert n - r < 10, (norms, ref)
     # recorded for the design notes: two-sided agreement with the reference's norms
     print("lpmethods norms", norms, "reference", ref)
+
+
+def test_fused_vector_kernels(setup):
+    """lp_vec_dot / lp_cg_step / lp_cg_dir / lp_em_ratio / lp_em_step against float64 NumPy
+    and float32 torch; the reductions are deterministic (same bits on a second call)."""
+    import torch
+    from lprec_gb300 import _lib
+    dev = torch.device("cuda", 0)
+    st = torch.cuda.current_stream().cuda_stream
+    rng = np.random.default_rng(3)
+    S, m = 5, 10007                       # odd length: vector and scalar tails
+    a = rng.standard_normal((S, m)).astype(np.float32)
+    b = rng.standard_normal((S, m)).astype(np.float32)
+    ta, tb = torch.as_tensor(a, device=dev), torch.as_tensor(b, device=dev)
+    work = torch.empty(_lib.vec_work_doubles(S), dtype=torch.float64, device=dev)
+    out = torch.empty(S, dtype=torch.float64, device=dev)
+    _lib.vec_dot(ta.data_ptr(), tb.data_ptr(), m, S, work.data_ptr(), out.data_ptr(), st)
+    ref = np.sum(a.astype(np.float64) * b, axis=1)
+    got = out.cpu().numpy()
+    assert np.allclose(got, ref, rtol=1e-12, atol=1e-9 * np.abs(ref).max()), (got, ref)
+    first = got.copy()
+    _lib.vec_dot(ta.data_ptr(), tb.data_ptr(), m, S, work.data_ptr(), out.data_ptr(), st)
+    assert np.array_equal(out.cpu().numpy(), first)
+    # misaligned views take the scalar path
+    _lib.vec_dot(ta.data_ptr() + 4, tb.data_ptr() + 4, m - 1, 1, work.data_ptr(), out.data_ptr(), st)
+    assert abs(out[0].item() - np.sum(a[0, 1:].astype(np.float64) * b[0, 1:])) < 1e-9 * abs(ref[0]) + 1e-9
+
+    n = S * m
+    x, r = ta.clone().reshape(-1), tb.clone().reshape(-1)
+    p = torch.as_tensor(rng.standard_normal(n).astype(np.float32), device=dev)
+    q = torch.as_tensor(rng.standard_normal(n).astype(np.float32), device=dev)
+    sc = torch.tensor([2.0, 4.0, 0.0], dtype=torch.float64, device=dev)
+    x0, r0 = x.clone(), r.clone()
+    _lib.cg_step(x.data_ptr(), r.data_ptr(), p.data_ptr(), q.data_ptr(), n, sc.data_ptr(), sc.data_ptr() + 8,
+                 work.data_ptr(), sc.data_ptr() + 16, st)
+    alpha = np.float32(0.5)
+    assert torch.allclose(x, x0 + alpha * p, rtol=1e-6, atol=1e-6)
+    assert torch.allclose(r, r0 - alpha * q, rtol=1e-6, atol=1e-6)
+    rr = float(np.sum(r.cpu().numpy().astype(np.float64) ** 2))
+    assert abs(sc[2].item() - rr) < 1e-12 * rr
+    p0 = p.clone()
+    _lib.cg_dir(p.data_ptr(), r.data_ptr(), n, sc.data_ptr() + 8, sc.data_ptr(), st)   # beta = 4 / 2
+    assert torch.allclose(p, r + 2.0 * p0, rtol=1e-6, atol=1e-6)
+    g = torch.rand(n, device=dev) + 0.5
+    tomo = torch.rand(n, device=dev)
+    g0 = g.clone()
+    _lib.em_ratio(g.data_ptr(), tomo.data_ptr(), 0.01, n, st)
+    assert torch.allclose(g, tomo / (g0 + 0.01), rtol=1e-6)
+    xi = torch.rand(n, device=dev) + 0.5
+    x0 = x.clone()
+    _lib.em_step(x.data_ptr(), g.data_ptr(), xi.data_ptr(), n, st)
+    assert torch.allclose(x, x0 * (g / xi), rtol=1e-6, atol=1e-7)
+
+
+def test_cg_deterministic(setup):
+    lp, lpmethods, tr, tomo, S, N = setup
+    x0 = np.zeros((S, N, N), np.float32)
+    assert np.array_equal(lpmethods.cg(lp, x0, tomo, 5, 0, 0), lpmethods.cg(lp, x0, tomo, 5, 0, 0))
