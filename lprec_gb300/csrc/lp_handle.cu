@@ -486,6 +486,7 @@ int lp_create(const float* glpars, int64_t n, int device, lp_handle** out) {
   if (h0.N < 16 || h0.N % 16 != 0 || h0.N > 8192)
     return set_err(LP_ERR_UNSUPPORTED, "lp_create: N=%d must be a multiple of 16 in [16, 8192]", h0.N);
   if (h0.Nth != h0.N || h0.Nrho != 2 * h0.N) return set_err(LP_ERR_ARG, "lp_create: Ntheta/Nrho inconsistent");
+  if (h0.Nslices > 65535) return set_err(LP_ERR_UNSUPPORTED, "lp_create: Nslices=%d above 65535", h0.Nslices);
   if (h0.N0 < 1 || h0.N0 > h0.N || h0.os < 1 || h0.Nproj < 1 || h0.Nproj % h0.os != 0 || h0.Nslices < 1)
     return set_err(LP_ERR_ARG, "lp_create: inconsistent geometry");
   if (h0.N / 2 - h0.cor < 0 || h0.N / 2 - h0.cor + h0.N0 > h0.N)

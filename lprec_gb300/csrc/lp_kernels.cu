@@ -746,7 +746,7 @@ __device__ __forceinline__ float interp_cols(const float* __restrict__ G, int Nr
 
 __global__ void k_adj_lp2cart(AdjLP2CartArgs a) {
   const int s = blockIdx.x;
-  const int p = blockIdx.y * blockDim.x + threadIdx.x;
+  const int p = (blockIdx.z * gridDim.y + blockIdx.y) * blockDim.x + threadIdx.x;
   if (p >= a.npix) return;
   const size_t gs = (size_t)s * a.W2 * a.Nrho;
   float acc = 0.f;
@@ -905,7 +905,9 @@ cudaError_t launch_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st) {
 }
 
 cudaError_t launch_adj_lp2cart(const AdjLP2CartArgs& a, int S, cudaStream_t st) {
-  dim3 grid(S, (a.npix + 255) / 256);
+  // pixel blocks over y and z (grid.y stops at 65535: N0 = 4096 has 65536 blocks of 256)
+  const int nb = (a.npix + 255) / 256;
+  dim3 grid(S, nb < 65535 ? nb : 65535, (nb + 65534) / 65535);
   k_adj_lp2cart<<<grid, 256, 0, st>>>(a);
   return cudaGetLastError();
 }
@@ -925,20 +927,24 @@ struct P2 {
   static constexpr int NSIG = T >= 256 ? 1 : 256 / T;
   static constexpr int BLOCK = T * NSIG;
   static constexpr int SLOTS = reg_fft_slots(L);
+  // resident blocks per SM to size registers for: as many threads as k blocks of 256
+  static constexpr int blocks(int k) { return k * 256 / BLOCK > 0 ? k * 256 / BLOCK : 1; }
 };
 
 // forward, per span: Cartesian -> log-polar gather for column pairs, e^rho, FFT along rho.
 // The disk points of a column form one rho interval (a.ival), so the two
 // columns' points are enumerated as one compact list and gathered in
-// straight-line groups of kGatherUnroll per thread: every thread keeps that
-// many independent texture gathers in flight and no fetch is spent outside the
-// disk.  Values land in the zeroed shared buffer at their rho position (real
-// part: column th, imaginary part: column th+1), from which the register FFT
-// takes its inputs.
-constexpr int kGatherUnroll = 4;
+// straight-line groups of kGatherUnroll per thread (the four quads of a sample
+// in flight together) and no fetch is spent outside the disk.  Values land in
+// the zeroed shared buffer at their rho position (real part: column th,
+// imaginary part: column th+1), from which the register FFT takes its inputs.
+// Measured at N=2048: one sample per group with 5 resident blocks per SM
+// (48 registers) beats 2, 4 or 8 samples per group with 2-4 blocks: the
+// gathers' latency is hidden by more warps rather than by depth per thread.
+constexpr int kGatherUnroll = 1;
 
 template <int L>
-__global__ void __launch_bounds__(256, 3) k_fwd_c2lp_p2(FwdC2LPArgs a) {
+__global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(5)) k_fwd_c2lp_p2(FwdC2LPArgs a) {
   extern __shared__ float2 sm2[];
   constexpr int T = P2<L>::T;
   const int sig = threadIdx.x / T, t = threadIdx.x % T;
@@ -1022,7 +1028,7 @@ struct TC {
 
 // per rho frequency: FFT along theta, multiply by the kernel, inverse; NSIG rows per block
 template <int L, int BLK>
-__global__ void __launch_bounds__(TC<L, BLK>::BLOCK, 512 / TC<L, BLK>::BLOCK) k_theta_conv_p2(ThetaConvArgs a) {
+__global__ void __launch_bounds__(TC<L, BLK>::BLOCK, 768 / TC<L, BLK>::BLOCK) k_theta_conv_p2(ThetaConvArgs a) {
   extern __shared__ float2 sm2[];
   using C = TC<L, BLK>;
   constexpr int T = C::T, KT = C::KT;
@@ -1067,7 +1073,7 @@ __device__ __forceinline__ float2 pair_elem(int p, int L, float2 v0, float2 v1) 
 // forward, per span: two angle rows per signal, theta taps combined in frequency,
 // inverse FFT along rho, rho interpolation into the caller's sinogram
 template <int L>
-__global__ void __launch_bounds__(256, 3) k_fwd_lp2polar_p2(FwdLP2PolarArgs a) {
+__global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(3)) k_fwd_lp2polar_p2(FwdLP2PolarArgs a) {
   extern __shared__ float2 sm2[];
   constexpr int T = P2<L>::T;
   const int sig = threadIdx.x / T, t = threadIdx.x % T;
@@ -1167,7 +1173,7 @@ __global__ void __launch_bounds__(256, 3) k_fwd_lp2polar_p2(FwdLP2PolarArgs a) {
 
 // adjoint ingest for N = L/2: one pair of input rows per block of T threads
 template <int L>
-__global__ void __launch_bounds__(256, 2) k_adj_ingest_p2(AdjIngestArgs a) {
+__global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(3)) k_adj_ingest_p2(AdjIngestArgs a) {
   extern __shared__ float2 sm2[];
   constexpr int T = P2<L>::T;
   const int N = L / 2;
@@ -1229,7 +1235,7 @@ __global__ void __launch_bounds__(256, 2) k_adj_ingest_p2(AdjIngestArgs a) {
 
 // adjoint, per span: polar -> log-polar for a column pair per signal, FFT along rho
 template <int L>
-__global__ void __launch_bounds__(256, 3) k_adj_polar2lp_p2(AdjPolar2LPArgs a) {
+__global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(4)) k_adj_polar2lp_p2(AdjPolar2LPArgs a) {
   extern __shared__ float2 sm2[];
   constexpr int T = P2<L>::T;
   const int N = L / 2;
@@ -1326,7 +1332,7 @@ __global__ void __launch_bounds__(256, 3) k_adj_polar2lp_p2(AdjPolar2LPArgs a) {
 
 // adjoint, per span: inverse FFT along rho for a column pair per signal
 template <int L>
-__global__ void __launch_bounds__(256, 3) k_adj_lpcols_p2(AdjLPColsArgs a) {
+__global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(4)) k_adj_lpcols_p2(AdjLPColsArgs a) {
   extern __shared__ float2 sm2[];
   constexpr int T = P2<L>::T;
   const int sig = threadIdx.x / T, t = threadIdx.x % T;

@@ -151,3 +151,25 @@ def test_tv_gd_decreases_objective(torch_cuda):
     x20 = lpmethods.tv_gd(lp, z, np.float32(tomo), 20, 1e-3, 0)
     o5, o20 = objective(x5.astype(np.float64)), objective(x20.astype(np.float64))
     assert o20 < o5 < o0, (o0, o5, o20)
+
+
+def test_n4096_dot_product(torch_cuda):
+    """N=4096: 8192-point register FFTs in 512-thread blocks.  Forward and exact transpose
+    pass the dot test, the drop-in adjoint passes the reference's looser one (1e-2)."""
+    torch = torch_cuda
+    N0, Nproj, S = 4096, 6144, 1
+    lp = _lp(N0, Nproj, S, N0 // 2, 'cubic')
+    rng = np.random.default_rng(0)
+    f = rng.random((S, N0, N0), dtype=np.float32)
+    g = rng.random((S, Nproj, N0), dtype=np.float32)
+    R = torch.zeros((S, Nproj, N0), device='cuda')
+    lp.fwdp(R, torch.as_tensor(f).cuda(), 0)
+    fT = _fwdT(torch, lp, g)
+    fa = torch.zeros((S, N0, N0), device='cuda')
+    lp.adjp(fa, torch.as_tensor(g).cuda(), 0)
+    torch.cuda.synchronize()
+    Rn = R.cpu().double().numpy()
+    assert np.all(np.isfinite(Rn)) and np.all(np.isfinite(fT))
+    lhs = float(np.sum(Rn * g))
+    assert abs(lhs - float(np.sum(f.astype(np.float64) * fT))) / abs(lhs) < 1e-6
+    assert abs(lhs - float(np.sum(f.astype(np.float64) * fa.cpu().double().numpy()))) / abs(lhs) < 1e-2
