@@ -63,6 +63,36 @@ def _stream(gpu):
     return torch.cuda.current_stream(gpu).cuda_stream
 
 
+def pipeline_chunks(S, c):
+    """Slice counts of the host pipeline's chunks for S slices and chunk size c.
+
+    The first host->device copy and the last device->host copy of a call are not
+    overlapped with any transform, and a chunk's device->host copy must finish
+    within the next chunk's transform (the forward's output is about 1.5x its
+    input).  So the chunks grow from c/16 by doubling, stay at c, and shrink by
+    0.7 per chunk at the end: short exposed copies at both ends, no copy backlog
+    in the tail.  Each chunk costs about 0.1 ms of launch tails at N=2048, which
+    bounds how fine the ramps are."""
+    if S < 1 or c < 1:
+        raise ValueError("need S >= 1 and c >= 1")
+    budget = S
+    head = []
+    u = max(1, c // 16)
+    while u < c and 2 * u <= budget:
+        head.append(u)
+        budget -= u
+        u *= 2
+    tail = []
+    t = int(c * 0.7)
+    while t >= 1:
+        if t <= budget:
+            tail.append(t)
+            budget -= t
+        t = int(t * 0.7)
+    mid = [c] * (budget // c) + ([budget % c] if budget % c else [])
+    return head + sorted(mid + tail, reverse=True)
+
+
 class lpTransform:
     def __init__(self, N, Nproj, Nslices, filter_type, cor, interp_type, precision="fp64"):
         self.N = int(N)
@@ -190,10 +220,13 @@ class lpTransform:
 
     # ---- host arrays, pipelined ---------------------------------------------
     def _host_op(self, op, x, out, gpu, chunk):
-        """Run fwdp/adjp over host arrays in slice chunks, overlapping the
-        host->device copy of chunk i+1 and the device->host copy of chunk i-1
-        with the transform of chunk i (three streams, events between them)."""
+        """Run fwdp/adjp over host arrays in slice chunks (pipeline_chunks), overlapping
+        the host->device copies of the next chunks and the device->host copies of the
+        previous ones with the transform of the current chunk: three streams, three
+        device buffers per side, events between them.  The buffers' last-use events
+        persist across calls, so calls may be issued back to back."""
         import torch
+        NB = 3  # device buffers per side
         h = self._handle(gpu)
         dev = torch.device("cuda", gpu)
         as_numpy = not isinstance(x, torch.Tensor)
@@ -209,24 +242,31 @@ class lpTransform:
             raise TypeError("out must be a torch CPU tensor")
         if tuple(out.shape) != oshape:
             raise ValueError("out has shape %s, expected %s" % (tuple(out.shape), oshape))
-        c = max(1, min(int(chunk or 16), h.Nslices, S))
+        c = max(1, min(int(chunk or 32), h.Nslices, S))
         key = (op, gpu, c) + tuple(xt.shape[1:])
         bufs = self._pipe_bufs.get(key) if hasattr(self, "_pipe_bufs") else None
         if bufs is None:
             if not hasattr(self, "_pipe_bufs"):
                 self._pipe_bufs = {}
-            bufs = ([torch.empty((c,) + tuple(xt.shape[1:]), dtype=torch.float32, device=dev) for _ in range(2)],
-                    [torch.empty((c,) + oshape[1:], dtype=torch.float32, device=dev) for _ in range(2)],
-                    torch.cuda.Stream(dev), torch.cuda.Stream(dev))
+            # device buffers, copy streams, and per buffer the events of its last use
+            # (compute done, copy-out done); the events outlive the call, so the next
+            # call on the same buffers waits for this one's work in flight
+            bufs = ([torch.empty((c,) + tuple(xt.shape[1:]), dtype=torch.float32, device=dev) for _ in range(NB)],
+                    [torch.empty((c,) + oshape[1:], dtype=torch.float32, device=dev) for _ in range(NB)],
+                    torch.cuda.Stream(dev), torch.cuda.Stream(dev), [None] * NB, [None] * NB, [0])
             self._pipe_bufs[key] = bufs
-        ins, outs, s_in, s_out = bufs
+        ins, outs, s_in, s_out, done_comp, done_out, nxt = bufs
         comp = torch.cuda.current_stream(dev)
-        done_comp = [None, None]
-        done_out = [None, None]
-        n = (S + c - 1) // c
+        # the copies in read host memory that work already on the caller's stream
+        # may write (e.g. the previous call's output)
+        s_in.wait_stream(comp)
+        sizes = pipeline_chunks(S, c)
+        n = len(sizes)
+        b = 0
         for i in range(n):
-            a, b = i * c, min(S, (i + 1) * c)
-            k = i % 2
+            a, b = b, b + sizes[i]
+            k = nxt[0]
+            nxt[0] = (k + 1) % NB
             with torch.cuda.stream(s_in):
                 if done_comp[k] is not None:
                     s_in.wait_event(done_comp[k])       # buffer's previous chunk consumed
@@ -249,9 +289,7 @@ class lpTransform:
                 ev_o = torch.cuda.Event()
                 ev_o.record(s_out)
             done_out[k] = ev_o
-        for e in done_out:
-            if e is not None:
-                comp.wait_event(e)
+        comp.wait_event(done_out[(nxt[0] - 1) % NB])   # the copies out run in order
         if as_numpy:
             torch.cuda.current_stream(dev).synchronize()
             return out.numpy()

@@ -273,6 +273,41 @@ def test_host_array_pipeline(torch_cuda):
         assert np.array_equal(fh[s], fd.cpu().numpy()[0])
 
 
+def test_host_calls_back_to_back(torch_cuda):
+    """Host calls issued without a synchronisation in between share the pipeline's
+    device buffers: each call waits for the previous call's compute and copy-out of a
+    buffer before reusing it, so every call's result equals the device path's."""
+    torch = torch_cuda
+    from lprec_gb300.lpTransform import lpTransform
+    S, N, Nproj, calls = 24, 256, 384, 4
+    lp = lpTransform(N, Nproj, S, 'ramp', N / 2, 'cubic')
+    lp.precompute(1)
+    lp.initcmem(1, 0)
+    rng = np.random.default_rng(5)
+    fs = [torch.from_numpy(rng.random((S, N, N), dtype=np.float32)).pin_memory() for _ in range(calls)]
+    Rs = [torch.from_numpy(rng.random((S, Nproj, N), dtype=np.float32)).pin_memory() for _ in range(calls)]
+    Routs = [torch.empty((S, Nproj, N)).pin_memory() for _ in range(calls)]
+    fouts = [torch.empty((S, N, N)).pin_memory() for _ in range(calls)]
+    for i in range(calls):
+        lp.fwd(fs[i], 0, out=Routs[i], chunk=4)
+        lp.adj(Rs[i], 0, out=fouts[i], chunk=4)
+    # chained: the adjoint's host input is the forward's host output, still being copied
+    fc = lp.adj(lp.fwd(fs[0], 0, chunk=8), 0, chunk=8)
+    torch.cuda.synchronize()
+    Rd = torch.empty((S, Nproj, N), device='cuda')
+    fd = torch.empty((S, N, N), device='cuda')
+    lp.fwdp(Rd, fs[0].cuda(), 0)
+    lp.adjp(fd, Rd, 0)
+    assert torch.equal(fc, fd.cpu())
+    for i in range(calls):
+        Rd = torch.empty((S, Nproj, N), device='cuda')
+        fd = torch.empty((S, N, N), device='cuda')
+        lp.fwdp(Rd, fs[i].cuda(), 0)
+        lp.adjp(fd, Rs[i].cuda(), 0)
+        assert torch.equal(Routs[i], Rd.cpu()), i
+        assert torch.equal(fouts[i], fd.cpu()), i
+
+
 def test_uneven_batch_graph(torch_cuda):
     """Requests of different geometry in one CUDA graph == per-request calls."""
     torch = torch_cuda

@@ -171,3 +171,19 @@ def test_graph_watchdog_times_out_on_host():
     t[0] = 0.0
     wait_event(After(3), 1.0, poll_s=0.01, clock=clock, sleep=sleep)
     assert t[0] < 0.05
+
+
+@pytest.mark.parametrize("S,c", [(128, 32), (128, 16), (7, 3), (1, 32), (5, 1), (100, 32), (33, 32), (128, 64)])
+def test_pipeline_chunks(S, c):
+    """The host pipeline's chunk sizes cover the slices once, never above c, growing
+    to their largest and shrinking after it (short first and last copies)."""
+    from lprec_gb300.lpTransform import pipeline_chunks
+    sizes = pipeline_chunks(S, c)
+    assert sum(sizes) == S and max(sizes) <= c and min(sizes) >= 1
+    top = sizes.index(max(sizes))
+    assert sizes[:top + 1] == sorted(sizes[:top + 1])
+    assert sizes[top:] == sorted(sizes[top:], reverse=True)
+    if S >= 2 * c >= 16:
+        assert sizes[0] <= c // 8 and sizes[-1] <= c // 8
+    with pytest.raises(ValueError):
+        pipeline_chunks(0, c)
