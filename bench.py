@@ -728,7 +728,8 @@ def run_report(args):
 def run_large_solve(torch, dev):
     """128 slices, N=2048, Nproj=3000, 30-ellipse phantoms (seed 3), 1 % Gaussian noise:
     FBP (shepp-logan), then 30 CG and 30 EM iterations (unfiltered adjoint) on the GPU,
-    timed with CUDA events; the results come back to the host inside the timing."""
+    timed with CUDA events; the results come back to the host inside the timing.  Also
+    30 TV iterations, timed separately."""
     from lprec_gb300.lpTransform import lpTransform
     from lprec_gb300 import lpmethods
     N, Nproj, S = 2048, 3000, 128
@@ -761,10 +762,13 @@ def run_large_solve(torch, dev):
     Rp = R.abs()
     t_em, xe = timed(lambda: lpmethods.em(lpn, x0 + 1e-3, Rp, 30, 0.01, dev))
     total = t_fbp + t_cg + t_em
+    # not part of the FBP+CG+EM sequence: 30 TV iterations (lambda 1e-3) on the same data
+    t_tv, xt = timed(lambda: lpmethods.tv(lpn, x0, R, 30, 1e-3, dev))
     return {"fbp_ms": t_fbp, "cg30_ms": t_cg, "em30_ms": t_em, "total_ms": total,
             "slices_per_s": S / (total / 1000.0),
             "cg_ms_per_iteration": t_cg / 30, "em_ms_per_iteration": t_em / 30,
-            "finite": bool(np.isfinite(xc).all() and np.isfinite(xe).all())}
+            "tv30_ms": t_tv, "tv_ms_per_iteration": t_tv / 30,
+            "finite": bool(np.isfinite(xc).all() and np.isfinite(xe).all() and np.isfinite(xt).all())}
 
 
 def main():

@@ -227,6 +227,38 @@ int lp_cg_dir(float* p, const float* r, int64_t n, const double* num, const doub
 int lp_em_ratio(float* g, const float* tomo, float eps, int64_t n, void* stream);
 int lp_em_step(float* x, const float* upd, const float* xi, int64_t n, void* stream);
 
+/*
+ * Fused updates of the total-variation solvers tv, tve and tvl1 (one
+ * Chambolle-Pock iteration = lp_tv_prox0, lp_fwd, lp_tv_prox1, lp_adj,
+ * lp_tv_recon).  Each replaces a group of the reference's CuPy statements
+ * (src/lprec/lpmethods.py:158-178 for tv, :209-232 tve, :264-286 tvl1) by one
+ * pass, computed in the statements' float32 operation order without fused
+ * multiply-adds, so results equal the statement sequence's bit for bit.  Images
+ * are [S][ny][nx] float32, sinograms n floats; c and lam are the reference's
+ * Python scalars, rounded to float32 where they meet an array (1 + c and 4*c
+ * rounded once).  Device pointers; nothing is allocated.
+ *
+ *   lp_tv_prox0: prox0x[.., :-1] += c*(recon[.., 1:] - recon[.., :-1]) along x,
+ *                prox0y likewise along y; both divided by
+ *                maximum(1, sqrt(prox0x^2 + prox0y^2)/lam)       (:158-163)
+ *   lp_tv_prox1: prox1 <- the data term's proximal step (mode):
+ *                LP_TV_L2      (prox1 + c g - c tomo)/(1 + c)     (:166)
+ *                LP_TV_ENTROPY u = prox1 + c g; t = 0.5(u - 1 + sqrt((u-1)^2 + 4c tomo));
+ *                              u - max(t, 0)                      (:218-220)
+ *                LP_TV_L1      t = prox1 + c g - c tomo; t - max(|t| - 1, 0) sign(t) (:272-275)
+ *   lp_tv_recon: div0 from backward differences of prox0x (x) and prox0y (y);
+ *                recon0 <- recon0 - c p + c div0; recon <- 2 recon0(new) - recon0(old)
+ *                                                                 (:169-178)
+ */
+#define LP_TV_L2 0
+#define LP_TV_ENTROPY 1
+#define LP_TV_L1 2
+int lp_tv_prox0(float* prox0x, float* prox0y, const float* recon, int S, int ny, int nx, double c, double lam,
+                void* stream);
+int lp_tv_prox1(float* prox1, const float* g, const float* tomo, int64_t n, double c, int mode, void* stream);
+int lp_tv_recon(float* recon0, float* recon, const float* p, const float* prox0x, const float* prox0y, int S, int ny,
+                int nx, double c, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -26,7 +26,8 @@ EXPORTS = ("lp_last_error", "lp_version", "lp_precompute_sizes", "lp_precompute"
            "lp_fwd_noalloc", "lp_noalloc_scratch_bytes", "lp_fwd_transpose", "lp_debug_fill_scratch",
            "lp_set_schedule", "lp_get_schedule", "lp_autotune",
            "lp_precompute_f64", "lp_init_fwd_f64", "lp_init_adj_f64",
-           "lp_vec_work_doubles", "lp_vec_dot", "lp_cg_step", "lp_cg_dir", "lp_em_ratio", "lp_em_step")
+           "lp_vec_work_doubles", "lp_vec_dot", "lp_cg_step", "lp_cg_dir", "lp_em_ratio", "lp_em_step",
+           "lp_tv_prox0", "lp_tv_prox1", "lp_tv_recon")
 
 
 class LprecError(RuntimeError):
@@ -67,6 +68,9 @@ def lib():
         "lp_cg_dir": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
         "lp_em_ratio": (c_int, [c_void_p, c_void_p, ctypes.c_float, c_int64, c_void_p]),
         "lp_em_step": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]),
+        "lp_tv_prox0": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_double, c_double, c_void_p]),
+        "lp_tv_prox1": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_double, c_int, c_void_p]),
+        "lp_tv_recon": (c_int, [c_void_p] * 5 + [c_int, c_int, c_int, c_double, c_void_p]),
         "lp_create": (c_int, [P_f32, c_int64, c_int, ctypes.POINTER(c_void_p)]),
         "lp_init_fwd": (c_int, [c_void_p, P_i32, c_int64, P_f32, c_int64]),
         "lp_init_adj": (c_int, [c_void_p, P_i32, c_int64, P_f32, c_int64]),
@@ -269,3 +273,21 @@ def em_ratio(g, tomo, eps, n, stream):
 
 def em_step(x, upd, xi, n, stream):
     check(lib().lp_em_step(c_void_p(x), c_void_p(upd), c_void_p(xi), int(n), c_void_p(stream)))
+
+
+TV_MODES = {"tv": 0, "tve": 1, "tvl1": 2}  # LP_TV_L2, LP_TV_ENTROPY, LP_TV_L1
+
+
+def tv_prox0(prox0x, prox0y, recon, S, ny, nx, c, lam, stream):
+    check(lib().lp_tv_prox0(c_void_p(prox0x), c_void_p(prox0y), c_void_p(recon), int(S), int(ny), int(nx),
+                            float(c), float(lam), c_void_p(stream)))
+
+
+def tv_prox1(prox1, g, tomo, n, c, mode, stream):
+    check(lib().lp_tv_prox1(c_void_p(prox1), c_void_p(g), c_void_p(tomo), int(n), float(c), TV_MODES[mode],
+                            c_void_p(stream)))
+
+
+def tv_recon(recon0, recon, p, prox0x, prox0y, S, ny, nx, c, stream):
+    check(lib().lp_tv_recon(c_void_p(recon0), c_void_p(recon), c_void_p(p), c_void_p(prox0x), c_void_p(prox0y),
+                            int(S), int(ny), int(nx), float(c), c_void_p(stream)))

@@ -11,7 +11,8 @@ Work is enqueued on the current torch stream of device `gpu`.
 
 cg, cg_exact and em run their vector updates with the library's fused kernels
 (one pass per update, the inner product it needs in the same pass, float64
-scalars kept on the device, deterministic reductions); the other methods use
+scalars kept on the device, deterministic reductions); tv, tve and tvl1 with
+the fused TV kernels (three passes per iteration besides fwdp/adjp); grad uses
 torch elementwise ops.
 """
 import numpy as np
@@ -151,67 +152,47 @@ def em(lp, init_recon, tomo0, num_iter, reg_par, gpu=0):
         return _out(recon)
 
 
-def _tv_family(lp, init_recon, tomo0, num_iter, reg_par, gpu, prox):
-    """Chambolle-Pock iterations shared by tv, tve, tvl1 (lpmethods.py:131-288)."""
+def _tv_family(lp, init_recon, tomo0, num_iter, reg_par, gpu, mode):
+    """Chambolle-Pock iterations shared by tv, tve, tvl1 (lpmethods.py:131-288): per
+    iteration the TV dual update, fwdp, the data-term dual update, adjp and the
+    divergence + primal update, each update one fused pass (results equal the
+    reference's float32 statement sequence bit for bit)."""
     torch = _torch()
     with torch.cuda.device(gpu):
         recon = _dev(init_recon, gpu)
         tomo = _dev(tomo0, gpu)
+        S, ny, nx = recon.shape
         g = torch.zeros_like(tomo)
         p = torch.zeros_like(recon)
         recon0 = recon.clone()
         prox0x = torch.zeros_like(recon)
         prox0y = torch.zeros_like(recon)
-        div0 = torch.zeros_like(recon)
         prox1 = torch.zeros_like(tomo)
-        lam = reg_par
         c = C_TV
+        st = _stream(recon)
         for i in range(num_iter):
-            prox0x[:, :, :-1] += c * (recon[:, :, 1:] - recon[:, :, :-1])
-            prox0y[:, :-1, :] += c * (recon[:, 1:, :] - recon[:, :-1, :])
-            nprox = torch.clamp(torch.sqrt(prox0x * prox0x + prox0y * prox0y) / lam, min=1)
-            prox0x = prox0x / nprox
-            prox0y = prox0y / nprox
+            _lib.tv_prox0(prox0x.data_ptr(), prox0y.data_ptr(), recon.data_ptr(), S, ny, nx, c, reg_par, st)
             lp.fwdp(g, recon, gpu)
-            prox1 = prox(prox1, g, tomo, c)
-            recon = recon0
-            div0[:, :, 1:] = prox0x[:, :, 1:] - prox0x[:, :, :-1]
-            div0[:, :, 0] = prox0x[:, :, 0]
-            div0[:, 1:, :] += prox0y[:, 1:, :] - prox0y[:, :-1, :]
-            div0[:, 0, :] += prox0y[:, 0, :]
+            _lib.tv_prox1(prox1.data_ptr(), g.data_ptr(), tomo.data_ptr(), g.numel(), c, mode, st)
             lp.adjp(p, prox1, gpu)
-            recon0 = recon0 - c * p + c * div0
-            recon = 2 * recon0 - recon
+            _lib.tv_recon(recon0.data_ptr(), recon.data_ptr(), p.data_ptr(), prox0x.data_ptr(), prox0y.data_ptr(),
+                          S, ny, nx, c, st)
         return _out(recon)
 
 
 def tv(lp, init_recon, tomo0, num_iter, reg_par, gpu=0):
     """1/2||R f - g||^2 + reg_par TV(f) (lpmethods.py:131-180)."""
-    return _tv_family(lp, init_recon, tomo0, num_iter, reg_par, gpu,
-                      lambda p1, g, tomo, c: (p1 + c * g - c * tomo) / (1 + c))
+    return _tv_family(lp, init_recon, tomo0, num_iter, reg_par, gpu, "tv")
 
 
 def tve(lp, init_recon, tomo0, num_iter, reg_par, gpu=0):
     """sum(R f - g log R f) + reg_par TV(f) (lpmethods.py:182-230)."""
-    torch = _torch()
-
-    def prox(p1, g, tomo, c):
-        t = p1 + c * g - 1
-        tmp = 0.5 * (t + torch.sqrt(t * t + 4 * c * tomo))
-        tmp = torch.clamp(tmp, min=0)
-        return p1 + c * g - tmp
-    return _tv_family(lp, init_recon, tomo0, num_iter, reg_par, gpu, prox)
+    return _tv_family(lp, init_recon, tomo0, num_iter, reg_par, gpu, "tve")
 
 
 def tvl1(lp, init_recon, tomo0, num_iter, reg_par, gpu=0):
     """||R f - g||_1 + reg_par TV(f) (lpmethods.py:232-288)."""
-    torch = _torch()
-
-    def prox(p1, g, tomo, c):
-        tmp = p1 + c * g - c * tomo
-        tmp2 = torch.clamp(tmp.abs() - 1, min=0)
-        return tmp - tmp2 * torch.sign(tmp)
-    return _tv_family(lp, init_recon, tomo0, num_iter, reg_par, gpu, prox)
+    return _tv_family(lp, init_recon, tomo0, num_iter, reg_par, gpu, "tvl1")
 
 
 # ---------------------------------------------------------------------------

@@ -128,3 +128,118 @@ def test_cg_deterministic(setup):
     lp, lpmethods, tr, tomo, S, N = setup
     x0 = np.zeros((S, N, N), np.float32)
     assert np.array_equal(lpmethods.cg(lp, x0, tomo, 5, 0, 0), lpmethods.cg(lp, x0, tomo, 5, 0, 0))
+
+
+def _tv_statements(lp, init, tomo0, num_iter, lam, mode):
+    """The reference's tv/tve/tvl1 loop (lpmethods.py:155-178, 206-232, 261-286) as
+    plain torch float32 statements, one elementwise op at a time.  Divisions use
+    device scalars: torch multiplies by the reciprocal when the divisor is a Python
+    number, CuPy (the reference) divides."""
+    import torch
+    dev = 'cuda'
+    recon = torch.as_tensor(init).to(dev)
+    tomo = torch.as_tensor(tomo0).to(dev)
+    g = torch.zeros_like(tomo)
+    p = torch.zeros_like(recon)
+    recon0 = recon.clone()
+    prox0x = torch.zeros_like(recon)
+    prox0y = torch.zeros_like(recon)
+    div0 = torch.zeros_like(recon)
+    prox1 = torch.zeros_like(tomo)
+    c = 0.35
+    lam_d = torch.tensor(lam, dtype=torch.float32, device=dev)
+    c1_d = torch.tensor(1 + c, dtype=torch.float32, device=dev)
+    for _ in range(num_iter):
+        prox0x[:, :, :-1] += c * (recon[:, :, 1:] - recon[:, :, :-1])
+        prox0y[:, :-1, :] += c * (recon[:, 1:, :] - recon[:, :-1, :])
+        nprox = torch.clamp(torch.sqrt(prox0x * prox0x + prox0y * prox0y) / lam_d, min=1)
+        prox0x = prox0x / nprox
+        prox0y = prox0y / nprox
+        lp.fwdp(g, recon, 0)
+        if mode == 'tv':
+            prox1 = (prox1 + c * g - c * tomo) / c1_d
+        elif mode == 'tve':
+            tmp = 0.5 * (prox1 + c * g - 1 + torch.sqrt((prox1 + c * g - 1) * (prox1 + c * g - 1) + 4 * c * tomo))
+            tmp[tmp < 0] = 0
+            prox1 = prox1 + c * g - tmp
+        else:
+            tmp = prox1 + c * g - c * tomo
+            tmp2 = torch.abs(tmp) - 1
+            tmp2[tmp2 < 0] = 0
+            prox1 = tmp - tmp2 * torch.sign(tmp)
+        recon = recon0
+        div0[:, :, 1:] = prox0x[:, :, 1:] - prox0x[:, :, :-1]
+        div0[:, :, 0] = prox0x[:, :, 0]
+        div0[:, 1:, :] += prox0y[:, 1:, :] - prox0y[:, :-1, :]
+        div0[:, 0, :] += prox0y[:, 0, :]
+        lp.adjp(p, prox1, 0)
+        recon0 = recon0 - c * p + c * div0
+        recon = 2 * recon0 - recon
+    return recon.cpu().numpy()
+
+
+@pytest.mark.parametrize("mode", ["tv", "tve", "tvl1"])
+def test_tv_fused_equals_statements(setup, mode):
+    """The fused TV passes reproduce the reference's float32 statement sequence bit
+    for bit (same operation order, no fused multiply-adds)."""
+    lp, lpmethods, tr, tomo, S, N = setup
+    rng = np.random.default_rng(11)
+    x0 = (0.1 * rng.standard_normal((S, N, N))).astype(np.float32)
+    t = np.abs(tomo) if mode == 'tve' else tomo
+    got = getattr(lpmethods, mode)(lp, x0, t, 6, 1e-3, 0)
+    want = _tv_statements(lp, x0, t, 6, 1e-3, mode)
+    assert np.array_equal(got, want), float(np.max(np.abs(got - want)))
+
+
+@pytest.mark.parametrize("shape,offset", [((2, 5, 37), 0), ((2, 8, 64), 0), ((3, 6, 12), 1)])
+def test_tv_kernels_shapes(setup, shape, offset):
+    """The TV passes on their own, 16-byte and scalar paths (odd widths, unaligned
+    pointers), against the statements they replace, bit for bit."""
+    import torch
+    from lprec_gb300 import _lib
+    S, ny, nx = shape
+    gen = torch.Generator(device='cuda').manual_seed(5)
+    n = S * ny * nx
+
+    def buf():
+        return torch.randn(n + offset, device='cuda', generator=gen)[offset:].view(S, ny, nx)
+    c, lam = 0.35, 0.7
+    lam_d = torch.tensor(lam, dtype=torch.float32, device='cuda')
+    r, px, py, p = buf(), buf(), buf(), buf()
+    st = torch.cuda.current_stream().cuda_stream
+    wx, wy = px.clone(), py.clone()
+    wx[:, :, :-1] += c * (r[:, :, 1:] - r[:, :, :-1])
+    wy[:, :-1, :] += c * (r[:, 1:, :] - r[:, :-1, :])
+    nprox = torch.clamp(torch.sqrt(wx * wx + wy * wy) / lam_d, min=1)
+    wx, wy = wx / nprox, wy / nprox
+    _lib.tv_prox0(px.data_ptr(), py.data_ptr(), r.data_ptr(), S, ny, nx, c, lam, st)
+    assert torch.equal(px, wx) and torch.equal(py, wy)
+
+    r0 = buf()
+    div0 = torch.zeros_like(r0)
+    div0[:, :, 1:] = px[:, :, 1:] - px[:, :, :-1]
+    div0[:, :, 0] = px[:, :, 0]
+    div0[:, 1:, :] += py[:, 1:, :] - py[:, :-1, :]
+    div0[:, 0, :] += py[:, 0, :]
+    w0 = r0 - c * p + c * div0
+    w = 2 * w0 - r0
+    out = torch.empty_like(r0)
+    _lib.tv_recon(r0.data_ptr(), out.data_ptr(), p.data_ptr(), px.data_ptr(), py.data_ptr(), S, ny, nx, c, st)
+    assert torch.equal(r0, w0) and torch.equal(out, w)
+
+    c1_d = torch.tensor(1 + c, dtype=torch.float32, device='cuda')
+    for mode in ("tv", "tve", "tvl1"):
+        q, g, t = buf().flatten(), buf().flatten(), buf().abs().flatten()
+        if mode == "tv":
+            want = (q + c * g - c * t) / c1_d
+        elif mode == "tve":
+            tmp = 0.5 * (q + c * g - 1 + torch.sqrt((q + c * g - 1) * (q + c * g - 1) + 4 * c * t))
+            tmp[tmp < 0] = 0
+            want = q + c * g - tmp
+        else:
+            tmp = q + c * g - c * t
+            tmp2 = torch.abs(tmp) - 1
+            tmp2[tmp2 < 0] = 0
+            want = tmp - tmp2 * torch.sign(tmp)
+        _lib.tv_prox1(q.data_ptr(), g.data_ptr(), t.data_ptr(), n, c, mode, st)
+        assert torch.equal(q, want), mode
