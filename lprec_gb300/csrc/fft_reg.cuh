@@ -34,12 +34,9 @@ __device__ __forceinline__ void reg_bfly(float2* x) {
   else bfly2<DIR>(x);
 }
 
-// twiddle powers w^i, i < R, of w = exp(DIR*2*pi*i*f) with f = k/(Ns*R)
-template <int R, int DIR>
-__device__ __forceinline__ void twiddle_powers(float f, float2* w) {
-  float s1, c1;
-  sincospif(2.0f * f, &s1, &c1);
-  const float2 w1 = make_float2(c1, DIR * s1);
+// twiddle powers w^i, i < R, from w1 = w and (R >= 8) w4 = w^4
+template <int R>
+__device__ __forceinline__ void twiddle_powers_from(float2 w1, float2 w4, float2* w) {
   w[0] = make_float2(1.f, 0.f);
   w[1] = w1;
   if constexpr (R >= 4) {
@@ -47,9 +44,6 @@ __device__ __forceinline__ void twiddle_powers(float f, float2* w) {
     w[3] = cmul(w[2], w1);
   }
   if constexpr (R >= 8) {
-    float s4, c4;
-    sincospif(8.0f * f, &s4, &c4);
-    const float2 w4 = make_float2(c4, DIR * s4);
     w[4] = w4;
     w[5] = cmul(w4, w1);
     w[6] = cmul(w4, w[2]);
@@ -66,6 +60,30 @@ __device__ __forceinline__ void twiddle_powers(float f, float2* w) {
   }
 }
 
+// twiddle powers w^i, i < R, of w = exp(DIR*2*pi*i*f) with f = k/(Ns*R)
+template <int R, int DIR>
+__device__ __forceinline__ void twiddle_powers(float f, float2* w) {
+  float s1, c1;
+  sincospif(2.0f * f, &s1, &c1);
+  float2 w4 = make_float2(1.f, 0.f);
+  if constexpr (R >= 8) {
+    float s4, c4;
+    sincospif(8.0f * f, &s4, &c4);
+    w4 = make_float2(c4, DIR * s4);
+  }
+  twiddle_powers_from<R>(make_float2(c1, DIR * s1), w4, w);
+}
+
+// cos(pi*m/8) and sin(pi*m/8), m = 0..7 (m is a compile-time constant at every use)
+__device__ __forceinline__ float cos_pi8(int m) {
+  return m == 0 ? 1.f : m == 1 ? LP_C8 : m == 2 ? LP_R2 : m == 3 ? LP_S8
+       : m == 4 ? 0.f : m == 5 ? -LP_S8 : m == 6 ? -LP_R2 : -LP_C8;
+}
+__device__ __forceinline__ float sin_pi8(int m) {
+  return m == 0 ? 0.f : m == 1 ? LP_S8 : m == 2 ? LP_R2 : m == 3 ? LP_C8
+       : m == 4 ? 1.f : m == 5 ? LP_C8 : m == 6 ? LP_R2 : LP_S8;
+}
+
 // where the last stage leaves the transform
 enum RegFftOut { kOutSmem = 0, kOutPlanar = 1, kOutRegs = 2, kOutCall = 3 };
 
@@ -79,6 +97,7 @@ __device__ __forceinline__ void reg_stage(float2 (&v)[16], float2* sm, int t, co
   constexpr int NB = 16 / R;
   static_assert((OUT != kOutRegs && OUT != kOutCall) || (LAST && NS * R == L),
                 "register or sink output only from a last stage spanning L");
+  float2 w1_0 = make_float2(1.f, 0.f), w4_0 = make_float2(1.f, 0.f);  // butterfly 0's w and w^4
 #pragma unroll
   for (int m = 0; m < NB; ++m) {
     const int jp = t + m * T;
@@ -88,7 +107,27 @@ __device__ __forceinline__ void reg_stage(float2 (&v)[16], float2* sm, int t, co
     for (int i = 0; i < R; ++i) x[i] = v[m + i * NB];
     if constexpr (NS > 1) {
       float2 w[R];
-      twiddle_powers<R, DIR>((float)k * (1.0f / (float)(NS * R)), w);
+      if constexpr (NB > 1) {
+        // NB > 1 only in a last stage (R < 16, NS*R = L), where k = t + m*T: butterfly m's
+        // base twiddle is butterfly 0's times exp(DIR*i*pi*m/8), its fourth power butterfly
+        // 0's times (DIR*i)^m -- one product instead of two sincospif
+        static_assert(NS * R == L, "multi-butterfly stages end the transform");
+        if (m == 0) {
+          twiddle_powers<R, DIR>((float)k * (1.0f / (float)(NS * R)), w);
+          w1_0 = w[1];
+          if constexpr (R >= 8) w4_0 = w[4];
+        } else {
+          const float2 w1 = rot<DIR>(w1_0, cos_pi8(m), sin_pi8(m));
+          float2 w4 = w4_0;
+          if constexpr (R >= 8) {
+#pragma unroll
+            for (int j = 0; j < (m & 3); ++j) w4 = mul_i<DIR>(w4);
+          }
+          twiddle_powers_from<R>(w1, w4, w);
+        }
+      } else {
+        twiddle_powers<R, DIR>((float)k * (1.0f / (float)(NS * R)), w);
+      }
 #pragma unroll
       for (int i = 1; i < R; ++i) x[i] = cmul(x[i], w[i]);
     }

@@ -241,9 +241,10 @@ static void free_adj(AdjDev* a) {
 }
 
 // Hermitian extension of the half kernel fZ[Nrho][Nth/2+1] (cuFFT R2C layout,
-// lpRgpu.cu:28-34) to the rho-half / theta-full layout [Nrho/2+1][Nth].  Only
-// the Hermitian part of the kernel affects C2R output, so the kt = 0 and
-// kt = Nth/2 columns are symmetrised.
+// lpRgpu.cu:28-34) to the rho-half / theta-full layout [Nrho/2+1][Nth], times the
+// 1/(Nrho*Nth) that the reference applies in its kernel multiply (lpRgpu.cu:274,
+// 318; a power of two at power-of-two sizes, so the products are unchanged).  Only the Hermitian part of the kernel affects C2R output, so the
+// kt = 0 and kt = Nth/2 columns are symmetrised.
 template <typename Real>
 static std::vector<float2> extend_kernel(const Real* v, int Nrho, int Nth) {
   const int nh = Nth / 2 + 1;
@@ -252,6 +253,7 @@ static std::vector<float2> extend_kernel(const Real* v, int Nrho, int Nth) {
     const size_t i = 2 * ((size_t)kr * nh + kt);
     return std::make_pair((double)v[i], (double)v[i + 1]);
   };
+  const double scale = 1.0 / ((double)Nrho * (double)Nth);
   std::vector<float2> out(spec_slice(Nk, Nth), make_float2(0.f, 0.f));
   for (int kr = 0; kr < Nk; ++kr) {
     const int mr = (Nrho - kr) % Nrho;
@@ -271,7 +273,7 @@ static std::vector<float2> extend_kernel(const Real* v, int Nrho, int Nth) {
         re = b.first;
         im = -b.second;
       }
-      out[sidx(kr, kt, Nth)] = make_float2((float)re, (float)im);
+      out[sidx(kr, kt, Nth)] = make_float2((float)(re * scale), (float)(im * scale));
     }
   }
   return out;
@@ -1001,7 +1003,7 @@ static int fwd_slices(lp_handle* h, float* R, const float* f, int s0, int n, cud
     FwdC2LPArgs a1{fbuf, spec, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, h->cubic,
                    h->plan_rho, tx, F->ival.p, F->dlo, F->dhi, F->F, F->fsc};
     CUDA_TRY(launch(h, K_FWD_C2LP, st, [&] { return launch_fwd_c2lp(a1, n, st); }));
-    ThetaConvArgs a2{spec, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), F->dlo, F->dhi,
+    ThetaConvArgs a2{spec, F->fz.p, h->Nth, h->Nk, F->dlo, F->dhi,
                      F->lo & ~1, std::min(F->hi | 1, h->Nth - 1), 0, h->plan_th, h->fwd_tblock};
     CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, n, st); }));
     FwdLP2PolarArgs a3{spec, R, F->thc.p, F->rhoc.p, F->rows[k].p, F->nrows[k], h->N, h->N0, h->Nth,
@@ -1038,7 +1040,7 @@ static int adj_slices(lp_handle* h, float* f, const float* R, int s0, int n, cud
     AdjPolar2LPArgs a1{rbuf, spec, A->ta[k].p, A->sx[k].p, A->woff[k].p, A->wpt[k].p, h->N, h->Nth,
                        h->Nrho, h->Nk, h->Nproj, h->cubic, A->clo[k], A->chi[k], h->plan_rho, A->F, A->fsc};
     CUDA_TRY(launch(h, K_ADJ_POLAR2LP, st, [&] { return launch_adj_polar2lp(a1, n, st); }));
-    ThetaConvArgs a2{spec, A->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), A->clo[k],
+    ThetaConvArgs a2{spec, A->fz.p, h->Nth, h->Nk, A->clo[k],
                      A->chi[k], A->lo2, A->hi2, 0, h->plan_th, h->adj_tblock};
     CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, n, st); }));
     AdjLPColsArgs a3{spec, G[k], h->Nth, h->Nrho, h->Nk, A->lo2, A->hi2, A->W2, h->plan_rho,
@@ -1085,7 +1087,7 @@ int lp_fwd_transpose(lp_handle* h, float* f, const float* R, int S0, void* strea
                      h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, F->lo, kTransposeCW, h->plan_rho,
                      F->F, F->fsc};
     CUDA_TRY(launch(h, K_FWDT_POLAR, st, [&] { return launch_fwdT_polar(a1, S0, F->nblk[k], st); }));
-    ThetaConvArgs a2{h->spec.p, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), F->lo, F->hi,
+    ThetaConvArgs a2{h->spec.p, F->fz.p, h->Nth, h->Nk, F->lo, F->hi,
                      F->dlo, F->dhi, 1, h->plan_th, h->fwd_tblock};
     if (F->dhi >= F->dlo)
       CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
@@ -1308,7 +1310,7 @@ extern "C" int lp_fwd_noalloc(lp_handle* h, float* R, const float* f, int S0, vo
     FwdC2LPArgs a1{fbuf, spec, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, h->cubic, h->plan_rho,
                    nullptr, F->ival.p, F->dlo, F->dhi, F->F, F->fsc};
     CUDA_TRY(launch(h, K_FWD_C2LP, st, [&] { return launch_fwd_c2lp(a1, S0, st); }));
-    ThetaConvArgs a2{spec, F->fz.p, h->Nth, h->Nk, 1.0f / ((float)h->Nth * (float)h->Nrho), F->dlo, F->dhi,
+    ThetaConvArgs a2{spec, F->fz.p, h->Nth, h->Nk, F->dlo, F->dhi,
                      F->lo & ~1, std::min(F->hi | 1, h->Nth - 1), 0, h->plan_th, h->fwd_tblock};
     CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
     FwdLP2PolarArgs a3{spec, R, F->thc.p, F->rhoc.p, F->rows[k].p, F->nrows[k], h->N, h->N0, h->Nth,

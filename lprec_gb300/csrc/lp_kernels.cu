@@ -457,7 +457,7 @@ __global__ void __launch_bounds__(256, 2) k_theta_conv(ThetaConvArgs a) {
     float2 w = __ldg(a.fz + sidx(k0 + r, t, a.Nth));
     if (a.conj_fz) w.y = -w.y;
     const CBuf Xr = X.offset(r * ps);
-    Xr.set(t, cscale(cmul(Xr.get(t), w), a.scale));
+    Xr.set(t, cmul(Xr.get(t), w));
   }
   __syncthreads();
   const CBuf Y = fft_block<1>(X, X.re == A.re ? B : A, a.plan, 2, ps);
@@ -1028,7 +1028,8 @@ struct TC {
   static constexpr int SLOTS = reg_fft_slots(L) + (KT > 1 ? 16 / KT : 0);
 };
 
-// per rho frequency: FFT along theta, multiply by the kernel, inverse; NSIG rows per block
+// per rho frequency: FFT along theta, multiply by the kernel (which carries the
+// 1/(Nrho*Ntheta) of the two unnormalised transforms), inverse; NSIG rows per block
 template <int L, int BLK>
 __global__ void __launch_bounds__(TC<L, BLK>::BLOCK, 768 / TC<L, BLK>::BLOCK) k_theta_conv_p2(ThetaConvArgs a) {
   extern __shared__ float2 sm2[];
@@ -1056,7 +1057,7 @@ __global__ void __launch_bounds__(TC<L, BLK>::BLOCK, 768 / TC<L, BLK>::BLOCK) k_
     const int c = t + i * T;
     float2 w = __ldg(a.fz + sidx(kf, c, L));
     if (a.conj_fz) w.y = -w.y;
-    v[i] = cscale(cmul(v[i], w), a.scale);
+    v[i] = cmul(v[i], w);
   }
   reg_fft<L, 1>(v, sm, t);
   if (!live) return;

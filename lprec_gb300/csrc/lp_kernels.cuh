@@ -56,9 +56,8 @@ struct FwdC2LPArgs {          // Cartesian -> log-polar gather, e^rho, FFT along
 
 struct ThetaConvArgs {        // FFT along theta, multiply by the kernel, inverse
   float2* spec;               // [S] spectra, tiled layout
-  const float2* fz;           // Hermitian-extended kernel, tiled layout
+  const float2* fz;           // Hermitian-extended kernel / (Nrho*Nth), tiled layout
   int Nth, Nk;
-  float scale;
   int in_lo, in_hi;           // columns outside [in_lo, in_hi] are read as 0
   int out_lo, out_hi;         // only these columns are written back
   int conj_fz;
