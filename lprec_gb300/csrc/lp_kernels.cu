@@ -388,6 +388,85 @@ __global__ void k_col_prefilter(ColPrefilterArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// prefilter along the slow axis, out of place (final coefficients to the
+// per-slice surfaces): one warp per 32 columns x kColC rows.  The warp copies
+// its rows plus LP_WARM rows on either side into shared memory with
+// asynchronous copies (all of them in flight at once), runs both recursions
+// there -- the same zero-state warm-ups and boundary initialisations as
+// k_col_prefilter -- and writes each coefficient once.  The input is only
+// read, so warps need no ordering between them.
+// ---------------------------------------------------------------------------
+constexpr int kColC = 64;                          // output rows per warp
+constexpr int kColRows = kColC + 2 * LP_WARM;      // rows staged per warp
+constexpr int kColWarps = 4;                       // 4 x 96 x 32 floats = 48 KB per block
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+
+__global__ void __launch_bounds__(32 * kColWarps) k_col_prefilter_staged(ColPrefilterArgs a) {
+  __shared__ float tile[kColWarps][kColRows][32];
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int H = a.H, W = a.W;
+  const int b = (blockIdx.y * kColWarps + wp) * kColC;
+  if (b >= H) return;  // warps are independent: no block-wide barrier below
+  const int e = min(b + kColC, H);
+  const int r0 = max(0, b - LP_WARM), r1 = min(H, e + LP_WARM);
+  const int x = blockIdx.x * 32 + lane;
+  const int s = blockIdx.z;
+  const bool inx = x < W;
+  float(*t)[32] = tile[wp];
+  const float* col = a.img + (size_t)s * H * W + x;
+  for (int r = r0; r < r1; ++r) {
+    if (inx) cp_async4(&t[r - r0][lane], col + (size_t)r * W);
+    else t[r - r0][lane] = 0.f;
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  __syncwarp();
+  const float z = LP_POLE;
+  // causal: exact initialisation at row 0, else LP_WARM warm-up rows from a zero state
+  float prev = 0.f;
+  int n;
+  if (b == 0) {
+    const int hor = min(12, H);
+    float sum = t[0][lane];
+    float zn = z;
+    for (int i = 0; i < hor; ++i) {
+      sum += zn * t[i][lane];
+      zn *= z;
+    }
+    prev = LP_LAMBDA * sum;
+    t[0][lane] = prev;
+    n = 1;
+  } else {
+#pragma unroll
+    for (int i = 0; i < LP_WARM; ++i) prev = LP_LAMBDA * t[i][lane] + z * prev;
+    n = b;
+  }
+  for (; n < r1; ++n) {
+    prev = LP_LAMBDA * t[n - r0][lane] + z * prev;
+    t[n - r0][lane] = prev;
+  }
+  // anticausal: exact initialisation at row H-1 when it is within reach, else a
+  // zero state LP_WARM rows past the chunk
+  const cudaSurfaceObject_t so = a.surf[s];
+  float c;
+  if (r1 == H && H - e <= LP_WARM) {
+    c = (z / (z - 1.0f)) * t[H - 1 - r0][lane];
+    if (e == H && inx) surf2Dwrite(c, so, x * (int)sizeof(float), H - 1);
+    n = H - 2;
+  } else {
+    c = -z * t[r1 - 1 - r0][lane];
+    n = r1 - 2;
+  }
+  for (; n >= b; --n) {
+    c = z * (c - t[n - r0][lane]);
+    if (n < e && inx) surf2Dwrite(c, so, x * (int)sizeof(float), n);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // forward, per span: gather Cartesian -> log-polar for two theta columns,
 // multiply by e^rho, FFT along rho (two real columns in one complex FFT).
 // Reference: interp mode 3 (lpRgpu.cu:263), mulexp (:267), R2C (:270).
@@ -841,6 +920,12 @@ cudaError_t launch_fwd_ingest(const FwdIngestArgs& a, int S, cudaStream_t st) {
 }
 
 cudaError_t launch_col_prefilter(const ColPrefilterArgs& a, int S, cudaStream_t st) {
+  if (a.surf) {
+    const int chunks = (a.H + kColC - 1) / kColC;
+    dim3 grid((a.W + 31) / 32, (chunks + kColWarps - 1) / kColWarps, S);
+    k_col_prefilter_staged<<<grid, 32 * kColWarps, 0, st>>>(a);
+    return cudaGetLastError();
+  }
   int nch = a.H / LP_WARM;
   if (nch > 32) nch = 32;
   if (nch < 1) nch = 1;

@@ -38,6 +38,7 @@ struct ColPrefilterArgs {     // prefilter along the slow axis, in place
   float* img;                 // [S][H][W]
   int H, W;
   const cudaSurfaceObject_t* surf;  // if set: final coefficients go to these per-slice 2-D arrays instead
+                                    // (img is then only read)
 };
 
 struct FwdC2LPArgs {          // Cartesian -> log-polar gather, e^rho, FFT along rho
