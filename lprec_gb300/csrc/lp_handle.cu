@@ -135,6 +135,7 @@ struct AdjDev {
   DevBuf<float> H;         // [4N] or empty
   bool filter = false;
   DevBuf<float> rbuf;      // [Nslices][Nproj][N]
+  DevBuf<float> rin;       // [Nslices][Nproj][N] ingest output before the column prefilter (cubic)
   DevBuf<float> G[3];      // [Nslices][W2][Nrho] (linear mode)
   // cubic mode: the real log-polar columns of each span and slice as 2-D CUDA
   // arrays (x = rho, y = theta - lo2), written through surfaces, read by gathers
@@ -230,6 +231,7 @@ static void free_adj(AdjDev* a) {
   a->fz.free_();
   a->H.free_();
   a->rbuf.free_();
+  a->rin.free_();
   for (int k = 0; k < 3; ++k) {
     for (cudaTextureObject_t t : a->tex_h[k]) cudaDestroyTextureObject(t);
     for (cudaSurfaceObject_t t : a->surf_h[k]) cudaDestroySurfaceObject(t);
@@ -847,6 +849,7 @@ static int init_adj_impl(lp_handle* h, const int32_t* pi, int64_t ni, const Real
     A->filter = true;
   }
   if (e == cudaSuccess) e = dev_alloc(A->rbuf, (size_t)h->Nslices * Nproj * N);
+  if (e == cudaSuccess && h->cubic) e = dev_alloc(A->rin, (size_t)h->Nslices * Nproj * N);
   int gw = 0, gh = 0;
   cudaDeviceGetAttribute(&gw, cudaDevAttrMaxTexture2DGatherWidth, h->device);
   cudaDeviceGetAttribute(&gh, cudaDevAttrMaxTexture2DGatherHeight, h->device);
@@ -930,6 +933,7 @@ int lp_debug_fill_scratch(lp_handle* h, float value, void* stream) {
   if (e == cudaSuccess && h->fwd) e = fill_async(h->fwd->fbuf.p, h->fwd->fbuf.n, value, st);
   if (e == cudaSuccess && h->adj) {
     e = fill_async(h->adj->rbuf.p, h->adj->rbuf.n, value, st);
+    if (e == cudaSuccess && h->adj->rin.p) e = fill_async(h->adj->rin.p, h->adj->rin.n, value, st);
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = fill_async(h->adj->G[k].p, h->adj->G[k].n, value, st);
   }
   if (e != cudaSuccess) return set_err(LP_ERR_CUDA, "lp_debug_fill_scratch: %s", cudaGetErrorString(e));
@@ -948,7 +952,7 @@ int lp_device_bytes(const lp_handle* h, int64_t* bytes) {
     for (int k = 0; k < 3; ++k)
       b += h->adj->ta[k].n * 4 + h->adj->sx[k].n * 4 + h->adj->woff[k].n * 4 + h->adj->wpt[k].n * 16 +
            h->adj->c2lp[k].n * 8 + h->adj->G[k].n * 4;
-    b += h->adj->fz.n * 8 + h->adj->H.n * 4 + h->adj->rbuf.n * 4;
+    b += h->adj->fz.n * 8 + h->adj->H.n * 4 + h->adj->rbuf.n * 4 + h->adj->rin.n * 4;
     b += (int64_t)h->adj->arr.size() * h->Nrho * h->adj->W2 * 4;
   }
   *bytes = b;
@@ -1019,13 +1023,15 @@ static int adj_slices(lp_handle* h, float* f, const float* R, int s0, int n, cud
   R += (size_t)s0 * h->Nproj0 * h->N0;
   f += (size_t)s0 * h->N0 * h->N0;
   float* rbuf = A->rbuf.p + (size_t)s0 * h->Nproj * h->N;
+  // cubic: the ingest writes rin and the column prefilter rin -> rbuf (out of place)
+  float* rin = h->cubic ? A->rin.p + (size_t)s0 * h->Nproj * h->N : rbuf;
   float2* spec = h->spec.p + (size_t)s0 * spec_slice(h->Nk, h->Nth);
   const size_t gstride = (size_t)A->W2 * h->Nrho;
-  AdjIngestArgs ia{R, rbuf, A->filter ? A->H.p : nullptr, h->N, h->N0, h->Nproj, h->Nproj0, h->os,
+  AdjIngestArgs ia{R, rin, A->filter ? A->H.p : nullptr, h->N, h->N0, h->Nproj, h->Nproj0, h->os,
                    h->N / 2 - h->cor, h->cubic, h->plan_filt};
   CUDA_TRY(launch(h, K_ADJ_INGEST, st, [&] { return launch_adj_ingest(ia, n, st); }));
   if (h->cubic) {
-    ColPrefilterArgs ca{rbuf, h->Nproj, h->N};
+    ColPrefilterArgs ca{rin, h->Nproj, h->N, nullptr, rbuf};
     CUDA_TRY(launch(h, K_COL_PREFILTER, st, [&] { return launch_col_prefilter(ca, n, st); }));
   }
   float* G[3];

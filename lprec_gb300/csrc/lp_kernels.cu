@@ -389,7 +389,7 @@ __global__ void k_col_prefilter(ColPrefilterArgs a) {
 
 // ---------------------------------------------------------------------------
 // prefilter along the slow axis, out of place (final coefficients to the
-// per-slice surfaces): one warp per 32 columns x kColC rows.  The warp copies
+// per-slice surfaces or to a separate array): one warp per 32 columns x kColC rows.  The warp copies
 // its rows plus LP_WARM rows on either side into shared memory with
 // asynchronous copies (all of them in flight at once), runs both recursions
 // there -- the same zero-state warm-ups and boundary initialisations as
@@ -450,11 +450,16 @@ __global__ void __launch_bounds__(32 * kColWarps) k_col_prefilter_staged(ColPref
   }
   // anticausal: exact initialisation at row H-1 when it is within reach, else a
   // zero state LP_WARM rows past the chunk
-  const cudaSurfaceObject_t so = a.surf[s];
+  const cudaSurfaceObject_t so = a.surf ? a.surf[s] : 0;
+  float* dst = a.out + (size_t)s * H * W + x;
+  auto put = [&](int row, float v) {
+    if (a.surf) surf2Dwrite(v, so, x * (int)sizeof(float), row);
+    else dst[(size_t)row * W] = v;
+  };
   float c;
   if (r1 == H && H - e <= LP_WARM) {
     c = (z / (z - 1.0f)) * t[H - 1 - r0][lane];
-    if (e == H && inx) surf2Dwrite(c, so, x * (int)sizeof(float), H - 1);
+    if (e == H && inx) put(H - 1, c);
     n = H - 2;
   } else {
     c = -z * t[r1 - 1 - r0][lane];
@@ -462,7 +467,7 @@ __global__ void __launch_bounds__(32 * kColWarps) k_col_prefilter_staged(ColPref
   }
   for (; n >= b; --n) {
     c = z * (c - t[n - r0][lane]);
-    if (n < e && inx) surf2Dwrite(c, so, x * (int)sizeof(float), n);
+    if (n < e && inx) put(n, c);
   }
 }
 
@@ -920,7 +925,7 @@ cudaError_t launch_fwd_ingest(const FwdIngestArgs& a, int S, cudaStream_t st) {
 }
 
 cudaError_t launch_col_prefilter(const ColPrefilterArgs& a, int S, cudaStream_t st) {
-  if (a.surf) {
+  if (a.surf || a.out) {
     const int chunks = (a.H + kColC - 1) / kColC;
     dim3 grid((a.W + 31) / 32, (chunks + kColWarps - 1) / kColWarps, S);
     k_col_prefilter_staged<<<grid, 32 * kColWarps, 0, st>>>(a);

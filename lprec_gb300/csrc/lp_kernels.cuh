@@ -39,6 +39,7 @@ struct ColPrefilterArgs {     // prefilter along the slow axis, in place
   int H, W;
   const cudaSurfaceObject_t* surf;  // if set: final coefficients go to these per-slice 2-D arrays instead
                                     // (img is then only read)
+  float* out;                 // else if set: final coefficients go to out [S][H][W] (img only read)
 };
 
 struct FwdC2LPArgs {          // Cartesian -> log-polar gather, e^rho, FFT along rho
