@@ -255,14 +255,34 @@ __global__ void k_fwd_ingest(FwdIngestArgs a) {
   const int y = blockIdx.y;
   const int Y = y - a.off;
   const float* src = a.fin + ((size_t)s * a.N0 + (size_t)max(Y, 0)) * a.N0;
-  for (int x = threadIdx.x; x < a.N; x += blockDim.x) {
-    const int X = x - a.off;
-    line[lpos(x, C)] = (Y >= 0 && Y < a.N0 && X >= 0 && X < a.N0) ? __ldg(src + X) : 0.f;
+  float* dst = a.fbuf + ((size_t)s * a.N + y) * a.N;
+  // 16-byte path: with off, N0 and N multiples of 4 every group of 4 samples lies
+  // wholly inside or outside the image, and rows start 16-byte aligned
+  const bool vec = ((a.off | a.N0 | a.N) & 3) == 0 && ((((uintptr_t)a.fin) | ((uintptr_t)a.fbuf)) & 15) == 0;
+  const bool rowin = Y >= 0 && Y < a.N0;
+  if (vec) {
+#pragma unroll 4
+    for (int x = 4 * threadIdx.x; x < a.N; x += 4 * blockDim.x) {
+      const int X = x - a.off;
+      const float4 v = (rowin && X >= 0 && X < a.N0) ? __ldg(reinterpret_cast<const float4*>(src + X))
+                                                      : make_float4(0.f, 0.f, 0.f, 0.f);
+      *reinterpret_cast<float4*>(line + x) = v;
+    }
+  } else {
+    for (int x = threadIdx.x; x < a.N; x += blockDim.x) {
+      const int X = x - a.off;
+      line[lpos(x, C)] = (rowin && X >= 0 && X < a.N0) ? __ldg(src + X) : 0.f;
+    }
   }
   __syncthreads();
   if (a.cubic) prefilter_line(line, cp, a.N, threadIdx.x, blockDim.x);
-  float* dst = a.fbuf + ((size_t)s * a.N + y) * a.N;
-  for (int x = threadIdx.x; x < a.N; x += blockDim.x) dst[x] = line[lpos(x, C)];
+  if (vec) {
+#pragma unroll 4
+    for (int x = 4 * threadIdx.x; x < a.N; x += 4 * blockDim.x)
+      *reinterpret_cast<float4*>(dst + x) = *reinterpret_cast<const float4*>(line + x);
+  } else {
+    for (int x = threadIdx.x; x < a.N; x += blockDim.x) dst[x] = line[lpos(x, C)];
+  }
 }
 
 // ---------------------------------------------------------------------------
