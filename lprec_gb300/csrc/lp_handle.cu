@@ -394,11 +394,6 @@ static int fixed_bits(double maxabs) {
   return F;
 }
 static inline int to_fixed(double x, int F) { return std::isnan(x) ? LP_FX_NONE : (int)std::llrint(std::ldexp(x, F)); }
-static std::vector<int> to_fixed(const std::vector<double>& v, int F) {
-  std::vector<int> out(v.size());
-  for (size_t i = 0; i < v.size(); ++i) out[i] = to_fixed(v[i], F);
-  return out;
-}
 // first interpolation tap of a fixed-point coordinate (the kernels' v >> F)
 static inline int first_tap(int v, int F, int cubic) { return (v >> F) - (cubic ? 1 : 0); }
 
