@@ -194,3 +194,97 @@ __device__ __forceinline__ void reg_fft(float2 (&v)[16], float2* sm, int t, cons
 }
 
 }  // namespace lpgb
+
+namespace lpgb {
+
+// Two signals of the same length on the same threads: thread t holds x0[t + i*T]
+// in v0[i] and x1[t + i*T] in v1[i].  Each stage computes its twiddles once and
+// applies them to both signals before either butterfly, then transforms and
+// writes one signal after the other (so only one butterfly's temporaries are
+// live at a time).  Same arithmetic per signal as reg_stage / reg_fft, so each
+// result equals the one-signal transform's bit for bit.
+template <int L, int DIR, int R, int NS, bool LAST, int OUT>
+__device__ __forceinline__ void reg_stage2(float2 (&v0)[16], float2 (&v1)[16], float2* sm0, float2* sm1, int t) {
+  constexpr int T = L / 16;
+  constexpr int NB = 16 / R;
+  static_assert(OUT == kOutSmem || OUT == kOutRegs, "two-signal stages write shared memory or registers");
+  static_assert(OUT != kOutRegs || (LAST && NS * R == L), "register output only from a last stage spanning L");
+  float2 w1_0 = make_float2(1.f, 0.f), w4_0 = make_float2(1.f, 0.f);
+#pragma unroll
+  for (int m = 0; m < NB; ++m) {
+    const int jp = t + m * T;
+    const int k = jp & (NS - 1);
+    if constexpr (NS > 1) {
+      float2 w[R];
+      if constexpr (NB > 1) {
+        static_assert(NS * R == L, "multi-butterfly stages end the transform");
+        if (m == 0) {
+          twiddle_powers<R, DIR>((float)k * (1.0f / (float)(NS * R)), w);
+          w1_0 = w[1];
+          if constexpr (R >= 8) w4_0 = w[4];
+        } else {
+          const float2 w1 = rot<DIR>(w1_0, cos_pi8(m), sin_pi8(m));
+          float2 w4 = w4_0;
+          if constexpr (R >= 8) {
+#pragma unroll
+            for (int j = 0; j < (m & 3); ++j) w4 = mul_i<DIR>(w4);
+          }
+          twiddle_powers_from<R>(w1, w4, w);
+        }
+      } else {
+        twiddle_powers<R, DIR>((float)k * (1.0f / (float)(NS * R)), w);
+      }
+#pragma unroll
+      for (int i = 1; i < R; ++i) {
+        v0[m + i * NB] = cmul(v0[m + i * NB], w[i]);
+        v1[m + i * NB] = cmul(v1[m + i * NB], w[i]);
+      }
+    }
+    const int base = (jp - k) * R + k;
+#pragma unroll
+    for (int sg = 0; sg < 2; ++sg) {
+      float2(&v)[16] = sg == 0 ? v0 : v1;
+      float2* sm = sg == 0 ? sm0 : sm1;
+      float2 x[R];
+#pragma unroll
+      for (int i = 0; i < R; ++i) x[i] = v[m + i * NB];
+      reg_bfly<R, DIR>(x);
+      if constexpr (OUT == kOutRegs) {
+#pragma unroll
+        for (int i = 0; i < R; ++i) v[m + i * NB] = x[i];
+      } else {
+#pragma unroll
+        for (int i = 0; i < R; ++i) sm[spad(base + i * NS)] = x[i];
+      }
+    }
+  }
+  if constexpr (OUT != kOutRegs) __syncthreads();
+  if constexpr (!LAST) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      v0[i] = sm0[spad(t + i * T)];
+      v1[i] = sm1[spad(t + i * T)];
+    }
+    __syncthreads();
+  }
+}
+
+// Two-signal transform (see reg_stage2); OUT kOutSmem or kOutRegs as in reg_fft.
+template <int L, int DIR, int OUT = kOutSmem>
+__device__ __forceinline__ void reg_fft2(float2 (&v0)[16], float2 (&v1)[16], float2* sm0, float2* sm1, int t) {
+  static_assert(L == 256 || L == 512 || L == 1024 || L == 2048 || L == 4096 || L == 8192, "size");
+  reg_stage2<L, DIR, 16, 1, false, kOutSmem>(v0, v1, sm0, sm1, t);
+  if constexpr (L == 256) {
+    reg_stage2<L, DIR, 16, 16, true, OUT>(v0, v1, sm0, sm1, t);
+  } else if constexpr (L == 8192) {
+    reg_stage2<L, DIR, 16, 16, false, kOutSmem>(v0, v1, sm0, sm1, t);
+    reg_stage2<L, DIR, 16, 256, false, kOutSmem>(v0, v1, sm0, sm1, t);
+    reg_stage2<L, DIR, 2, 4096, true, OUT>(v0, v1, sm0, sm1, t);
+  } else {
+    reg_stage2<L, DIR, 16, 16, false, kOutSmem>(v0, v1, sm0, sm1, t);
+    constexpr int R3 = L / 256;
+    reg_stage2<L, DIR, R3, 256, true, OUT>(v0, v1, sm0, sm1, t);
+  }
+}
+
+}  // namespace lpgb

@@ -1174,6 +1174,74 @@ __global__ void __launch_bounds__(TC<L, BLK>::BLOCK, 768 / TC<L, BLK>::BLOCK) k_
   for (int c = a.out_lo + t; c <= a.out_hi; c += T) sp[sidx(k, c, L)] = sm[spad(c)];
 }
 
+// Two rows per thread (used for L <= 4096; at L = 8192 the two rows spill and the
+// one-row kernel runs): the thread owns rho frequencies k, k+1 (k even, the same
+// tile, adjacent in memory), so one 16-byte access moves both rows' element of a
+// theta column, and the two transforms share their twiddles (reg_fft2).  256
+// threads carry NP = 256/T row pairs; KP = min(2, NP) pairs alternate fastest
+// across lanes (lane l: pair l % KP, position l / KP), so a warp access covers
+// 32/KP consecutive columns of 2*KP rows -- contiguous in the tiled layout.  The
+// 2*NP row buffers are signal-major (buffer j*NP + p for signal j of pair p) and
+// spaced by SLOTS (padded by 8 float2 when KP = 2) so that the pairs of a
+// half-warp fall in distinct banks.
+template <int L>
+struct TC2 {
+  static constexpr int T = L / 16;
+  static constexpr int BLOCK = 256 > T ? 256 : T;
+  static constexpr int NP = BLOCK / T;
+  static constexpr int KP = NP < 2 ? NP : 2;
+  static constexpr int SLOTS = reg_fft_slots(L) + (KP > 1 ? 8 : 0);
+  static constexpr size_t SMEM = (size_t)2 * NP * SLOTS * sizeof(float2);
+};
+
+template <int L>
+__global__ void __launch_bounds__(TC2<L>::BLOCK, 512 / TC2<L>::BLOCK) k_theta_conv2_p2(ThetaConvArgs a) {
+  extern __shared__ float2 sm2[];
+  using C = TC2<L>;
+  constexpr int T = C::T, KP = C::KP;
+  const int g = threadIdx.x / (KP * T), r = threadIdx.x % (KP * T);
+  const int pr = g * KP + r % KP, t = r / KP;
+  float2* sm0 = sm2 + pr * C::SLOTS;
+  float2* sm1 = sm2 + (C::NP + pr) * C::SLOTS;
+  const int s = blockIdx.x;
+  const int k = (blockIdx.y * C::NP + pr) * 2;
+  const bool live0 = k < a.Nk, live1 = k + 1 < a.Nk;
+  float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, L);
+  float2 v0[16], v1[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const int c = t + i * T;
+    float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (live0 && c >= a.in_lo && c <= a.in_hi) q = *reinterpret_cast<const float4*>(sp + sidx(k, c, L));
+    v0[i] = make_float2(q.x, q.y);
+    v1[i] = live1 ? make_float2(q.z, q.w) : make_float2(0.f, 0.f);
+  }
+  reg_fft2<L, -1, kOutRegs>(v0, v1, sm0, sm1, t);
+  const int kf = live0 ? k : 0;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const int c = t + i * T;
+    float4 w = __ldg(reinterpret_cast<const float4*>(a.fz + sidx(kf, c, L)));
+    if (a.conj_fz) {
+      w.y = -w.y;
+      w.w = -w.w;
+    }
+    v0[i] = cmul(v0[i], make_float2(w.x, w.y));
+    v1[i] = cmul(v1[i], make_float2(w.z, w.w));
+  }
+  reg_fft2<L, 1>(v0, v1, sm0, sm1, t);
+  if (!live0) return;
+  for (int c = a.out_lo + t; c <= a.out_hi; c += T) {
+    const float2 y0 = sm0[spad(c)];
+    if (live1) {
+      const float2 y1 = sm1[spad(c)];
+      *reinterpret_cast<float4*>(sp + sidx(k, c, L)) = make_float4(y0.x, y0.y, y1.x, y1.y);
+    } else {
+      sp[sidx(k, c, L)] = y0;
+    }
+  }
+}
+
 // element p of the complex signal whose inverse FFT gives two real profiles
 // with half spectra V0, V1 (C2R semantics: imaginary parts at 0 and L/2 ignored)
 __device__ __forceinline__ float2 pair_elem(int p, int L, float2 v0, float2 v1) {
@@ -1500,6 +1568,7 @@ static void set_p2_attrs(int optin) {
   cudaFuncSetAttribute(k_fwd_c2lp_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_theta_conv_p2<L, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_theta_conv_p2<L, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  cudaFuncSetAttribute(k_theta_conv2_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_fwd_lp2polar_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_adj_ingest_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_adj_polar2lp_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -1547,6 +1616,11 @@ bool p2_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st, cudaError_t* 
       if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; } \
       dim3 grid(S, (a.Nk + C::NSIG - 1) / C::NSIG);                                           \
       k_theta_conv_p2<LL, 512><<<grid, C::BLOCK, sm, st>>>(a);                                \
+    } else if (LL <= 4096) {                                                                  \
+      using C = TC2<LL>;                                                                      \
+      if (smem_ok(C::SMEM) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; } \
+      dim3 grid(S, (a.Nk + 2 * C::NP - 1) / (2 * C::NP));                                     \
+      k_theta_conv2_p2<LL><<<grid, C::BLOCK, C::SMEM, st>>>(a);                               \
     } else {                                                                                  \
       using C = TC<LL, 256>;                                                                  \
       const size_t sm = (size_t)C::NSIG * C::SLOTS * sizeof(float2);                          \
