@@ -38,11 +38,11 @@ ALGO_BYTES_PER_SLICE = 1.541e9
 # 128-slice launch is taken as 128 times these (every term but the per-launch tables grows
 # with the slice count)
 NCU_DRAM_BYTES_PER_SLICE = {
-    "fwd_ingest": (134.2e6 + 85.6e6) / 8, "col_prefilter": (166.7e6 + 232.2e6) / 8,
-    "fwd_c2lp": (128.9e6 + 98.5e6) / 8, "theta_conv": (168.2e6 + 79.6e6) / 8,
-    "fwd_lp2polar": (143.8e6 + 43.4e6) / 8, "adj_ingest": (196.7e6 + 151.0e6) / 8,
-    "adj_polar2lp": (83.2e6 + 88.1e6) / 8, "adj_lpcols": (135.6e6 + 93.5e6) / 8,
-    "adj_lp2cart": (354.1e6 + 119.1e6) / 8,
+    "fwd_ingest": (134.2e6 + 85.5e6) / 8, "col_prefilter": (165.4e6 + 117.9e6) / 8,
+    "fwd_c2lp": (129.1e6 + 100.0e6) / 8, "theta_conv": (168.3e6 + 79.8e6) / 8,
+    "fwd_lp2polar": (143.8e6 + 44.2e6) / 8, "adj_ingest": (196.7e6 + 150.5e6) / 8,
+    "adj_polar2lp": (83.2e6 + 87.9e6) / 8, "adj_lpcols": (135.6e6 + 92.3e6) / 8,
+    "adj_lp2cart": (354.1e6 + 117.2e6) / 8,
 }
 
 
