@@ -165,10 +165,29 @@ def _cpu_span(args):
     return O.adj_span(tr.G, tr.Ta, arr, k)
 
 
-class CpuBaseline:
-    """fwd+adj of one slice per step with the oracle, spans in parallel processes."""
+def _cpu_prep(args):
+    """Per-slice preparation: centre and prefilter an image (fwd), or pad, FBP-filter and
+    prefilter a sinogram (adj)."""
+    kind, arr = args
+    O, tr = _W["O"], _W["tr"]
+    G = tr.G
+    if kind == "fwd":
+        o = G.N // 2 - G.N0 // 2
+        d = np.zeros((1, G.N, G.N))
+        d[:, o:o + G.N0, o:o + G.N0] = arr
+    else:
+        d = O.pad_sinogram(G, arr)
+        if tr.Ta.get("filter") is not None:
+            d = O.apply_filter(G, d, tr.Ta["filter"])
+    return O.prefilter2d(d) if G.cubic else d
 
-    def __init__(self, packed, nproc):
+
+class CpuBaseline:
+    """fwd+adj of B slices per step with the oracle in one process pool: the slices'
+    preparation jobs, then the 3 spans of each direction and slice as parallel jobs
+    (6 B jobs, so B = cores // 6 keeps every core busy)."""
+
+    def __init__(self, packed, nproc, slices=1):
         import multiprocessing as mp
         sys.path.insert(0, ROOT)
         from oracle import lprec_oracle as O
@@ -180,38 +199,35 @@ class CpuBaseline:
         self.tr = O.Transform.from_packed(*packed)
         self.pool = mp.get_context("spawn").Pool(nproc, initializer=_cpu_init, initargs=(self.path,))
         self.nproc = nproc
+        self.B = max(1, int(slices))
         rng = np.random.default_rng(WORKLOAD["seed"])
-        self.f = O.ellipse_phantom(self.tr.G.N0, WORKLOAD["ellipses"], rng)[None]
+        self.f = [O.ellipse_phantom(self.tr.G.N0, WORKLOAD["ellipses"], rng)[None] for _ in range(self.B)]
         self.R = None
 
     def step(self):
-        O, tr = self.O, self.tr
+        tr, B = self.tr, self.B
         G = tr.G
         t0 = time.perf_counter()
-        # forward: centre + prefilter here, spans in the pool
-        o = G.N // 2 - G.N0 // 2
-        df = np.zeros((1, G.N, G.N))
-        df[:, o:o + G.N0, o:o + G.N0] = self.f
-        fp = O.prefilter2d(df) if G.cubic else df
-        adj_in = self.R if self.R is not None else None
-        jobs = [("fwd", k, fp) for k in range(3)]
-        if adj_in is not None:
-            dR = O.pad_sinogram(G, adj_in)
-            if tr.Ta.get("filter") is not None:
-                dR = O.apply_filter(G, dR, tr.Ta["filter"])
-            Rp = O.prefilter2d(dR) if G.cubic else dR
-            jobs += [("adj", k, Rp) for k in range(3)]
+        adj = self.R is not None
+        prep = [("fwd", f) for f in self.f] + ([("adj", R) for R in self.R] if adj else [])
+        pre = self.pool.map(_cpu_prep, prep)
+        jobs = [("fwd", k, pre[b]) for b in range(B) for k in range(3)]
+        if adj:
+            jobs += [("adj", k, pre[B + b]) for b in range(B) for k in range(3)]
         res = self.pool.map(_cpu_span, jobs)
-        R = np.zeros((1, G.Nproj * G.N))
-        for k in range(3):
-            R[:, tr.Tf["pids"][k]] += res[k]
-        R = R.reshape(1, G.Nproj, G.N)[:, ::G.osangles, G.N // 2 - G.cor:G.N // 2 - G.cor + G.N0]
-        if adj_in is not None:
-            f = np.zeros((1, G.N * G.N))
+        Rs = []
+        for b in range(B):
+            R = np.zeros((1, G.Nproj * G.N))
             for k in range(3):
-                f[:, tr.Ta["cids"]] += res[3 + k]
-        self.R = R
-        return time.perf_counter() - t0, adj_in is not None
+                R[:, tr.Tf["pids"][k]] += res[3 * b + k]
+            Rs.append(R.reshape(1, G.Nproj, G.N)[:, ::G.osangles, G.N // 2 - G.cor:G.N // 2 - G.cor + G.N0])
+        if adj:
+            for b in range(B):
+                f = np.zeros((1, G.N * G.N))
+                for k in range(3):
+                    f[:, tr.Ta["cids"]] += res[3 * B + 3 * b + k]
+        self.R = Rs
+        return time.perf_counter() - t0, adj
 
     def close(self):
         self.pool.close()
@@ -219,15 +235,22 @@ class CpuBaseline:
         os.unlink(self.path)
 
 
-def cpu_baseline(packed, nproc, steps):
-    """slices/s of fwd+adj (one slice per step) after one warm-up step that produces the sinogram."""
-    cb = CpuBaseline(packed, nproc)
+def cpu_plan():
+    """(processes, slices per step) that keep the host's cores busy: 6 jobs per slice."""
+    cores = len(os.sched_getaffinity(0))
+    slices = max(1, cores // 6)
+    return max(1, min(cores, 6 * slices)), slices
+
+
+def cpu_baseline(packed, nproc, steps, slices=1):
+    """slices/s of fwd+adj (`slices` per step) after one warm-up step that produces the sinograms."""
+    cb = CpuBaseline(packed, nproc, slices)
     try:
         cb.step()
         times = [cb.step()[0] for _ in range(steps)]
     finally:
         cb.close()
-    return 1.0 / statistics.median(times), sum(times)
+    return slices / statistics.median(times), sum(times)
 
 
 def cpu_side_configs():
@@ -253,26 +276,26 @@ def run_reference(args):
     from lprec_gb300 import _lib
     W = WORKLOAD
     packed = _lib.precompute(W["N"], W["Nproj"], 1, W["N"] / 2, W["interp"], W["filter"], precision="fp64")
-    cores = len(os.sched_getaffinity(0))
-    nproc = max(1, min(cores, 6))
-    cb = CpuBaseline(packed, nproc)
+    nproc, B = cpu_plan()
+    cb = CpuBaseline(packed, nproc, B)
     try:
-        cb.step()  # produces the adjoint's input sinogram
+        cb.step()  # produces the adjoint's input sinograms
         for _ in range(args.warmup):
             cb.step()
         times = [cb.step()[0] for _ in range(args.steps)]
     finally:
         cb.close()
-    value = 1.0 / statistics.median(times)
+    value = B / statistics.median(times)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * statistics.median(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic random-ellipse phantom (30 ellipses, seed 3)",
-            "config": {"workload": "fwd+adj N=2048 Nproj=3000 shepp-logan cubic", "slices_per_step": 1},
+            "config": {"workload": "fwd+adj N=2048 Nproj=3000 shepp-logan cubic", "slices_per_step": B},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nproc, "kind": "port",
-                             "sample": "1 slice fwd+adj per step; float64 NumPy restatement of the reference "
-                                       "algorithm (its CUDA code does not build with CUDA 13); the 3 spans of "
-                                       "fwd and adj in %d processes" % nproc},
+                             "sample": "%d slice(s) fwd+adj per step; float64 NumPy restatement of the reference "
+                                       "algorithm (its CUDA code does not build with CUDA 13); per-slice "
+                                       "preparation and the 3 spans of fwd and adj of each slice as jobs in %d "
+                                       "processes" % (B, nproc)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -577,13 +600,12 @@ def run_ours(args):
     if rank == 0 and not args.no_side and not args.small:
         line.update(run_side_configs(torch, dev))
     if rank == 0 and not args.no_cpu:
-        cores = len(os.sched_getaffinity(0))
-        nproc = max(1, min(cores, 6))
+        nproc, B = cpu_plan()
         packed = lp.tables()
-        v, busy = cpu_baseline(packed, nproc, 3)
+        v, busy = cpu_baseline(packed, nproc, 3, B)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nproc, "kind": "port",
-                                "sample": "3 steps of 1 slice fwd+adj N=%d (%.1f s), float64 oracle, spans in %d "
-                                          "processes" % (N, busy, nproc)}
+                                "sample": "3 steps of %d slice(s) fwd+adj N=%d (%.1f s), float64 oracle, slice "
+                                          "preparation and spans as jobs in %d processes" % (B, N, busy, nproc)}
         if not args.small:
             line["cpu_baseline"]["single_process"] = cpu_side_configs()
     if dist:
