@@ -1050,13 +1050,14 @@ struct P2 {
 // in flight together) and no fetch is spent outside the disk.  Values land in
 // the zeroed shared buffer at their rho position (real part: column th,
 // imaginary part: column th+1), from which the register FFT takes its inputs.
-// Measured at N=2048: one sample per group with 5 resident blocks per SM
-// (48 registers) beats 2, 4 or 8 samples per group with 2-4 blocks: the
+// Measured at N=2048: one sample per group with 6 resident blocks per SM
+// (40 registers, the shared-memory limit; 8.7 ms per step against 9.0 at 5
+// and 9.3 at 4) beats 2, 4 or 8 samples per group with 2-4 blocks: the
 // gathers' latency is hidden by more warps rather than by depth per thread.
 constexpr int kGatherUnroll = 1;
 
 template <int L>
-__global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(5)) k_fwd_c2lp_p2(FwdC2LPArgs a) {
+__global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(6)) k_fwd_c2lp_p2(FwdC2LPArgs a) {
   extern __shared__ float2 sm2[];
   constexpr int T = P2<L>::T;
   const int sig = threadIdx.x / T, t = threadIdx.x % T;
