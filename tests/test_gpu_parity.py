@@ -335,3 +335,19 @@ def test_uneven_batch_graph(torch_cuda):
         torch.cuda.synchronize()
         assert torch.equal(R, b.output_R(i)), i
         assert torch.equal(f, b.output_f(i)), i
+
+
+@pytest.mark.parametrize("args", [(64, 70, 32, 'ramp'), (48, 36, 24, 'none'), (80, 100, 40, 'shepp-logan'),
+                                  (64, 40, 32.5, 'hann')])
+def test_prefilter_chunk_edges(torch_cuda, args):
+    """Column lengths that end a few rows into a 64-row chunk's warm-up (H = 70, 72, 80)
+    or fit one chunk (H = 40): the staged column prefilter's exact boundary
+    initialisations against the oracle."""
+    from lprec_gb300 import _lib
+    N0, Nproj, cor, filt = args
+    packed = _lib.precompute(N0, Nproj, 2, cor, 'cubic', filt, precision='fp64')
+    h = _handle(packed)
+    tr = O.Transform.from_packed(*packed)
+    f, R = _inputs(tr.G, 2, 4)
+    assert O.rel_l2(_fwd(torch_cuda, h, f), tr.fwd(f)) < TOL
+    assert O.rel_l2(_adj(torch_cuda, h, R), tr.adj(R)) < TOL
