@@ -290,7 +290,10 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * statistics.median(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic random-ellipse phantom (30 ellipses, seed 3)",
-            "config": {"workload": "fwd+adj N=2048 Nproj=3000 shepp-logan cubic", "slices_per_step": B},
+            "config": {"workload": "fwd+adj batch: %d slices N=%d Nproj=%d cubic %s" % (W["S"], W["N"], W["Nproj"],
+                                                                                      W["filter"]),
+                       "slices": W["S"], "N": W["N"], "Nproj": W["Nproj"], "parallelism": "host processes",
+                       "sample_slices_per_step": B},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nproc, "kind": "port",
                              "sample": "%d slice(s) fwd+adj per step; float64 NumPy restatement of the reference "
                                        "algorithm (its CUDA code does not build with CUDA 13); per-slice "
