@@ -1097,10 +1097,14 @@ int lp_fwd_transpose(lp_handle* h, float* f, const float* R, int S0, void* strea
     CUDA_TRY(launch(h, K_FWDT_CART, st, [&] { return launch_fwdT_cart(a3, S0, st); }));
   }
   if (h->cubic) {
-    PrefilterTArgs pc{acc, h->N, h->N, 0};
-    CUDA_TRY(launch(h, K_PREFILTER_T, st, [&] { return launch_prefilter_T(pc, S0, st); }));
-    PrefilterTArgs pr{acc, h->N, h->N, 1};
-    CUDA_TRY(launch(h, K_PREFILTER_T, st, [&] { return launch_prefilter_T(pr, S0, st); }));
+    // transposed column prefilter acc -> the spectrum buffer (free now; it holds S0 N x N
+    // float images), then the transposed row prefilter into the caller's cropped image
+    float* tmp = reinterpret_cast<float*>(h->spec.p);
+    PrefilterTColsArgs pc{acc, tmp, h->N, h->N};
+    CUDA_TRY(launch(h, K_PREFILTER_T, st, [&] { return launch_prefilter_T_cols(pc, S0, st); }));
+    PrefilterTRowsCropArgs pr{tmp, f, h->N, h->N0, h->N / 2 - h->N0 / 2};
+    CUDA_TRY(launch(h, K_PREFILTER_T, st, [&] { return launch_prefilter_T_rows_crop(pr, S0, st); }));
+    return LP_OK;
   }
   CropArgs cr{acc, f, h->N, h->N0, h->N / 2 - h->N0 / 2};
   CUDA_TRY(launch(h, K_CROP, st, [&] { return launch_crop(cr, S0, st); }));

@@ -1850,36 +1850,105 @@ __global__ void __launch_bounds__(256) k_fwdT_cart(FwdTCartArgs a) {
   }
 }
 
-// one thread per line: y -> A^T (causal sum, boundary scaling) -> anticausal sum -> K^T
-__global__ void k_prefilter_T(PrefilterTArgs a) {
-  const int s = blockIdx.y;
-  const int line = blockIdx.x * blockDim.x + threadIdx.x;
-  const int L = a.along_rows ? a.W : a.H;
-  const int nl = a.along_rows ? a.H : a.W;
-  if (line >= nl) return;
-  const size_t stride = a.along_rows ? 1 : (size_t)a.W;
-  float* p = a.img + (size_t)s * a.H * a.W + (a.along_rows ? (size_t)line * a.W : (size_t)line);
+// ---------------------------------------------------------------------------
+// Chunked transposed prefilter.  The transpose of one line's prefilter
+// (ConvertToInterpolationCoefficients, main_kernels.cuh:97-142, with its
+// boundary initialisations): y1 = causal pass t = x + z t with outputs -z t
+// (q t = z/(z-1) t at the last sample), then w = y1 + z w backwards, then
+// out = lambda w plus, for the first 12 samples, lambda z^(m+1) w(0) (the
+// transposed causal boundary term).  Each chunk starts both recursions LP_WARM
+// samples outside itself from a zero state (exact to |pole|^16 ~ 7e-10, as the
+// forward prefilter's chunks are) and the line ends use the exact starts.
+// ---------------------------------------------------------------------------
+
+// columns: one warp per 32 columns x kColC rows staged in shared memory, out of place
+__global__ void __launch_bounds__(32 * kColWarps) k_prefilter_T_cols(PrefilterTColsArgs a) {
+  __shared__ float tile[kColWarps][kColRows][32];
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int H = a.H, W = a.W;
+  const int b = (blockIdx.y * kColWarps + wp) * kColC;
+  if (b >= H) return;  // warps are independent
+  const int e = min(b + kColC, H);
+  const int r0 = max(0, b - LP_WARM), r1 = min(H, e + LP_WARM);
+  const int x = blockIdx.x * 32 + lane;
+  const int s = blockIdx.z;
+  const bool inx = x < W;
+  float(*t)[32] = tile[wp];
+  const float* col = a.in + (size_t)s * H * W + x;
+  for (int r = r0; r < r1; ++r) {
+    if (inx) cp_async4(&t[r - r0][lane], col + (size_t)r * W);
+    else t[r - r0][lane] = 0.f;
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  __syncwarp();
   const float z = LP_POLE, q = LP_POLE / (LP_POLE - 1.0f);
-  float t = 0.f;
-  for (int m = 0; m < L; ++m) {
-    t = p[m * stride] + z * t;
-    p[m * stride] = (m < L - 1) ? -z * t : q * t;
+  float tc = 0.f;  // row 0 is the exact start; other chunks warm up from a zero state
+  for (int m = r0; m < r1; ++m) {
+    tc = t[m - r0][lane] + z * tc;
+    t[m - r0][lane] = (m < H - 1) ? -z * tc : q * tc;
   }
-  float w = p[(size_t)(L - 1) * stride];
-  for (int m = L - 2; m >= 0; --m) {
-    w = p[m * stride] + z * w;
-    p[m * stride] = w;
+  float w = 0.f;  // row H-1 is the exact start (w = y1 there); elsewhere a zero-state warm-up
+  for (int m = r1 - 1; m >= b; --m) {
+    w = t[m - r0][lane] + z * w;
+    t[m - r0][lane] = w;
   }
-  const float w0 = p[0];
-  const int hor = min(12, L);
+  float* dst = a.out + (size_t)s * H * W + x;
+  if (!inx) return;
+  const int hor = b == 0 ? min(12, H) : 0;
+  const float w0 = t[0][lane];
   float zn = z;
-  for (int m = 0; m < L; ++m) {
-    float v = LP_LAMBDA * p[m * stride];
+  for (int m = b; m < e; ++m) {
+    float v = LP_LAMBDA * t[m - r0][lane];
     if (m < hor) {
       v += LP_LAMBDA * zn * w0;
       zn *= z;
     }
-    p[m * stride] = v;
+    dst[(size_t)m * W] = v;
+  }
+}
+
+// rows: one block per output row, the padded row in shared memory, chunks of odd
+// length per thread (distinct banks), the window [off, off + N0) of it written
+// into the caller's image (the crop of the forward's centring)
+__global__ void k_prefilter_T_rows_crop(PrefilterTRowsCropArgs a) {
+  extern __shared__ float smf[];
+  const int N = a.N;
+  float* line = smf;
+  float* y1 = smf + N;
+  const int s = blockIdx.x, yo = blockIdx.y;
+  const float* src = a.in + ((size_t)s * N + yo + a.off) * N;
+  for (int x = threadIdx.x; x < N; x += blockDim.x) line[x] = __ldg(src + x);
+  __syncthreads();
+  const float z = LP_POLE, q = LP_POLE / (LP_POLE - 1.0f);
+  const int C = line_chunk(N, blockDim.x);
+  const int b = threadIdx.x * C, e = min(b + C, N);
+  if (b < N) {
+    float tc = 0.f;
+    for (int m = max(0, b - LP_WARM); m < e; ++m) {
+      tc = line[m] + z * tc;
+      if (m >= b) y1[m] = (m < N - 1) ? -z * tc : q * tc;
+    }
+  }
+  __syncthreads();
+  if (b < N) {
+    // the next chunks' causal outputs serve as this chunk's anticausal warm-up
+    float w = 0.f;
+    for (int m = min(N, e + LP_WARM) - 1; m >= b; --m) {
+      w = y1[m] + z * w;
+      if (m < e) line[m] = w;
+    }
+  }
+  __syncthreads();
+  const float w0 = line[0];
+  float* dst = a.out + ((size_t)s * a.N0 + yo) * a.N0 - a.off;
+  for (int x = max(threadIdx.x, a.off); x < a.off + a.N0; x += blockDim.x) {
+    float v = LP_LAMBDA * line[x];
+    if (x < 12) {
+      float zn = z;
+      for (int i = 0; i < x; ++i) zn *= z;
+      v += LP_LAMBDA * zn * w0;
+    }
+    dst[x] = v;
   }
 }
 
@@ -1911,10 +1980,18 @@ cudaError_t launch_fwdT_cart(const FwdTCartArgs& a, int S, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_prefilter_T(const PrefilterTArgs& a, int S, cudaStream_t st) {
-  const int nl = a.along_rows ? a.H : a.W;
-  dim3 grid((nl + 127) / 128, S);
-  k_prefilter_T<<<grid, 128, 0, st>>>(a);
+cudaError_t launch_prefilter_T_cols(const PrefilterTColsArgs& a, int S, cudaStream_t st) {
+  const int chunks = (a.H + kColC - 1) / kColC;
+  dim3 grid((a.W + 31) / 32, (chunks + kColWarps - 1) / kColWarps, S);
+  k_prefilter_T_cols<<<grid, 32 * kColWarps, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prefilter_T_rows_crop(const PrefilterTRowsCropArgs& a, int S, cudaStream_t st) {
+  const size_t sm = 2 * (size_t)a.N * sizeof(float);
+  if (smem_ok(sm) != cudaSuccess) return cudaErrorInvalidConfiguration;
+  dim3 grid(S, a.N0);
+  k_prefilter_T_rows_crop<<<grid, 128, sm, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -170,9 +170,16 @@ struct FwdTCartArgs {         // spectrum columns -> real log-polar columns -> s
   float fsc;
 };
 
-struct PrefilterTArgs {       // transposed prefilter along lines of length L, in place
-  float* img;                 // [S][H][W]
-  int H, W, along_rows;       // along_rows: lines are rows (length W); else columns (length H)
+struct PrefilterTColsArgs {   // transposed prefilter along columns, out of place
+  const float* in;            // [S][H][W]
+  float* out;                 // [S][H][W]
+  int H, W;
+};
+
+struct PrefilterTRowsCropArgs {  // transposed prefilter along rows, cropped into the caller's image
+  const float* in;            // [S][N][N]
+  float* out;                 // [S][N0][N0]
+  int N, N0, off;
 };
 
 struct CropArgs {
@@ -183,6 +190,7 @@ struct CropArgs {
 
 cudaError_t launch_fwdT_polar(const FwdTPolarArgs& a, int S, int nblk, cudaStream_t st);
 cudaError_t launch_fwdT_cart(const FwdTCartArgs& a, int S, cudaStream_t st);
-cudaError_t launch_prefilter_T(const PrefilterTArgs& a, int S, cudaStream_t st);
+cudaError_t launch_prefilter_T_cols(const PrefilterTColsArgs& a, int S, cudaStream_t st);
+cudaError_t launch_prefilter_T_rows_crop(const PrefilterTRowsCropArgs& a, int S, cudaStream_t st);
 cudaError_t launch_crop(const CropArgs& a, int S, cudaStream_t st);
 }  // namespace lpgb
