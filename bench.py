@@ -546,6 +546,25 @@ def run_ours(args):
         lp.fwd(fh, dev, out=Rh_out)
         lp.adj(Rh, dev, out=fh_out)
 
+    # the host link's copy bandwidth right now (the host is shared with other jobs, so it
+    # varies from run to run and bounds e2e when it drops below ~200 GB/s both ways)
+    def link_gbs():
+        n = min(fh.numel(), Rh_out.numel())
+        a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f.view(-1)[:n].copy_(fh.view(-1)[:n], non_blocking=True)
+        torch.cuda.synchronize()
+        a_.record(stream)
+        f.view(-1)[:n].copy_(fh.view(-1)[:n], non_blocking=True)
+        b_.record(stream)
+        torch.cuda.synchronize()
+        h2d_ = n * 4 / (a_.elapsed_time(b_) / 1e3) / 1e9
+        a_.record(stream)
+        Rh_out.view(-1)[:n].copy_(R.view(-1)[:n], non_blocking=True)
+        b_.record(stream)
+        torch.cuda.synchronize()
+        return {"h2d": round(h2d_, 1), "d2h": round(n * 4 / (a_.elapsed_time(b_) / 1e3) / 1e9, 1)}
+    link = link_gbs()
+
     for _ in range(max(2, args.warmup // 2)):
         e2e_step()
     torch.cuda.synchronize()
@@ -586,7 +605,7 @@ def run_ours(args):
                        "precompute_s": round(t_pre, 2), "schedule": sched, "autotune_s": round(t_tune, 2)},
             "plain_value": plain, "batched_over_plain": value / plain / ws,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "matches_device_result": e2e_ok},
+                    "matches_device_result": e2e_ok, "link_gbs_before": link},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
