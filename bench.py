@@ -39,7 +39,7 @@ ALGO_BYTES_PER_SLICE = 1.541e9
 # with the slice count)
 NCU_DRAM_BYTES_PER_SLICE = {
     "fwd_ingest": (134.2e6 + 85.5e6) / 8, "col_prefilter": (165.4e6 + 117.9e6) / 8,
-    "fwd_c2lp": (129.1e6 + 100.0e6) / 8, "theta_conv": (168.3e6 + 79.8e6) / 8,
+    "fwd_c2lp": (129.7e6 + 121.7e6) / 8, "theta_conv": (168.2e6 + 79.9e6) / 8,
     "fwd_lp2polar": (143.8e6 + 44.2e6) / 8, "adj_ingest": (196.7e6 + 150.5e6) / 8,
     "adj_polar2lp": (83.2e6 + 87.9e6) / 8, "adj_lpcols": (135.6e6 + 92.3e6) / 8,
     "adj_lp2cart": (354.1e6 + 117.2e6) / 8,
