@@ -196,6 +196,9 @@ struct lp_handle {
   int fwd_tblock = 256, adj_tblock = 256;  // threads per block of the theta convolution
   cudaStream_t side = nullptr;        // second stream of a 2-stream schedule
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // spans 1 and 2 of a call of few slices run on their own streams (spread_spans)
+  cudaStream_t span_st[2] = {nullptr, nullptr};
+  cudaEvent_t ev_sfork = nullptr, ev_sjoin[2] = {nullptr, nullptr};
 };
 
 static void free_fwd(FwdDev* f) {
@@ -397,6 +400,37 @@ static inline int to_fixed(double x, int F) { return std::isnan(x) ? LP_FX_NONE 
 // first interpolation tap of a fixed-point coordinate (the kernels' v >> F)
 static inline int first_tap(int v, int F, int cubic) { return (v >> F) - (cubic ? 1 : 0); }
 
+static void destroy_span_streams(lp_handle* h) {
+  for (int i = 0; i < 2; ++i) {
+    if (h->span_st[i]) cudaStreamDestroy(h->span_st[i]);
+    if (h->ev_sjoin[i]) cudaEventDestroy(h->ev_sjoin[i]);
+  }
+  if (h->ev_sfork) cudaEventDestroy(h->ev_sfork);
+}
+
+// A call of at most kSpreadSlices slices, run as one chunk, runs its three spans
+// concurrently: span k on its own stream (span 0 on the caller's) in spectrum
+// slots slot + k*n.  Small grids leave most SMs idle, and the spans are
+// independent from the prefiltered input until the forward's output rows
+// (disjoint per span) or the adjoint's final sum (after the join).
+constexpr int kSpreadSlices = 8;
+static bool spread_spans(const lp_handle* h, int slot, int n, bool one_chunk) {
+  return one_chunk && n <= kSpreadSlices && slot + 3 * n <= h->Nslices;
+}
+static cudaError_t span_fork(lp_handle* h, cudaStream_t st) {
+  cudaError_t e = cudaEventRecord(h->ev_sfork, st);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(h->span_st[i], h->ev_sfork, 0);
+  return e;
+}
+static cudaError_t span_join(lp_handle* h, cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+    e = cudaEventRecord(h->ev_sjoin[i], h->span_st[i]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, h->ev_sjoin[i], 0);
+  }
+  return e;
+}
+
 static cudaEvent_t take_event(lp_handle* h) {
   if (!h->evpool.empty()) {
     cudaEvent_t e = h->evpool.back();
@@ -506,6 +540,11 @@ int lp_create(const float* glpars, int64_t n, int device, lp_handle** out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+    e = cudaStreamCreateWithFlags(&h->span_st[i], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_sjoin[i], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_sfork, cudaEventDisableTiming);
   h->plan_rho = make_fft_plan(h->Nrho, h->tw_rho.p);
   h->plan_th = make_fft_plan(h->Nth, h->tw_th.p);
   h->plan_filt = h->plan_rho;
@@ -517,6 +556,7 @@ int lp_create(const float* glpars, int64_t n, int device, lp_handle** out) {
     if (h->side) cudaStreamDestroy(h->side);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
+    destroy_span_streams(h);
     delete h;
     return set_err(e == cudaErrorMemoryAllocation ? LP_ERR_OOM : LP_ERR_CUDA, "lp_create: %s",
                    cudaGetErrorString(e));
@@ -897,6 +937,7 @@ int lp_destroy(lp_handle* h) {
   if (h->side) cudaStreamDestroy(h->side);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
+  destroy_span_streams(h);
   delete h;
   return LP_OK;
 }
@@ -982,8 +1023,9 @@ static int run_chunks(lp_handle* h, cudaStream_t st, int S0, int chunk, int stre
   return LP_OK;
 }
 
-// forward transform of slices [s0, s0 + n) of the call (scratch slots s0..)
-static int fwd_slices(lp_handle* h, float* R, const float* f, int s0, int n, cudaStream_t st) {
+// forward transform of slices [s0, s0 + n) of the call (scratch slots s0..; with
+// spread spans also the spectrum slots up to s0 + 3n)
+static int fwd_slices(lp_handle* h, float* R, const float* f, int s0, int n, cudaStream_t st, bool one_chunk) {
   FwdDev* F = h->fwd;
   const bool tex = !F->tex_h.empty();
   f += (size_t)s0 * h->N0 * h->N0;
@@ -998,22 +1040,28 @@ static int fwd_slices(lp_handle* h, float* R, const float* f, int s0, int n, cud
     ColPrefilterArgs ca{fbuf, h->N, h->N, sf};
     CUDA_TRY(launch(h, K_COL_PREFILTER, st, [&] { return launch_col_prefilter(ca, n, st); }));
   }
+  const bool spread = spread_spans(h, s0, n, one_chunk);
+  if (spread) CUDA_TRY(span_fork(h, st));
   for (int k = 0; k < 3; ++k) {
-    FwdC2LPArgs a1{fbuf, spec, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, h->cubic,
+    const cudaStream_t sk = spread && k > 0 ? h->span_st[k - 1] : st;
+    float2* spk = spread ? spec + (size_t)k * n * spec_slice(h->Nk, h->Nth) : spec;
+    FwdC2LPArgs a1{fbuf, spk, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, h->cubic,
                    h->plan_rho, tx, F->ival.p, F->dlo, F->dhi, F->F, F->fsc};
-    CUDA_TRY(launch(h, K_FWD_C2LP, st, [&] { return launch_fwd_c2lp(a1, n, st); }));
-    ThetaConvArgs a2{spec, F->fz.p, h->Nth, h->Nk, F->dlo, F->dhi,
+    CUDA_TRY(launch(h, K_FWD_C2LP, sk, [&] { return launch_fwd_c2lp(a1, n, sk); }));
+    ThetaConvArgs a2{spk, F->fz.p, h->Nth, h->Nk, F->dlo, F->dhi,
                      F->lo & ~1, std::min(F->hi | 1, h->Nth - 1), 0, h->plan_th, h->fwd_tblock};
-    CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, n, st); }));
-    FwdLP2PolarArgs a3{spec, R, F->thc.p, F->rhoc.p, F->rows[k].p, F->nrows[k], h->N, h->N0, h->Nth,
+    CUDA_TRY(launch(h, K_THETA_CONV, sk, [&] { return launch_theta_conv(a2, n, sk); }));
+    FwdLP2PolarArgs a3{spk, R, F->thc.p, F->rhoc.p, F->rows[k].p, F->nrows[k], h->N, h->N0, h->Nth,
                        h->Nrho, h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho, F->F, F->fsc};
-    CUDA_TRY(launch(h, K_FWD_LP2POLAR, st, [&] { return launch_fwd_lp2polar(a3, n, st); }));
+    CUDA_TRY(launch(h, K_FWD_LP2POLAR, sk, [&] { return launch_fwd_lp2polar(a3, n, sk); }));
   }
+  if (spread) CUDA_TRY(span_join(h, st));
   return LP_OK;
 }
 
-// adjoint of slices [s0, s0 + n) of the call (scratch slots s0..)
-static int adj_slices(lp_handle* h, float* f, const float* R, int s0, int n, cudaStream_t st) {
+// adjoint of slices [s0, s0 + n) of the call (scratch slots s0..; with spread spans
+// also the spectrum slots up to s0 + 3n)
+static int adj_slices(lp_handle* h, float* f, const float* R, int s0, int n, cudaStream_t st, bool one_chunk) {
   AdjDev* A = h->adj;
   R += (size_t)s0 * h->Nproj0 * h->N0;
   f += (size_t)s0 * h->N0 * h->N0;
@@ -1031,23 +1079,28 @@ static int adj_slices(lp_handle* h, float* f, const float* R, int s0, int n, cud
   }
   float* G[3];
   for (int k = 0; k < 3; ++k) G[k] = A->G[k].p ? A->G[k].p + s0 * gstride : nullptr;
+  const bool spread = spread_spans(h, s0, n, one_chunk);
+  if (spread) CUDA_TRY(span_fork(h, st));
   for (int k = 0; k < 3; ++k) {
+    const cudaStream_t sk = spread && k > 0 ? h->span_st[k - 1] : st;
+    float2* spk = spread ? spec + (size_t)k * n * spec_slice(h->Nk, h->Nth) : spec;
     const bool tex = !A->tex_h[k].empty();
     if (A->chi[k] < A->clo[k]) {
       if (tex) return set_err(LP_ERR_UNSUPPORTED, "lp_adj: span %d has no log-polar points", k);
-      CUDA_TRY(cudaMemsetAsync(G[k], 0, n * gstride * sizeof(float), st));
+      CUDA_TRY(cudaMemsetAsync(G[k], 0, n * gstride * sizeof(float), sk));
       continue;
     }
-    AdjPolar2LPArgs a1{rbuf, spec, A->ta[k].p, A->sx[k].p, A->woff[k].p, A->wpt[k].p, h->N, h->Nth,
+    AdjPolar2LPArgs a1{rbuf, spk, A->ta[k].p, A->sx[k].p, A->woff[k].p, A->wpt[k].p, h->N, h->Nth,
                        h->Nrho, h->Nk, h->Nproj, h->cubic, A->clo[k], A->chi[k], h->plan_rho, A->F, A->fsc};
-    CUDA_TRY(launch(h, K_ADJ_POLAR2LP, st, [&] { return launch_adj_polar2lp(a1, n, st); }));
-    ThetaConvArgs a2{spec, A->fz.p, h->Nth, h->Nk, A->clo[k],
+    CUDA_TRY(launch(h, K_ADJ_POLAR2LP, sk, [&] { return launch_adj_polar2lp(a1, n, sk); }));
+    ThetaConvArgs a2{spk, A->fz.p, h->Nth, h->Nk, A->clo[k],
                      A->chi[k], A->lo2, A->hi2, 0, h->plan_th, h->adj_tblock};
-    CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, n, st); }));
-    AdjLPColsArgs a3{spec, G[k], h->Nth, h->Nrho, h->Nk, A->lo2, A->hi2, A->W2, h->plan_rho,
+    CUDA_TRY(launch(h, K_THETA_CONV, sk, [&] { return launch_theta_conv(a2, n, sk); }));
+    AdjLPColsArgs a3{spk, G[k], h->Nth, h->Nrho, h->Nk, A->lo2, A->hi2, A->W2, h->plan_rho,
                      tex ? A->surf[k].p + s0 : nullptr};
-    CUDA_TRY(launch(h, K_ADJ_LPCOLS, st, [&] { return launch_adj_lpcols(a3, n, st); }));
+    CUDA_TRY(launch(h, K_ADJ_LPCOLS, sk, [&] { return launch_adj_lpcols(a3, n, sk); }));
   }
+  if (spread) CUDA_TRY(span_join(h, st));
   const bool tex = !A->tex_h[0].empty();
   AdjLP2CartArgs a4{G[0], G[1], G[2], A->c2lp[0].p, A->c2lp[1].p, A->c2lp[2].p, f,
                     h->N0, h->Nth, h->Nrho, A->lo2, A->W2, h->cubic, h->N0 * h->N0,
@@ -1067,7 +1120,7 @@ int lp_fwd(lp_handle* h, float* R, const float* f, int S0, void* stream) {
   if (!R || !f) return set_err(LP_ERR_ARG, "lp_fwd: null data pointer");
   DeviceGuard g(h->device);
   return run_chunks(h, (cudaStream_t)stream, S0, h->fwd_chunk, h->fwd_streams,
-                    [&](int s0, int n, cudaStream_t st) { return fwd_slices(h, R, f, s0, n, st); });
+                    [&](int s0, int n, cudaStream_t st) { return fwd_slices(h, R, f, s0, n, st, n == S0); });
 }
 
 int lp_fwd_transpose(lp_handle* h, float* f, const float* R, int S0, void* stream) {
@@ -1119,7 +1172,7 @@ int lp_adj(lp_handle* h, float* f, const float* R, int S0, void* stream) {
   if (!R || !f) return set_err(LP_ERR_ARG, "lp_adj: null data pointer");
   DeviceGuard g(h->device);
   return run_chunks(h, (cudaStream_t)stream, S0, h->adj_chunk, h->adj_streams,
-                    [&](int s0, int n, cudaStream_t st) { return adj_slices(h, f, R, s0, n, st); });
+                    [&](int s0, int n, cudaStream_t st) { return adj_slices(h, f, R, s0, n, st, n == S0); });
 }
 
 int lp_set_schedule(lp_handle* h, const int32_t* sched, int n) {
@@ -1171,7 +1224,7 @@ static int tune_one(lp_handle* h, bool fwd, float* R, float* f, int S0, cudaStre
       if (ns == 2 && (c == 0 || (S0 + c - 1) / c < 2)) continue;
       auto one = [&] {
         return run_chunks(h, st, S0, c, ns, [&](int s0, int n, cudaStream_t s2) {
-          return fwd ? fwd_slices(h, R, f, s0, n, s2) : adj_slices(h, f, R, s0, n, s2);
+          return fwd ? fwd_slices(h, R, f, s0, n, s2, n == S0) : adj_slices(h, f, R, s0, n, s2, n == S0);
         });
       };
       rc = one();  // warm-up
