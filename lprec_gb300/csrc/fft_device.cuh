@@ -241,12 +241,21 @@ __device__ __forceinline__ void fft_stage(const CBuf in, const CBuf out, const f
   }
 }
 
-// Any prime radix > 7: direct DFT per butterfly.
+// Any odd radix R > 7 the planner leaves (primes 11, 13, 17, ...).  The thread's R
+// inputs belong to its butterfly alone, so they are twiddled and folded in place in
+// the source buffer: S_i = x_i + x_{R-i} and D_i = x_i - x_{R-i}, i = 1..h, h = (R-1)/2.
+// With c = cos(2 pi i q / R) and s = sin(2 pi i q / R),
+//   X_0 = x_0 + sum_i S_i,  X_q = x_0 + A_q + DIR i B_q,  X_{R-q} = x_0 + A_q - DIR i B_q,
+// A_q = sum_i S_i c, B_q = sum_i D_i s, so an output pair costs h complex-by-real
+// products of each kind.  The root index i q mod R advances by additions; the roots
+// come from the length-L table (exp(-2 pi i t / L) at t = m L / R).
 template <int DIR>
 __device__ void fft_stage_dyn(const CBuf in, const CBuf out, const float2* __restrict__ tw, int L, int Ns, int R,
                               int nfft, int stride) {
   const int Lr = L / R;
   const int total = nfft * Lr;
+  const int tstep = L / (Ns * R);
+  const int h = (R - 1) / 2;
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
     const int f = t / Lr;
     const int j = t - f * Lr;
@@ -254,14 +263,35 @@ __device__ void fft_stage_dyn(const CBuf in, const CBuf out, const float2* __res
     const CBuf src = in.offset(f * stride);
     const CBuf dst = out.offset(f * stride);
     const int base = (j - k) * R + k;
-    for (int q = 0; q < R; ++q) {
-      float2 acc = make_float2(0.f, 0.f);
-      for (int i = 0; i < R; ++i) {
-        // twiddle i*k/(Ns*R) and butterfly root i*q/R in units of 1/L
-        const long long e = (long long)i * k * (L / (Ns * R)) + (long long)((i * q) % R) * Lr;
-        acc = cadd(acc, cmul(src.get(j + i * Lr), twid<DIR>(tw, (int)(e % L))));
+    if (Ns > 1)
+      for (int i = 1; i < R; ++i) src.set(j + i * Lr, cmul(src.get(j + i * Lr), twid<DIR>(tw, i * k * tstep)));
+    const float2 x0 = src.get(j);
+    float2 sum = x0;
+    for (int i = 1; i <= h; ++i) {
+      const float2 a = src.get(j + i * Lr), b = src.get(j + (R - i) * Lr);
+      const float2 si = cadd(a, b);
+      src.set(j + i * Lr, si);
+      src.set(j + (R - i) * Lr, csub(a, b));
+      sum = cadd(sum, si);
+    }
+    dst.set(base, sum);
+    for (int q = 1; q <= h; ++q) {
+      float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
+      int m = 0;
+      for (int i = 1; i <= h; ++i) {
+        m += q;
+        if (m >= R) m -= R;
+        const float2 w = __ldg(tw + m * Lr);  // (cos, -sin) of 2 pi m / R
+        const float2 si = src.get(j + i * Lr), di = src.get(j + (R - i) * Lr);
+        A.x += si.x * w.x;
+        A.y += si.y * w.x;
+        B.x -= di.x * w.y;
+        B.y -= di.y * w.y;
       }
-      dst.set(base + q * Ns, acc);
+      // DIR i B = (-DIR B.y, DIR B.x)
+      const float2 iB = make_float2(-DIR * B.y, DIR * B.x);
+      dst.set(base + q * Ns, cadd(cadd(x0, A), iB));
+      dst.set(base + (R - q) * Ns, csub(cadd(x0, A), iB));
     }
   }
 }

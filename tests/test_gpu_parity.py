@@ -351,3 +351,18 @@ def test_prefilter_chunk_edges(torch_cuda, args):
     f, R = _inputs(tr.G, 2, 4)
     assert O.rel_l2(_fwd(torch_cuda, h, f), tr.fwd(f)) < TOL
     assert O.rel_l2(_adj(torch_cuda, h, R), tr.adj(R)) < TOL
+
+
+@pytest.mark.parametrize("args", [(176, 264, 88, 'cubic', 'ramp'), (272, 408, 136, 'cubic', 'shepp-logan'),
+                                  (208, 150, 104, 'linear', 'hann')])
+def test_prime_radix_lengths(torch_cuda, args):
+    """Padded sizes with a prime factor above 7 (176 = 16*11, 272 = 16*17, 208 = 16*13):
+    the generic FFT's odd-prime stage against the oracle."""
+    from lprec_gb300 import _lib
+    N0, Nproj, cor, interp, filt = args
+    packed = _lib.precompute(N0, Nproj, 2, cor, interp, filt, precision='fp64')
+    h = _handle(packed)
+    tr = O.Transform.from_packed(*packed)
+    f, R = _inputs(tr.G, 2, 6)
+    assert O.rel_l2(_fwd(torch_cuda, h, f), tr.fwd(f)) < TOL
+    assert O.rel_l2(_adj(torch_cuda, h, R), tr.adj(R)) < TOL
