@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(32 * kColWarps) k_col_prefilter_staged(ColPref
 // multiply by e^rho, FFT along rho (two real columns in one complex FFT).
 // Reference: interp mode 3 (lpRgpu.cu:263), mulexp (:267), R2C (:270).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256, 2) k_fwd_c2lp(FwdC2LPArgs a) {
+__global__ void __launch_bounds__(256, 4) k_fwd_c2lp(FwdC2LPArgs a) {
   extern __shared__ float smf[];
   CBuf A, B;
   carve(smf, a.Nrho, 1, A, B);
@@ -540,7 +540,7 @@ __global__ void __launch_bounds__(256, 2) k_fwd_c2lp(FwdC2LPArgs a) {
 // Reference: the theta half of cuFFT's 2-D R2C/C2R and `mul`
 // (lpRgpu.cu:270-277, simple_kernels.cuh:2-12).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256, 2) k_theta_conv(ThetaConvArgs a) {
+__global__ void __launch_bounds__(256, 4) k_theta_conv(ThetaConvArgs a) {
   extern __shared__ float smf[];
   CBuf A, B;
   carve(smf, a.Nth, 2, A, B);
@@ -549,15 +549,18 @@ __global__ void __launch_bounds__(256, 2) k_theta_conv(ThetaConvArgs a) {
   const int nrow = (k0 + 1 < a.Nk) ? 2 : 1;
   float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
   const int ps = fft_plane_floats(a.Nth);  // plane stride between the two rows
+  // rows k0, k0 + 1 (k0 even) are adjacent in the tiled layout: neighbouring threads
+  // take the two rows of one column, so global accesses cover 16 of every 32 bytes
   for (int i = threadIdx.x; i < 2 * a.Nth; i += blockDim.x) {
-    const int r = i / a.Nth, t = i - r * a.Nth;
+    const int r = i & 1, t = i >> 1;
     const bool in = r < nrow && t >= a.in_lo && t <= a.in_hi;
     A.offset(r * ps).set(t, in ? sp[sidx(k0 + r, t, a.Nth)] : make_float2(0.f, 0.f));
   }
   __syncthreads();
   const CBuf X = fft_block<-1>(A, B, a.plan, 2, ps);
-  for (int i = threadIdx.x; i < nrow * a.Nth; i += blockDim.x) {
-    const int r = i / a.Nth, t = i - r * a.Nth;
+  for (int i = threadIdx.x; i < 2 * a.Nth; i += blockDim.x) {
+    const int r = i & 1, t = i >> 1;
+    if (r >= nrow) continue;
     float2 w = __ldg(a.fz + sidx(k0 + r, t, a.Nth));
     if (a.conj_fz) w.y = -w.y;
     const CBuf Xr = X.offset(r * ps);
@@ -566,9 +569,9 @@ __global__ void __launch_bounds__(256, 2) k_theta_conv(ThetaConvArgs a) {
   __syncthreads();
   const CBuf Y = fft_block<1>(X, X.re == A.re ? B : A, a.plan, 2, ps);
   const int w = a.out_hi - a.out_lo + 1;
-  for (int i = threadIdx.x; i < nrow * w; i += blockDim.x) {
-    const int r = i / w, t = a.out_lo + (i - r * w);
-    sp[sidx(k0 + r, t, a.Nth)] = Y.offset(r * ps).get(t);
+  for (int i = threadIdx.x; i < 2 * w; i += blockDim.x) {
+    const int r = i & 1, t = a.out_lo + (i >> 1);
+    if (r < nrow) sp[sidx(k0 + r, t, a.Nth)] = Y.offset(r * ps).get(t);
   }
 }
 
@@ -592,7 +595,7 @@ __device__ __forceinline__ void put_pair(const CBuf& Z, int k, int Nrho, float2 
 // into the caller's sinogram (stepangles + cor window, lpRgpu.cu:191-192).
 // Reference: C2R (:277), interp mode 5 (:284).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256, 2) k_fwd_lp2polar(FwdLP2PolarArgs a) {
+__global__ void __launch_bounds__(256, 4) k_fwd_lp2polar(FwdLP2PolarArgs a) {
   extern __shared__ float smf[];
   CBuf A, B;
   carve(smf, a.Nrho, 1, A, B);
@@ -655,7 +658,7 @@ __global__ void __launch_bounds__(256, 2) k_fwd_lp2polar(FwdLP2PolarArgs a) {
 // lpRgpu.cu:333-382) as one complex FFT of length 4N for both rows, and the
 // row (s direction) prefilter.  Rows between angle steps are written as 0.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256, 2) k_adj_ingest(AdjIngestArgs a) {
+__global__ void __launch_bounds__(256, 4) k_adj_ingest(AdjIngestArgs a) {
   extern __shared__ float smf[];
   const int N = a.N;
   const int M = 2 * N;  // the filter couples samples less than N apart: a 2N circular convolution is exact
@@ -716,7 +719,7 @@ __global__ void __launch_bounds__(256, 2) k_adj_ingest(AdjIngestArgs a) {
 // points add a direct 2-D sample.  Then FFT along rho.
 // Reference: interp mode 4 for lpids and wids (lpRgpu.cu:307, :311), R2C (:314).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256, 2) k_adj_polar2lp(AdjPolar2LPArgs a) {
+__global__ void __launch_bounds__(256, 4) k_adj_polar2lp(AdjPolar2LPArgs a) {
   extern __shared__ float smf[];
   CBuf A, B;
   float* prof = carve(smf, a.Nrho, 1, A, B);  // 2 x N
@@ -790,7 +793,7 @@ __global__ void __launch_bounds__(256, 2) k_adj_polar2lp(AdjPolar2LPArgs a) {
 // adjoint, per span: inverse FFT along rho for two theta columns, store the
 // real log-polar columns [theta][rho] for the Cartesian gather (C2R :321).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256, 2) k_adj_lpcols(AdjLPColsArgs a) {
+__global__ void __launch_bounds__(256, 4) k_adj_lpcols(AdjLPColsArgs a) {
   extern __shared__ float smf[];
   CBuf A, B;
   carve(smf, a.Nrho, 1, A, B);
