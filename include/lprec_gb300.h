@@ -103,14 +103,19 @@ int lp_destroy(lp_handle* h);
  * Forward transform R = Radon(f) on device pointers, enqueued on `stream`
  * (a cudaStream_t; NULL = legacy default stream).  Replaces
  * lpRgpu::execFwdManyPtr(size_t Rptr, size_t fptr, int Nslices0, int gpu),
- * src/cuda/lpRgpu.cu:184-193.
+ * src/cuda/lpRgpu.cu:184-193.  Calls of few slices (S0 * N^2 <= 8 * 2048^2 and
+ * 3 * S0 <= Nslices, run as one chunk) fork their three spans onto two streams
+ * owned by the handle and join them back into `stream` with events before
+ * returning work to it, so ordering on `stream` is preserved (a captured graph
+ * gets three branches).
  */
 int lp_fwd(lp_handle* h, float* R, const float* f, int S0, void* stream);
 
 /*
  * Adjoint / filtered back-projection f = R*(filter(R)) on device pointers.
  * Replaces lpRgpu::execAdjManyPtr(size_t fptr, size_t Rptr, int Nslices0,
- * int gpu), src/cuda/lpRgpu.cu:196-207.  R is read only.
+ * int gpu), src/cuda/lpRgpu.cu:196-207.  R is read only.  Small calls run their
+ * spans concurrently as lp_fwd does (joined before the final sum).
  */
 int lp_adj(lp_handle* h, float* f, const float* R, int S0, void* stream);
 
