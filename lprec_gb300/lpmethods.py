@@ -13,7 +13,7 @@ cg, cg_exact and em run their vector updates with the library's fused kernels
 (one pass per update, the inner product it needs in the same pass, float64
 scalars kept on the device, deterministic reductions); tv, tve and tvl1 with
 the fused TV kernels (three passes per iteration besides fwdp/adjp); grad uses
-torch elementwise ops.
+torch elementwise updates and the fused per-slice inner products.
 """
 import numpy as np
 
@@ -32,15 +32,6 @@ def _dev(a, gpu):
     if isinstance(a, torch.Tensor):
         return a.to(device="cuda:%d" % gpu, dtype=torch.float32).contiguous().clone()
     return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float32)).to("cuda:%d" % gpu)
-
-
-def _dot(a, b):
-    """float64 inner product of two float32 device tensors."""
-    return (a.double() * b.double()).sum()
-
-
-def _dot_slices(a, b):
-    return (a.double() * b.double()).sum(dim=(1, 2))
 
 
 def _out(x):
@@ -104,10 +95,15 @@ def grad(lp, init_recon, tomo0, num_iter, reg_par, gpu=0):
         recon = _dev(init_recon, gpu)
         tomo = _dev(tomo0, gpu)
         S = tomo.shape[0]
+        m = recon[0].numel()
+        st = _stream(recon)
         recon0 = recon.clone()
         grad0 = torch.zeros_like(recon)
         g = torch.zeros_like(tomo)
         gr = torch.zeros_like(recon)
+        work = torch.empty(_lib.vec_work_doubles(S), dtype=torch.float64, device=recon.device)
+        num = torch.empty(S, dtype=torch.float64, device=recon.device)
+        den = torch.empty(S, dtype=torch.float64, device=recon.device)
         for i in range(num_iter):
             lp.fwdp(g, recon, gpu)
             g.sub_(tomo).mul_(2)
@@ -116,8 +112,13 @@ def grad(lp, init_recon, tomo0, num_iter, reg_par, gpu=0):
                 if i == 0:
                     lam = torch.full((S,), 1e-3, dtype=torch.float64, device=recon.device)
                 else:
+                    # Barzilai-Borwein step per slice: <dx, dg> / <dg, dg>, float64 sums of
+                    # the float32 differences (fused kernel, no float64 copies of the arrays)
                     dg = gr - grad0
-                    lam = _dot_slices(recon - recon0, dg) / _dot_slices(dg, dg)
+                    dx = recon - recon0
+                    _lib.vec_dot(dx.data_ptr(), dg.data_ptr(), m, S, work.data_ptr(), num.data_ptr(), st)
+                    _lib.vec_dot(dg.data_ptr(), dg.data_ptr(), m, S, work.data_ptr(), den.data_ptr(), st)
+                    lam = num / den
             else:
                 lam = torch.full((S,), float(reg_par), dtype=torch.float64, device=recon.device)
             recon0.copy_(recon)
