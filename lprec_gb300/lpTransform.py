@@ -234,6 +234,9 @@ class lpTransform:
         if xt.dtype != torch.float32 or xt.device.type != "cpu":
             raise ValueError("expected a float32 host array")
         xt = xt.contiguous()
+        ishape = (h.N0, h.N0) if op == "fwd" else (h.Nproj, h.N0)
+        if xt.dim() != 3 or tuple(xt.shape[1:]) != ishape:
+            raise ValueError("%s: input must be [S0,%d,%d], got %s" % (op, ishape[0], ishape[1], tuple(xt.shape)))
         S = xt.shape[0]
         oshape = (S, h.Nproj, h.N0) if op == "fwd" else (S, h.N0, h.N0)
         if out is None:

@@ -187,3 +187,27 @@ def test_pipeline_chunks(S, c):
         assert sizes[0] <= c // 8 and sizes[-1] <= c // 8
     with pytest.raises(ValueError):
         pipeline_chunks(0, c)
+
+
+def test_host_pipeline_rejects_bad_arrays():
+    """lpTransform.fwd/adj on host arrays check dtype and shape against the handle
+    before any device work (a stand-in handle carries the geometry)."""
+    pytest.importorskip("torch")
+    from lprec_gb300.lpTransform import lpTransform
+
+    class Geometry:
+        N0, Nproj, Nslices = 8, 12, 4
+    lp = lpTransform(8, 12, 4, 'ramp', 4, 'cubic')
+    lp.clphandle[0] = Geometry()
+    with pytest.raises(ValueError, match="input must be"):
+        lp.fwd(np.zeros((2, 8, 9), np.float32), 0)
+    with pytest.raises(ValueError, match="input must be"):
+        lp.adj(np.zeros((2, 8, 8), np.float32), 0)
+    import torch
+    with pytest.raises(ValueError, match="float32"):
+        lp.fwd(torch.zeros((2, 8, 8), dtype=torch.float64), 0)
+    with pytest.raises(ValueError, match="out has shape"):
+        lp.fwd(torch.zeros((2, 8, 8)), 0, out=torch.zeros((2, 12, 9)))
+    with pytest.raises(TypeError):
+        lp.adj(torch.zeros((2, 12, 8)), 0, out=np.zeros((2, 8, 8), np.float32))
+    lp.clphandle[0] = None
