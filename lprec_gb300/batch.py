@@ -31,18 +31,35 @@ def wait_event(ev, timeout_s, poll_s=0.001, clock=time.monotonic, sleep=time.sle
         sleep(poll_s)
 
 
+def group_requests(requests):
+    """Requests (N, Nproj, slices) grouped by geometry, smallest N first.  Returns the
+    groups as (N, Nproj, total slices, request indices) and, per request, its
+    (group, slice offset in the group, slices)."""
+    requests = [tuple(int(v) for v in r) for r in requests]
+    for N, Nproj, S in requests:
+        if N < 1 or Nproj < 1 or S < 1:
+            raise ValueError("requests need N, Nproj and slices >= 1, got %s" % ((N, Nproj, S),))
+    byg = {}
+    for i, (N, Nproj, S) in enumerate(requests):
+        byg.setdefault((N, Nproj), []).append(i)
+    groups, where = [], {}
+    for (N, Nproj), idx in sorted(byg.items(), key=lambda kv: kv[0]):
+        off = 0
+        for i in idx:
+            where[i] = (len(groups), off, requests[i][2])
+            off += requests[i][2]
+        groups.append((N, Nproj, off, idx))
+    return groups, where
+
+
 class UnevenBatch:
     def __init__(self, requests, filter_type="ramp", interp_type="cubic", gpu=0, precision="fp64"):
         self.gpu = gpu
         self.dev = torch.device("cuda", gpu)
         self.requests = [tuple(int(v) for v in r) for r in requests]
-        groups = {}
-        for i, (N, Nproj, S) in enumerate(self.requests):
-            groups.setdefault((N, Nproj), []).append(i)
+        plan, self.where = group_requests(self.requests)
         self.groups = []
-        self.where = {}
-        for (N, Nproj), idx in sorted(groups.items(), key=lambda kv: kv[0][0]):
-            total = sum(self.requests[i][2] for i in idx)
+        for N, Nproj, total, idx in plan:
             lp = lpTransform(N, Nproj, total, filter_type, N / 2, interp_type, precision)
             lp.precompute(1)
             lp.initcmem(1, gpu)
@@ -51,10 +68,6 @@ class UnevenBatch:
                      R=torch.zeros((total, Nproj, N), device=self.dev),
                      Rout=torch.zeros((total, Nproj, N), device=self.dev),
                      fout=torch.zeros((total, N, N), device=self.dev))
-            off = 0
-            for i in idx:
-                self.where[i] = (len(self.groups), off, self.requests[i][2])
-                off += self.requests[i][2]
             self.groups.append(g)
         self.graph = None
 

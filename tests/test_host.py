@@ -211,3 +211,15 @@ def test_host_pipeline_rejects_bad_arrays():
     with pytest.raises(TypeError):
         lp.adj(torch.zeros((2, 12, 8)), 0, out=np.zeros((2, 8, 8), np.float32))
     lp.clphandle[0] = None
+
+
+def test_uneven_request_grouping():
+    """Requests of the same geometry share one handle and one graph segment, smallest
+    geometry first; each request keeps its slice range in its group."""
+    pytest.importorskip("torch")
+    from lprec_gb300.batch import group_requests
+    groups, where = group_requests([(512, 768, 2), (256, 384, 3), (512, 768, 1), (256, 384, 4), (1024, 96, 1)])
+    assert groups == [(256, 384, 7, [1, 3]), (512, 768, 3, [0, 2]), (1024, 96, 1, [4])]
+    assert where == {1: (0, 0, 3), 3: (0, 3, 4), 0: (1, 0, 2), 2: (1, 2, 1), 4: (2, 0, 1)}
+    with pytest.raises(ValueError):
+        group_requests([(256, 384, 0)])
