@@ -226,9 +226,13 @@ std::vector<cd> kernel_half(const Geo& G, bool adjoint, bool ref, int nthreads) 
   std::vector<cd> cen((size_t)Nrho * Nth);
   const float twopi32 = (float)(2.0 * PI);
   HostFFT fft(NL);
+  // exp(er * log cos) does not depend on the rho row: once per sample
+  const double er = adjoint ? 0.0 : -1.0;
+  std::vector<double> mag(NL);
+  for (int i = 0; i < NL; ++i) mag[i] = exp(er * lc[i]);
   parallel_for(Nrho, nthreads, [&](int j) {
     const double kj = (double)(j - Nrho / 2);
-    double er, ei;
+    double ei;
     if (ref) {
       const double im32 = (double)(twopi32 * (float)kj);
       // NumPy divides the complex64 product by the float64 scalar with
@@ -237,13 +241,11 @@ std::vector<cd> kernel_half(const Geo& G, bool adjoint, bool ref, int nthreads) 
     } else {
       ei = (adjoint ? 2 * PI * kj : -2 * PI * kj) / rhos;
     }
-    er = adjoint ? 0.0 : -1.0;
     std::vector<cd> a(NL), b(NL);
     for (int i = 0; i < NL; ++i) {
       const double L = lc[i];
-      const double mag = exp(er * L);
       const double ph = ei * L;
-      const cd v = cd(mag * cos(ph), mag * sin(ph)) * h[i];
+      const cd v = cd(mag[i] * cos(ph), mag[i] * sin(ph)) * h[i];
       a[(i + NL / 2) % NL] = v;  // fftshift before the FFT
     }
     fft.run(a.data(), b.data());
@@ -422,43 +424,68 @@ struct Tables {
   std::vector<double> C2lp1[3], C2lp2[3], lp2p1[3], lp2p2[3], lp2p1w[3], lp2p2w[3];
 };
 
+// Rows r of a (row, column) grid processed in parallel, each appending to its own
+// buffers; the buffers are then concatenated in row order, so the result is the
+// serial loop's, element for element.
+template <typename T>
+void concat_rows(std::vector<std::vector<T>>& rows, std::vector<T>& out) {
+  size_t n = out.size();
+  for (const auto& v : rows) n += v.size();
+  out.reserve(n);
+  for (auto& v : rows) {
+    out.insert(out.end(), v.begin(), v.end());
+    std::vector<T>().swap(v);
+  }
+}
+
 // index sets and coordinates (no kernels); `ref` selects the value precision
-bool build_fwd_coords(Tables& T, bool ref, std::string& err) {
+bool build_fwd_coords(Tables& T, bool ref, std::string& err, int nthreads) {
   const Geo& G = T.G;
   const int Nth = G.Nth, Nrho = G.Nrho, N = G.N;
   const double b = G.beta, aR = G.aR;
-  const size_t L = (size_t)Nrho * Nth;
   std::vector<float> e32(Nrho), c32(Nth), s32(Nth);
   for (int r = 0; r < Nrho; ++r) e32[r] = expf_ref(G.rhosp[r]);
   for (int t = 0; t < Nth; ++t) {
     c32[t] = cosf_ref(G.thsp[t]);
     s32[t] = sinf_ref(G.thsp[t]);
   }
+  // float64 grid values for the fp64 coordinates (the same expressions, hoisted)
+  std::vector<double> e64(Nrho), c64(Nth), s64(Nth);
+  for (int r = 0; r < Nrho; ++r) e64[r] = exp((double)G.rhosp[r]);
+  for (int t = 0; t < Nth; ++t) {
+    c64[t] = cos((double)G.thsp[t]);
+    s64[t] = sin((double)G.thsp[t]);
+  }
   std::vector<int32_t> cids_k[3];
   for (int k = 0; k < 3; ++k) {
     const double c = cos(k * b + b / 2), sn = sin(k * b + b / 2);
-    std::vector<int32_t>& ids = cids_k[k];
-    for (size_t i = 0; i < L; ++i) {
-      const int r = (int)(i / Nth), t = (int)(i % Nth);
-      // mask from the float32 products, as the reference
-      const double t1 = (double)(e32[r] * c32[t]), t2 = (double)(e32[r] * s32[t]);
-      const double X = ((t1 - (1 - aR)) * c - t2 * sn) / aR;
-      double Y = ((t1 - (1 - aR)) * sn + t2 * c) / aR;
-      Y *= -1;
-      if (X * X + Y * Y <= 1) {
-        ids.push_back((int32_t)i);
-        double x = X, y = Y;
-        if (!ref) {
-          const double ee = exp((double)G.rhosp[r]);
-          const double u1 = ee * cos((double)G.thsp[t]), u2 = ee * sin((double)G.thsp[t]);
-          x = ((u1 - (1 - aR)) * c - u2 * sn) / aR;
-          y = ((u1 - (1 - aR)) * sn + u2 * c) / aR;
-          y *= -1;
+    std::vector<std::vector<int32_t>> rid(Nrho);
+    std::vector<std::vector<double>> rx(Nrho), ry(Nrho);
+    parallel_for(Nrho, nthreads, [&](int r) {
+      for (int t = 0; t < Nth; ++t) {
+        // mask from the float32 products, as the reference
+        const double t1 = (double)(e32[r] * c32[t]), t2 = (double)(e32[r] * s32[t]);
+        const double X = ((t1 - (1 - aR)) * c - t2 * sn) / aR;
+        double Y = ((t1 - (1 - aR)) * sn + t2 * c) / aR;
+        Y *= -1;
+        if (X * X + Y * Y <= 1) {
+          rid[r].push_back((int32_t)((size_t)r * Nth + t));
+          double x = X, y = Y;
+          if (!ref) {
+            const double ee = e64[r];
+            const double u1 = ee * c64[t], u2 = ee * s64[t];
+            x = ((u1 - (1 - aR)) * c - u2 * sn) / aR;
+            y = ((u1 - (1 - aR)) * sn + u2 * c) / aR;
+            y *= -1;
+          }
+          rx[r].push_back((x + 1) / 2 * (N - 1));
+          ry[r].push_back((y + 1) / 2 * (N - 1));
         }
-        T.lp2C1[k].push_back((x + 1) / 2 * (N - 1));
-        T.lp2C2[k].push_back((y + 1) / 2 * (N - 1));
       }
-    }
+    });
+    concat_rows(rid, cids_k[k]);
+    concat_rows(rx, T.lp2C1[k]);
+    concat_rows(ry, T.lp2C2[k]);
   }
   if (cids_k[0] != cids_k[1] || cids_k[0] != cids_k[2]) {
     err = "disk index sets differ between spans";
@@ -485,7 +512,7 @@ bool build_fwd_coords(Tables& T, bool ref, std::string& err) {
   return true;
 }
 
-bool build_adj_coords(Tables& T, bool ref, std::string& err) {
+bool build_adj_coords(Tables& T, bool ref, std::string& err, int nthreads) {
   const Geo& G = T.G;
   const int Nth = G.Nth, Nrho = G.Nrho, N = G.N;
   const double b = G.beta, aR = G.aR, am = G.am, g = G.g;
@@ -496,15 +523,22 @@ bool build_adj_coords(Tables& T, bool ref, std::string& err) {
   }
   const double thden = (double)(G.thsp[Nth - 1] - G.thsp[0]);
   const double rhoden = (double)(G.rhosp[Nrho - 1] - G.rhosp[0]);
+  const int na = (int)T.acids.size();
+  const int nblk = (na + 4095) / 4096;
   for (int k = 0; k < 3; ++k) {
     const double c = cos(k * b + b / 2), sn = sin(k * b + b / 2);
-    for (int32_t i : T.acids) {
-      const double x1 = lin[i % N], x2 = -lin[i / N];
-      const double z1 = aR * (x1 * c + x2 * sn) + (1 - aR);
-      const double z2 = aR * (-x1 * sn + x2 * c);
-      T.C2lp1[k].push_back((atan2(z2, z1) - (double)G.thsp[0]) / thden * (Nth - 1));
-      T.C2lp2[k].push_back((log(sqrt(z1 * z1 + z2 * z2)) - (double)G.rhosp[0]) / rhoden * (Nrho - 1));
-    }
+    T.C2lp1[k].resize(na);
+    T.C2lp2[k].resize(na);
+    parallel_for(nblk, nthreads, [&](int blk) {
+      for (int j = blk * 4096; j < std::min(na, (blk + 1) * 4096); ++j) {
+        const int32_t i = T.acids[j];
+        const double x1 = lin[i % N], x2 = -lin[i / N];
+        const double z1 = aR * (x1 * c + x2 * sn) + (1 - aR);
+        const double z2 = aR * (-x1 * sn + x2 * c);
+        T.C2lp1[k][j] = (atan2(z2, z1) - (double)G.thsp[0]) / thden * (Nth - 1);
+        T.C2lp2[k][j] = (log(sqrt(z1 * z1 + z2 * z2)) - (double)G.rhosp[0]) / rhoden * (Nrho - 1);
+      }
+    });
   }
   // log-polar grid in float32 as the reference, for the index sets
   const float lo32 = (float)(-b / 2), hi32 = (float)(b / 2);
@@ -512,36 +546,55 @@ bool build_adj_coords(Tables& T, bool ref, std::string& err) {
   std::vector<double> z2n_v;
   std::vector<int32_t> wr, wl;          // wrap candidates (right: log z2 > g; left)
   std::vector<double> wrv, wlv;
-  for (int r = 0; r < Nrho; ++r) {
-    const float z2f = expf_ref(G.rhosp[r]);
-    const double z2 = ref ? (double)z2f : exp((double)G.rhosp[r]);
-    const float lz2f = logf_ref(z2f);
-    const double lz2 = ref ? (double)lz2f : log(z2);
+  {
+    // per theta column: cos in float32 (masks) and in the value precision (hoisted)
+    std::vector<double> cm(Nth), cv(Nth);
     for (int t = 0; t < Nth; ++t) {
-      const float z1f = G.thsp[t];
-      const double cz1 = ref ? (double)cosf_ref(z1f) : cos((double)z1f);
-      // masks always from the float32 (reference) values
-      const double z2n_m = ((double)z2f - (1 - aR) * (double)cosf_ref(z1f)) / aR;
-      const double z2n = (z2 - (1 - aR) * cz1) / aR;
-      const int idx = r * Nth + t;
-      const bool inspan = (z1f >= lo32) && (z1f < hi32);
-      if (inspan && fabs(z2n_m) <= 1) {
-        T.lpids.push_back(idx);
-        z2n_v.push_back(z2n);
-      }
-      if ((double)lz2f > g) {
-        wr.push_back(idx);
-        const double vm = (exp((double)lz2f + log(am) - g) - (1 - aR) * (double)cosf_ref(z1f)) / aR;
-        const double v = (exp(lz2 + log(am) - g) - (1 - aR) * cz1) / aR;
-        wrv.push_back(inspan && fabs(vm) <= 1 ? v : NAN);
-      }
-      if ((double)lz2f < log(am) - g + drho32) {
-        wl.push_back(idx);
-        const double vm = (exp((double)lz2f - log(am) + g) - (1 - aR) * (double)cosf_ref(z1f)) / aR;
-        const double v = (exp(lz2 - log(am) + g) - (1 - aR) * cz1) / aR;
-        wlv.push_back(inspan && fabs(vm) <= 1 ? v : NAN);
-      }
+      cm[t] = (double)cosf_ref(G.thsp[t]);
+      cv[t] = ref ? cm[t] : cos((double)G.thsp[t]);
     }
+    std::vector<std::vector<int32_t>> r_lp(Nrho), r_wr(Nrho), r_wl(Nrho);
+    std::vector<std::vector<double>> r_z2n(Nrho), r_wrv(Nrho), r_wlv(Nrho);
+    parallel_for(Nrho, nthreads, [&](int r) {
+      const float z2f = expf_ref(G.rhosp[r]);
+      const double z2 = ref ? (double)z2f : exp((double)G.rhosp[r]);
+      const float lz2f = logf_ref(z2f);
+      const double lz2 = ref ? (double)lz2f : log(z2);
+      const bool right = (double)lz2f > g, left = (double)lz2f < log(am) - g + drho32;
+      const double vrm = right ? exp((double)lz2f + log(am) - g) : 0, vr = right ? exp(lz2 + log(am) - g) : 0;
+      const double vlm = left ? exp((double)lz2f - log(am) + g) : 0, vl = left ? exp(lz2 - log(am) + g) : 0;
+      for (int t = 0; t < Nth; ++t) {
+        const float z1f = G.thsp[t];
+        const double cz1 = cv[t];
+        // masks always from the float32 (reference) values
+        const double z2n_m = ((double)z2f - (1 - aR) * cm[t]) / aR;
+        const double z2n = (z2 - (1 - aR) * cz1) / aR;
+        const int idx = r * Nth + t;
+        const bool inspan = (z1f >= lo32) && (z1f < hi32);
+        if (inspan && fabs(z2n_m) <= 1) {
+          r_lp[r].push_back(idx);
+          r_z2n[r].push_back(z2n);
+        }
+        if (right) {
+          r_wr[r].push_back(idx);
+          const double vm = (vrm - (1 - aR) * cm[t]) / aR;
+          const double v = (vr - (1 - aR) * cz1) / aR;
+          r_wrv[r].push_back(inspan && fabs(vm) <= 1 ? v : NAN);
+        }
+        if (left) {
+          r_wl[r].push_back(idx);
+          const double vm = (vlm - (1 - aR) * cm[t]) / aR;
+          const double v = (vl - (1 - aR) * cz1) / aR;
+          r_wlv[r].push_back(inspan && fabs(vm) <= 1 ? v : NAN);
+        }
+      }
+    });
+    concat_rows(r_lp, T.lpids);
+    concat_rows(r_z2n, z2n_v);
+    concat_rows(r_wr, wr);
+    concat_rows(r_wrv, wrv);
+    concat_rows(r_wl, wl);
+    concat_rows(r_wlv, wlv);
   }
   // selected positions inside the wrap candidate lists
   std::vector<int64_t> lw, lw2;
@@ -638,7 +691,8 @@ extern "C" int lp_precompute_sizes(int N0, int Nproj, int Nslices, double cor, i
   Tables T;
   T.G = make_geo(N0, Nproj, Nslices, cor, cubic);
   std::string err;
-  if (!build_fwd_coords(T, true, err) || !build_adj_coords(T, true, err))
+  const int nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+  if (!build_fwd_coords(T, true, err, nthreads) || !build_adj_coords(T, true, err, nthreads))
     return lp_internal_set_err(LP_ERR_UNSUPPORTED, err.c_str());
   Sizes s = sizes_of(T, wf);
   sizes[0] = s.gl;
@@ -666,7 +720,7 @@ static int precompute_impl(int N0, int Nproj, int Nslices, double cor, int cubic
   T.G = make_geo(N0, Nproj, Nslices, cor, cubic);
   const Geo& G = T.G;
   std::string err;
-  if ((with_fwd && !build_fwd_coords(T, ref, err)) || !build_adj_coords(T, ref, err))
+  if ((with_fwd && !build_fwd_coords(T, ref, err, nthreads)) || !build_adj_coords(T, ref, err, nthreads))
     return lp_internal_set_err(LP_ERR_UNSUPPORTED, err.c_str());
   // glpars: [N, N0, Ntheta, Nrho, Nspan, Nproj, Nslices, cor, osangles, cubic] ++ erho
   const float head[10] = {(float)G.N, (float)G.N0, (float)G.Nth, (float)G.Nrho, 3.f, (float)G.Nproj,
