@@ -223,3 +223,14 @@ def test_uneven_request_grouping():
     assert where == {1: (0, 0, 3), 3: (0, 3, 4), 0: (1, 0, 2), 2: (1, 2, 1), 4: (2, 0, 1)}
     with pytest.raises(ValueError):
         group_requests([(256, 384, 0)])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "reference"])
+def test_precompute_thread_count_invariant(lib, precision):
+    """The tables are built row-parallel and concatenated in row order: one thread and
+    all threads give the same arrays, bit for bit."""
+    args = (176, 264, 1, 88.5, 'cubic', 'cosine')
+    one = lib.precompute(*args, precision=precision, nthreads=1, wide=precision == "fp64")
+    many = lib.precompute(*args, precision=precision, nthreads=0, wide=precision == "fp64")
+    for a, b in zip(one, many):
+        assert a.dtype == b.dtype and np.array_equal(a, b, equal_nan=True)
