@@ -4,7 +4,6 @@ Tables come either from the reference's own precompute (fixtures made by
 tests/golden/make_golden.py) or from this library's precompute; the oracle is
 fed exactly the same packed arrays, so any difference is the kernels'.
 """
-import glob
 import os
 
 import numpy as np

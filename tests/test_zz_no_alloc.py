@@ -7,7 +7,6 @@ allocation-free entry point takes its scratch from a fixed device array inside
 the library.  This file is collected last so that a run stopping at the first
 failure has already run every other test.
 """
-import ctypes
 
 import numpy as np
 import pytest
