@@ -234,3 +234,37 @@ def test_precompute_thread_count_invariant(lib, precision):
     many = lib.precompute(*args, precision=precision, nthreads=0, wide=precision == "fp64")
     for a, b in zip(one, many):
         assert a.dtype == b.dtype and np.array_equal(a, b, equal_nan=True)
+
+
+def test_c_header_compiles_and_links(lib, tmp_path):
+    """include/lprec_gb300.h is plain C (what a cgo/JNI/C caller includes): a C99 program
+    includes it, links liblprec_gb300.so and calls host-only entry points."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "abi.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include "lprec_gb300.h"
+int main(void) {
+  int64_t sizes[5];
+  if (lp_version() < 100) return 2;
+  if (lp_precompute_sizes(64, 96, 1, 32.0, 1, "ramp", sizes) != LP_OK) return 3;
+  if (lp_precompute_sizes(64, 96, 1, 32.0, 1, "no-such-filter", sizes) == LP_OK) return 4;
+  if (lp_last_error()[0] == 0) return 5;
+  printf("%lld %lld %lld %lld %lld\n", (long long)sizes[0], (long long)sizes[1], (long long)sizes[2],
+         (long long)sizes[3], (long long)sizes[4]);
+  return 0;
+}
+''')
+    exe = tmp_path / "abi"
+    libdir = os.path.dirname(lib.LIB_PATH)
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                    "-L", libdir, "-llprec_gb300", "-Wl,-rpath," + libdir], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, (out.returncode, out.stderr)
+    got = [int(v) for v in out.stdout.split()]
+    arrays = lib.precompute(64, 96, 1, 32.0, 'cubic', 'ramp')
+    assert got == [a.size for a in arrays]
