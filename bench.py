@@ -34,9 +34,8 @@ WORKLOAD = dict(N=2048, Nproj=3000, S=128, filter="shepp-logan", interp="cubic",
 # algorithmic HBM bytes per slice of one fwd+adj step (N=2048, Nproj=3000, batch 128)
 ALGO_BYTES_PER_SLICE = 1.541e9
 # DRAM bytes (read + write) per slice and launch measured by ncu on an 8-slice step of the
-# same geometry (profiles/ncu_full_step_n2048_s8.md: launch averages / 8); the traffic of a
-# 128-slice launch is taken as 128 times these (every term but the per-launch tables grows
-# with the slice count)
+# same geometry (launch averages / 8); the traffic of a 128-slice launch is taken as 128
+# times these (every term but the per-launch tables grows with the slice count)
 NCU_DRAM_BYTES_PER_SLICE = {
     "fwd_ingest": (134.2e6 + 85.5e6) / 8, "col_prefilter": (165.4e6 + 117.9e6) / 8,
     "fwd_c2lp": (129.7e6 + 121.7e6) / 8, "theta_conv": (168.2e6 + 79.9e6) / 8,
@@ -235,6 +234,109 @@ class CpuBaseline:
         os.unlink(self.path)
 
 
+def _fp64_init(N, Nproj, filt):
+    sys.path.insert(0, ROOT)
+    from oracle import lprec_oracle as O
+    _W["O"] = O
+    _W["tr"] = O.Transform(N, Nproj, 1, filt, N / 2, "cubic", mode="fp64", rounded=False)
+
+
+def fp64_oracle_outputs(f, noise, seed, nproc):
+    """The float64 oracle with unrounded float64 tables on one slice of the headline
+    geometry: R = fwd(f), Rn = R + Gaussian noise (noise * max|R|), FBP(Rn) with the
+    workload's filter and the unfiltered adj(Rn).  The spans run as jobs in a spawn
+    pool whose workers build the tables themselves."""
+    import multiprocessing as mp
+    from oracle import lprec_oracle as O
+    W = WORKLOAD
+    N, Nproj = W["N"], W["Nproj"]
+    t0 = time.perf_counter()
+    pool = mp.get_context("spawn").Pool(min(nproc, 6), initializer=_fp64_init, initargs=(N, Nproj, W["filter"]))
+    try:
+        tr = O.Transform(N, Nproj, 1, W["filter"], N / 2, "cubic", mode="fp64", rounded=False)
+        G = tr.G
+        o = G.N // 2 - G.N0 // 2
+        d = np.zeros((1, G.N, G.N))
+        d[:, o:o + G.N0, o:o + G.N0] = f
+        fp = O.prefilter2d(d)
+        res = pool.map(_cpu_span, [("fwd", k, fp) for k in range(3)])
+        Rfull = np.zeros((1, G.Nproj * G.N))
+        for k in range(3):
+            Rfull[:, tr.Tf["pids"][k]] += res[k]
+        c0 = G.N // 2 - G.cor
+        R = Rfull.reshape(1, G.Nproj, G.N)[:, ::G.osangles, c0:c0 + G.N0][:, :G.Nproj0]
+        rng = np.random.default_rng(seed)
+        Rn = np.float32(R + noise * np.abs(R).max() * rng.standard_normal(R.shape)).astype(np.float64)
+        dR = O.pad_sinogram(G, Rn)
+        pf = O.prefilter2d(O.apply_filter(G, dR, tr.Ta["filter"]))
+        pn = O.prefilter2d(dR)
+        res = pool.map(_cpu_span, [("adj", k, pf) for k in range(3)] + [("adj", k, pn) for k in range(3)])
+        outs = []
+        for j in range(2):
+            full = np.zeros((1, G.N * G.N))
+            for k in range(3):
+                full[:, tr.Ta["cids"]] += res[3 * j + k]
+            outs.append(full.reshape(1, G.N, G.N)[:, o:o + G.N0, o:o + G.N0])
+    finally:
+        pool.close()
+        pool.join()
+    return R, Rn, outs[0], outs[1], time.perf_counter() - t0
+
+
+def rel_l2_vs_fp64(torch, dev, nproc):
+    """Relative L2 of the GPU's fwd, unfiltered adj and FBP on one slice of the headline
+    geometry against the float64 oracle with unrounded float64 tables, for both table
+    precisions of lpTransform."""
+    from oracle import lprec_oracle as O
+    from lprec_gb300.lpTransform import lpTransform
+    W = WORKLOAD
+    N, Nproj = W["N"], W["Nproj"]
+    f = O.ellipse_phantom(N, W["ellipses"], np.random.default_rng(W["seed"]))[None]
+    R64, Rn, fbp64, adj64, secs = fp64_oracle_outputs(f, W["noise"], W["seed"], nproc)
+    out = {"slice": "one N=%d slice, %d-ellipse phantom (seed %d), %g%% noise on the adjoint input"
+                    % (N, W["ellipses"], W["seed"], 100 * W["noise"]), "oracle_seconds": round(secs, 1)}
+    fd = torch.as_tensor(np.float32(f)).to(dev)
+    Rd = torch.as_tensor(np.float32(Rn)).to(dev)
+    for prec in ("fp64", "reference"):
+        e = {}
+        for filt in ("none", W["filter"]):
+            lp = lpTransform(N, Nproj, 1, filt, N / 2, "cubic", precision=prec)
+            lp.precompute(1)
+            lp.initcmem(1, dev)
+            Ro = torch.empty((1, Nproj, N), device=dev)
+            fo = torch.empty((1, N, N), device=dev)
+            if filt == "none":
+                lp.fwdp(Ro, fd, dev)
+                e["fwd"] = O.rel_l2(Ro.cpu().double().numpy(), R64)
+            lp.adjp(fo, Rd, dev)
+            if filt == "none":
+                e["adj"] = O.rel_l2(fo.cpu().double().numpy(), adj64)
+            else:
+                e["fbp"] = O.rel_l2(fo.cpu().double().numpy(), fbp64)
+            lp.close()
+        out["tables_" + prec] = e
+    return out
+
+
+def e2e_timeline(tf, ta):
+    """Summary of the per-chunk events of one e2e step (fwd call then adj call)."""
+    def ms(a, b):
+        return a.elapsed_time(b)
+    calls = {}
+    for name, tr in (("fwd", tf), ("adj", ta)):
+        comp = sum(ms(c["c0"], c["c1"]) for c in tr)
+        gaps = sum(max(0.0, ms(tr[i]["c1"], tr[i + 1]["c0"])) for i in range(len(tr) - 1))
+        calls[name] = {"chunks": [c["slices"] for c in tr], "compute_ms": round(comp, 2),
+                       "compute_gaps_ms": round(gaps, 2),
+                       "head_exposed_ms": round(ms(tr[0]["in0"], tr[0]["c0"]), 2),
+                       "tail_exposed_ms": round(ms(tr[-1]["c1"], tr[-1]["o1"]), 2),
+                       "h2d_ms": round(sum(ms(c["in0"], c["in1"]) for c in tr), 2),
+                       "d2h_ms": round(sum(ms(c["o0"], c["o1"]) for c in tr), 2)}
+    calls["step_ms"] = round(ms(tf[0]["in0"], ta[-1]["o1"]), 2)
+    calls["between_calls_ms"] = round(ms(tf[-1]["c1"], ta[0]["c0"]), 2)
+    return calls
+
+
 def cpu_plan():
     """(processes, slices per step) that keep the host's cores busy: 6 jobs per slice."""
     cores = len(os.sched_getaffinity(0))
@@ -273,9 +375,11 @@ def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
         return
-    from lprec_gb300 import _lib
+    from oracle import lprec_oracle as O
     W = WORKLOAD
-    packed = _lib.precompute(W["N"], W["Nproj"], 1, W["N"] / 2, W["interp"], W["filter"], precision="fp64")
+    # the oracle's restatement of the reference's own float32 precompute (initsgl.py,
+    # initsfwd.py, initsadj.py): nothing of this library is loaded in this arm
+    packed = O.Transform(W["N"], W["Nproj"], 1, W["filter"], W["N"] / 2, W["interp"], mode="ref").packed()
     nproc, B = cpu_plan()
     cb = CpuBaseline(packed, nproc, B)
     try:
@@ -296,7 +400,8 @@ def run_reference(args):
                        "sample_slices_per_step": B},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nproc, "kind": "port",
                              "sample": "%d slice(s) fwd+adj per step; float64 NumPy restatement of the reference "
-                                       "algorithm (its CUDA code does not build with CUDA 13); per-slice "
+                                       "algorithm (its CUDA code does not build with CUDA 13) on tables from the "
+                                       "restatement of the reference's float32 precompute; per-slice "
                                        "preparation and the 3 spans of fwd and adj of each slice as jobs in %d "
                                        "processes" % (B, nproc)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -466,7 +571,7 @@ def run_ours(args):
         S = args.slices
     if args.small:
         N, Nproj, S = 256, 384, 8
-    lp = lpTransform(N, Nproj, S, W["filter"], N / 2, W["interp"])
+    lp = lpTransform(N, Nproj, S, W["filter"], N / 2, W["interp"], precision="fp64")
     t0 = time.perf_counter()
     lp.precompute(1)
     t_pre = time.perf_counter() - t0
@@ -576,6 +681,13 @@ def run_ours(args):
     q1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = q0.elapsed_time(q1) / ke
+    link_after = link_gbs()
+    # one more step with events around every chunk's copies and transform
+    tf_, ta_ = [], []
+    lp.fwd(fh, dev, out=Rh_out, trace=tf_)
+    lp.adj(Rh, dev, out=fh_out, trace=ta_)
+    torch.cuda.synchronize()
+    timeline = e2e_timeline(tf_, ta_)
     e2e_ms = max_over_ranks(e2e_ms, device=dev)
     e2e = ws * S / (e2e_ms / 1000.0)
     h2d = (f.numel() + R.numel()) * 4
@@ -605,7 +717,8 @@ def run_ours(args):
                        "precompute_s": round(t_pre, 2), "schedule": sched, "autotune_s": round(t_tune, 2)},
             "plain_value": plain, "batched_over_plain": value / plain / ws,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "matches_device_result": e2e_ok, "link_gbs_before": link},
+                    "matches_device_result": e2e_ok, "link_gbs_before": link, "link_gbs_after": link_after,
+                    "timeline": timeline},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
@@ -621,6 +734,8 @@ def run_ours(args):
         line["uneven_batch"] = run_uneven(torch, dev, max(2, args.steps // 2))
     if rank == 0 and not args.no_side and not args.small:
         line.update(run_side_configs(torch, dev))
+    if rank == 0 and not args.no_cpu and not args.small:
+        line["rel_l2_vs_fp64"] = rel_l2_vs_fp64(torch, dev, cpu_plan()[0])
     if rank == 0 and not args.no_cpu:
         nproc, B = cpu_plan()
         packed = lp.tables()

@@ -157,12 +157,32 @@ int lp_device_bytes(const lp_handle* h, int64_t* bytes);
  * owned by another allocator or a fixed pool and that may not call cudaMalloc
  * or cudaFree while processing.  Calls needing more scratch than the fixed
  * size (lp_noalloc_scratch_bytes) fail with LP_ERR_UNSUPPORTED.  The first
- * call on a device looks the array up (make it before any stream capture);
- * all calls share the array, so calls that overlap on the GPU race.
+ * call on a device loads the array (with lazy module loading, the CUDA
+ * default, its 64 MiB of device memory are reserved then) and looks up its
+ * address: make that first call -- S0 = 0 does only this -- before reserving
+ * a fixed pool and before any stream capture.  The address is looked up again
+ * if the device's context is recreated.  All calls share the array, so calls
+ * that overlap on the GPU race.
  */
 #define LP_NOALLOC_SCRATCH_BYTES (64LL * 1024 * 1024)
 int lp_fwd_noalloc(lp_handle* h, float* R, const float* f, int S0, void* stream);
 int lp_noalloc_scratch_bytes(const lp_handle* h, int S0, int64_t* bytes);
+/* Test hook: fill the allocation-free scratch array of `device` with `value`. */
+int lp_debug_fill_noalloc_scratch(int device, float value, void* stream);
+
+/*
+ * Helpers for device arrays handed over through __cuda_array_interface__
+ * (no reference counterpart; lprec's lpTransform.fwdp/adjp pass raw CuPy
+ * pointers unchecked, src/lprec/lpTransform.py:42-50).
+ *   lp_pointer_device  the device a pointer's memory belongs to (LP_ERR_ARG if
+ *                      it is not device or managed memory)
+ *   lp_stream_wait     make `waiter` wait for the work enqueued on `producer`
+ *                      so far (an event recorded on `producer`); the special
+ *                      handles 1 (legacy default stream) and 2 (per-thread
+ *                      default stream) are accepted as CUDA defines them
+ */
+int lp_pointer_device(const void* p, int* device);
+int lp_stream_wait(int device, void* waiter, void* producer);
 
 long long lp_launch_count(void);
 int lp_kernel_count(void);

@@ -27,7 +27,8 @@ EXPORTS = ("lp_last_error", "lp_version", "lp_precompute_sizes", "lp_precompute"
            "lp_set_schedule", "lp_get_schedule", "lp_autotune",
            "lp_precompute_f64", "lp_init_fwd_f64", "lp_init_adj_f64",
            "lp_vec_work_doubles", "lp_vec_dot", "lp_cg_step", "lp_cg_dir", "lp_em_ratio", "lp_em_step",
-           "lp_tv_prox0", "lp_tv_prox1", "lp_tv_recon")
+           "lp_tv_prox0", "lp_tv_prox1", "lp_tv_recon", "lp_debug_fill_noalloc_scratch", "lp_pointer_device",
+           "lp_stream_wait")
 
 
 class LprecError(RuntimeError):
@@ -91,6 +92,9 @@ def lib():
         "lp_set_schedule": (c_int, [c_void_p, P_i32, c_int]),
         "lp_get_schedule": (c_int, [c_void_p, P_i32, c_int]),
         "lp_autotune": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, P_f32]),
+        "lp_debug_fill_noalloc_scratch": (c_int, [c_int, ctypes.c_float, c_void_p]),
+        "lp_pointer_device": (c_int, [c_void_p, ctypes.POINTER(c_int)]),
+        "lp_stream_wait": (c_int, [c_int, c_void_p, c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -107,6 +111,23 @@ def check(rc):
 
 def _ptr(a, ctype):
     return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+def pointer_device(ptr):
+    """Device id that the memory at device pointer `ptr` belongs to."""
+    d = c_int(-1)
+    check(lib().lp_pointer_device(c_void_p(ptr), ctypes.byref(d)))
+    return d.value
+
+
+def stream_wait(device, waiter, producer):
+    """Make stream `waiter` wait for the work enqueued on stream `producer` so far."""
+    check(lib().lp_stream_wait(int(device), c_void_p(waiter), c_void_p(producer)))
+
+
+def debug_fill_noalloc_scratch(device, value, stream):
+    """Test hook: fill the allocation-free scratch array of `device` with `value`."""
+    check(lib().lp_debug_fill_noalloc_scratch(int(device), float(value), c_void_p(stream)))
 
 
 def launch_count():

@@ -53,7 +53,7 @@ def group_requests(requests):
 
 
 class UnevenBatch:
-    def __init__(self, requests, filter_type="ramp", interp_type="cubic", gpu=0, precision="fp64"):
+    def __init__(self, requests, filter_type="ramp", interp_type="cubic", gpu=0, precision="reference"):
         self.gpu = gpu
         self.dev = torch.device("cuda", gpu)
         self.requests = [tuple(int(v) for v in r) for r in requests]

@@ -1298,34 +1298,79 @@ int lp_autotune(lp_handle* h, float* R, float* f, int S0, void* stream, float ou
 // instead of the handle's buffers; it calls no allocating routine.
 //
 // Every GPU that loads this library holds the array until the process exits.
-// Its device address is looked up with cudaGetSymbolAddress on the first call
-// on each device (with that device current); make that first call before any
-// stream capture.  All calls share the array and it keeps the last call's
-// contents: calls whose work overlaps on the GPU (other streams, other host
-// threads) race on it and must be serialised by the caller.  Nothing in it has
-// to start at zero: every scratch word this path reads was written earlier in
-// the same call.
+// The array lives in this file's device module; with lazy module loading (the
+// CUDA default) the module, and with it the array's device memory, is loaded
+// by the first lp_fwd_noalloc call on a device.  So a caller that reserves a
+// fixed pool at start-up makes one call first (it may process zero slices of
+// a real handle: S0 = 0 still resolves the array), and a caller that captures
+// streams into graphs makes that first call before any capture.  The array's
+// device address is looked up with cudaGetSymbolAddress once per device and
+// context (with that device current): if the process's context on a device
+// is destroyed and recreated (cudaDeviceReset), the next call looks it up
+// again.  All calls share the array and it keeps the last call's contents:
+// calls whose work overlaps on the GPU (other streams, other host threads)
+// race on it and must be serialised by the caller.  Nothing in it has to start
+// at zero: every scratch word this path reads was written earlier in the same
+// call.
 // ---------------------------------------------------------------------------
+#include <cuda.h>  // CUcontext / CUresult types only; the driver calls are resolved at run time
+
 #include <mutex>
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[LP_NOALLOC_SCRATCH_BYTES];
 
 #define LP_NOALLOC_MAX_DEVICES 64
-static void* g_noalloc_ptr[LP_NOALLOC_MAX_DEVICES];
+struct NoallocSlot {
+  unsigned long long ctx = 0;  // driver id of the context the address belongs to (0: none yet)
+  void* ptr = nullptr;
+};
+static NoallocSlot g_noalloc[LP_NOALLOC_MAX_DEVICES];
 static std::mutex g_noalloc_mu;
 
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+
+// Process-unique id of the calling thread's current context (ids are never
+// reused, unlike context handles).  Returns false when no context is current.
+// Called with g_noalloc_mu held.
+static bool current_ctx_id(unsigned long long* id) {
+  static PfnCtxGetCurrent get_cur = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  if (!get_cur || !get_id) {
+    void* a = nullptr;
+    void* b = nullptr;
+    cudaDriverEntryPointQueryResult qa, qb;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) != cudaSuccess ||
+        qa != cudaDriverEntryPointSuccess || qb != cudaDriverEntryPointSuccess || !a || !b)
+      return false;
+    get_cur = (PfnCtxGetCurrent)a;
+    get_id = (PfnCtxGetId)b;
+  }
+  CUcontext c = nullptr;
+  if (get_cur(&c) != CUDA_SUCCESS || !c) return false;
+  return get_id(c, id) == CUDA_SUCCESS;
+}
+
+// Device address of the scratch array for `device` (which must be current).
 static int noalloc_scratch(int device, void** out) {
   if (device < 0 || device >= LP_NOALLOC_MAX_DEVICES)
     return set_err(LP_ERR_UNSUPPORTED, "lp_fwd_noalloc: device id %d too large", device);
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[device]) {
+  NoallocSlot& slot = g_noalloc[device];
+  unsigned long long id = 0;
+  const bool have = current_ctx_id(&id);
+  if (!have || !slot.ptr || slot.ctx != id) {
     void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // device is current (DeviceGuard)
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // loads the module if needed
     if (e != cudaSuccess)
       return set_err(LP_ERR_CUDA, "lp_fwd_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-    g_noalloc_ptr[device] = p;
+    if (!current_ctx_id(&id))
+      return set_err(LP_ERR_CUDA, "lp_fwd_noalloc: no current CUDA context on device %d", device);
+    slot.ctx = id;
+    slot.ptr = p;
   }
-  *out = g_noalloc_ptr[device];
+  *out = slot.ptr;
   return LP_OK;
 }
 
@@ -1333,6 +1378,8 @@ static inline size_t round256(size_t b) { return (b + 255) / 256 * 256; }
 
 extern "C" int lp_noalloc_scratch_bytes(const lp_handle* h, int S0, int64_t* bytes) {
   if (!h || !bytes) return set_err(LP_ERR_ARG, "lp_noalloc_scratch_bytes: null pointer");
+  if (S0 < 0 || S0 > h->Nslices)
+    return set_err(LP_ERR_ARG, "lp_noalloc_scratch_bytes: S0=%d outside [0, %d]", S0, h->Nslices);
   *bytes = (int64_t)(round256((size_t)S0 * h->N * h->N * sizeof(float)) +
                      round256((size_t)S0 * spec_slice(h->Nk, h->Nth) * sizeof(float2)));
   return LP_OK;
@@ -1343,8 +1390,7 @@ extern "C" int lp_fwd_noalloc(lp_handle* h, float* R, const float* f, int S0, vo
   if (!h->fwd) return set_err(LP_ERR_STATE, "lp_fwd_noalloc: forward tables not initialised (lp_init_fwd)");
   if (S0 < 0 || S0 > h->Nslices)
     return set_err(LP_ERR_ARG, "lp_fwd_noalloc: S0=%d outside [0, %d]", S0, h->Nslices);
-  if (S0 == 0) return LP_OK;
-  if (!R || !f) return set_err(LP_ERR_ARG, "lp_fwd_noalloc: null data pointer");
+  if (S0 > 0 && (!R || !f)) return set_err(LP_ERR_ARG, "lp_fwd_noalloc: null data pointer");
   const size_t fbytes = round256((size_t)S0 * h->N * h->N * sizeof(float));
   const size_t sbytes = round256((size_t)S0 * spec_slice(h->Nk, h->Nth) * sizeof(float2));
   if (fbytes + sbytes > (size_t)LP_NOALLOC_SCRATCH_BYTES)
@@ -1356,6 +1402,7 @@ extern "C" int lp_fwd_noalloc(lp_handle* h, float* R, const float* f, int S0, vo
   void* base = nullptr;
   int rc = noalloc_scratch(h->device, &base);
   if (rc != LP_OK) return rc;
+  if (S0 == 0) return LP_OK;  // set-up only: the array is resolved (and its module loaded)
   float* fbuf = (float*)base;
   float2* spec = (float2*)((unsigned char*)base + fbytes);
   cudaStream_t st = (cudaStream_t)stream;
@@ -1377,5 +1424,49 @@ extern "C" int lp_fwd_noalloc(lp_handle* h, float* R, const float* f, int S0, vo
                        h->Nrho, h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho, F->F, F->fsc};
     CUDA_TRY(launch(h, K_FWD_LP2POLAR, st, [&] { return launch_fwd_lp2polar(a3, S0, st); }));
   }
+  return LP_OK;
+}
+
+// Test hook: fill the whole allocation-free scratch array of `device` with
+// `value` (enqueued on `stream`), so a test can show that no later call reads
+// a word it did not write first.
+extern "C" int lp_debug_fill_noalloc_scratch(int device, float value, void* stream) {
+  DeviceGuard g(device);
+  void* base = nullptr;
+  int rc = noalloc_scratch(device, &base);
+  if (rc != LP_OK) return rc;
+  cudaError_t e = fill_async((float*)base, (size_t)LP_NOALLOC_SCRATCH_BYTES / sizeof(float), value,
+                             (cudaStream_t)stream);
+  if (e != cudaSuccess) return set_err(LP_ERR_CUDA, "lp_debug_fill_noalloc_scratch: %s", cudaGetErrorString(e));
+  return LP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Helpers for arrays that arrive through __cuda_array_interface__ (CuPy and
+// others): the device a pointer belongs to, and ordering against the stream
+// the array's producer named.
+// ---------------------------------------------------------------------------
+extern "C" int lp_pointer_device(const void* p, int* device) {
+  if (!p || !device) return set_err(LP_ERR_ARG, "lp_pointer_device: null pointer");
+  cudaPointerAttributes at;
+  cudaError_t e = cudaPointerGetAttributes(&at, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(LP_ERR_ARG, "lp_pointer_device: %s", cudaGetErrorString(e));
+  }
+  if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+    return set_err(LP_ERR_ARG, "lp_pointer_device: %p is not device memory", p);
+  *device = at.device;
+  return LP_OK;
+}
+
+extern "C" int lp_stream_wait(int device, void* waiter, void* producer) {
+  DeviceGuard g(device);
+  cudaEvent_t ev = nullptr;
+  CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  cudaError_t e = cudaEventRecord(ev, (cudaStream_t)producer);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent((cudaStream_t)waiter, ev, 0);
+  cudaEventDestroy(ev);  // released once the wait has been satisfied
+  if (e != cudaSuccess) return set_err(LP_ERR_CUDA, "lp_stream_wait: %s", cudaGetErrorString(e));
   return LP_OK;
 }

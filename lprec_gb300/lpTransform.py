@@ -11,6 +11,15 @@ Device arrays are CUDA tensors (torch) or anything exposing
 ``gpu``.  Outputs are written in place.  ``fwd``/``adj`` are host-array
 (NumPy in, NumPy out) conveniences that do not exist in the reference.
 
+``precision`` selects how the tables are evaluated.  'reference' (the default)
+repeats lprec's own float32 precompute steps (initsgl.py, initsfwd.py,
+initsadj.py), so a caller switching from lprec gets lprec's discretisation at
+lprec's precision: the same index sets, and outputs within a few 1e-6 of those
+computed from lprec's own tables.  'fp64' evaluates every table value in
+float64 and keeps it (the precision form): the outputs then sit about 1e-7 from
+a float64 evaluation of the same discretisation, while lprec's float32 tables
+sit about 3e-4 from it at N=2048.
+
 Differences from the reference, by design: errors raise ``LprecError`` instead
 of printing and resetting the device (src/cuda/callerr.cu:3-8); work is
 enqueued on the current torch stream of the device; ``filter_type`` None or
@@ -32,7 +41,14 @@ def _norm_filter(filter_type):
 
 
 def _dev_ptr(a):
-    """(pointer, shape, device) of a CUDA array-like; float32 C-contiguous required."""
+    """(pointer, shape, device, stream) of a CUDA array-like; float32 C-contiguous required.
+
+    For torch tensors the stream is None (work is enqueued on torch's current
+    stream, which orders it after the tensor's producers).  For arrays exposing
+    ``__cuda_array_interface__`` the device is the one the pointer's memory
+    belongs to, and the stream is the interface's ``stream`` entry (None when
+    the producer asks for no ordering; 1 and 2 are the legacy and per-thread
+    default streams)."""
     try:
         import torch
         if isinstance(a, torch.Tensor):
@@ -42,7 +58,7 @@ def _dev_ptr(a):
                 raise ValueError("expected float32, got %s" % a.dtype)
             if not a.is_contiguous():
                 raise ValueError("expected a C-contiguous tensor")
-            return a.data_ptr(), tuple(a.shape), a.device.index
+            return a.data_ptr(), tuple(a.shape), a.device.index, None
     except ImportError:
         pass
     iface = getattr(a, "__cuda_array_interface__", None)
@@ -50,12 +66,29 @@ def _dev_ptr(a):
         raise TypeError("expected a CUDA array (torch tensor or __cuda_array_interface__)")
     if np.dtype(iface["typestr"]) != np.float32:
         raise ValueError("expected float32")
-    if iface.get("strides") not in (None,):
-        shape = iface["shape"]
+    shape = tuple(iface["shape"])
+    if iface.get("strides") is not None:
         want = tuple(int(np.prod(shape[i + 1:])) * 4 for i in range(len(shape)))
         if tuple(iface["strides"]) != want:
             raise ValueError("expected a C-contiguous array")
-    return iface["data"][0], tuple(iface["shape"]), None
+    ptr = int(iface["data"][0])
+    dev = _lib.pointer_device(ptr) if ptr else None
+    return ptr, shape, dev, iface.get("stream")
+
+
+def _check_arrays(name, gpu, *arrs):
+    """Raise unless every array lives on device `gpu`; order the launch stream after the
+    streams that __cuda_array_interface__ producers named."""
+    for _, _, d, _ in arrs:
+        if d is not None and d != gpu:
+            raise ValueError("%s: arrays live on cuda:%d, handle on cuda:%d" % (name, d, gpu))
+    cur = None
+    for _, _, _, st in arrs:
+        if st is not None:
+            if cur is None:
+                cur = _stream(gpu)
+            if int(st) != int(cur or 0):
+                _lib.stream_wait(gpu, cur, int(st))
 
 
 def _stream(gpu):
@@ -94,7 +127,9 @@ def pipeline_chunks(S, c):
 
 
 class lpTransform:
-    def __init__(self, N, Nproj, Nslices, filter_type, cor, interp_type, precision="fp64"):
+    def __init__(self, N, Nproj, Nslices, filter_type, cor, interp_type, precision="reference"):
+        if precision not in ("reference", "fp64"):
+            raise ValueError("precision must be 'reference' or 'fp64', got %r" % (precision,))
         self.N = int(N)
         self.Nslices = int(Nslices)
         self.filter_type = _norm_filter(filter_type)
@@ -162,40 +197,37 @@ class lpTransform:
     # ---- transforms on device arrays (lpTransform.py:42-50) ---------------
     def fwdp(self, R, f, gpu):
         h = self._handle(gpu)
-        fp, fs, fd = _dev_ptr(f)
-        Rp, Rs, Rd = _dev_ptr(R)
+        fa, Ra = _dev_ptr(f), _dev_ptr(R)
+        fs, Rs = fa[1], Ra[1]
         S0 = fs[0]
         if fs[1:] != (h.N0, h.N0) or Rs != (S0, h.Nproj, h.N0):
             raise ValueError("fwdp: f must be [S0,%d,%d] and R [S0,%d,%d]; got %s, %s"
                              % (h.N0, h.N0, h.Nproj, h.N0, fs, Rs))
-        for d in (fd, Rd):
-            if d is not None and d != gpu:
-                raise ValueError("fwdp: arrays live on cuda:%d, handle on cuda:%d" % (d, gpu))
-        h.fwd(Rp, fp, S0, _stream(gpu))
+        _check_arrays("fwdp", gpu, fa, Ra)
+        h.fwd(Ra[0], fa[0], S0, _stream(gpu))
 
     def adjp(self, f, R, gpu):
         h = self._handle(gpu)
-        fp, fs, fd = _dev_ptr(f)
-        Rp, Rs, Rd = _dev_ptr(R)
+        fa, Ra = _dev_ptr(f), _dev_ptr(R)
+        fs, Rs = fa[1], Ra[1]
         S0 = Rs[0]
         if Rs[1:] != (h.Nproj, h.N0) or fs != (S0, h.N0, h.N0):
             raise ValueError("adjp: R must be [S0,%d,%d] and f [S0,%d,%d]; got %s, %s"
                              % (h.Nproj, h.N0, h.N0, h.N0, Rs, fs))
-        for d in (fd, Rd):
-            if d is not None and d != gpu:
-                raise ValueError("adjp: arrays live on cuda:%d, handle on cuda:%d" % (d, gpu))
-        h.adj(fp, Rp, S0, _stream(gpu))
+        _check_arrays("adjp", gpu, fa, Ra)
+        h.adj(fa[0], Ra[0], S0, _stream(gpu))
 
     def fwdp_T(self, f, R, gpu):
         """Exact transpose of fwdp: f[S0,N0,N0] <- Radon^T(R[S0,Nproj,N0]) (autograd backward)."""
         h = self._handle(gpu)
-        fp, fs, fd = _dev_ptr(f)
-        Rp, Rs, Rd = _dev_ptr(R)
+        fa, Ra = _dev_ptr(f), _dev_ptr(R)
+        fs, Rs = fa[1], Ra[1]
         S0 = Rs[0]
         if Rs[1:] != (h.Nproj, h.N0) or fs != (S0, h.N0, h.N0):
             raise ValueError("fwdp_T: R must be [S0,%d,%d] and f [S0,%d,%d]; got %s, %s"
                              % (h.Nproj, h.N0, h.N0, h.N0, Rs, fs))
-        h.fwd_transpose(fp, Rp, S0, _stream(gpu))
+        _check_arrays("fwdp_T", gpu, fa, Ra)
+        h.fwd_transpose(fa[0], Ra[0], S0, _stream(gpu))
 
     # ---- batch schedule (not in the reference) ------------------------------
     def autotune(self, gpu, S0=None):
@@ -219,12 +251,16 @@ class lpTransform:
         self._handle(gpu).set_schedule(**sched)
 
     # ---- host arrays, pipelined ---------------------------------------------
-    def _host_op(self, op, x, out, gpu, chunk):
+    def _host_op(self, op, x, out, gpu, chunk, trace=None):
         """Run fwdp/adjp over host arrays in slice chunks (pipeline_chunks), overlapping
         the host->device copies of the next chunks and the device->host copies of the
         previous ones with the transform of the current chunk: three streams, three
         device buffers per side, events between them.  The buffers' last-use events
-        persist across calls, so calls may be issued back to back."""
+        persist across calls, so calls may be issued back to back.
+
+        `trace`: a list to which one dict of timing events per chunk is appended
+        (keys in0/in1 around its host->device copy, c0/c1 around its transform,
+        o0/o1 around its device->host copy, and `slices`), for timelines."""
         import torch
         NB = 3  # device buffers per side
         h = self._handle(gpu)
@@ -270,26 +306,37 @@ class lpTransform:
             a, b = b, b + sizes[i]
             k = nxt[0]
             nxt[0] = (k + 1) % NB
+            tr = None
+            if trace is not None:
+                tr = {key: torch.cuda.Event(enable_timing=True) for key in ("in0", "in1", "c0", "c1", "o0", "o1")}
+                tr["slices"] = b - a
+                trace.append(tr)
             with torch.cuda.stream(s_in):
                 if done_comp[k] is not None:
                     s_in.wait_event(done_comp[k])       # buffer's previous chunk consumed
+                if tr:
+                    tr["in0"].record(s_in)
                 ins[k][:b - a].copy_(xt[a:b], non_blocking=True)
-                ev_in = torch.cuda.Event()
+                ev_in = tr["in1"] if tr else torch.cuda.Event()
                 ev_in.record(s_in)
             comp.wait_event(ev_in)
             if done_out[k] is not None:
                 comp.wait_event(done_out[k])            # output buffer drained
+            if tr:
+                tr["c0"].record(comp)
             if op == "fwd":
                 self.fwdp(outs[k][:b - a], ins[k][:b - a], gpu)
             else:
                 self.adjp(outs[k][:b - a], ins[k][:b - a], gpu)
-            ev_c = torch.cuda.Event()
+            ev_c = tr["c1"] if tr else torch.cuda.Event()
             ev_c.record(comp)
             done_comp[k] = ev_c
             with torch.cuda.stream(s_out):
                 s_out.wait_event(ev_c)
+                if tr:
+                    tr["o0"].record(s_out)
                 out[a:b].copy_(outs[k][:b - a], non_blocking=True)
-                ev_o = torch.cuda.Event()
+                ev_o = tr["o1"] if tr else torch.cuda.Event()
                 ev_o.record(s_out)
             done_out[k] = ev_o
         comp.wait_event(done_out[(nxt[0] - 1) % NB])   # the copies out run in order
@@ -298,15 +345,15 @@ class lpTransform:
             return out.numpy()
         return out
 
-    def fwd(self, f, gpu=0, out=None, chunk=None):
+    def fwd(self, f, gpu=0, out=None, chunk=None, trace=None):
         """Forward transform of host images f[S,N0,N0] -> host sinograms.  With torch
         CPU tensors the result is enqueued on the current stream (synchronise before
         reading it); NumPy input returns a NumPy array after synchronising."""
-        return self._host_op("fwd", f, out, gpu, chunk)
+        return self._host_op("fwd", f, out, gpu, chunk, trace)
 
-    def adj(self, R, gpu=0, out=None, chunk=None):
+    def adj(self, R, gpu=0, out=None, chunk=None, trace=None):
         """Adjoint / FBP of host sinograms R[S,Nproj,N0] -> host images (see fwd)."""
-        return self._host_op("adj", R, out, gpu, chunk)
+        return self._host_op("adj", R, out, gpu, chunk, trace)
 
     def close(self):
         for i, h in enumerate(self.clphandle):

@@ -21,6 +21,7 @@ kwargs    lpmethod   'fbp' (default), 'grad', 'cg', 'em', 'tv', 'tve', 'tvl1'
           gpu_list   devices (default [0]): slices are split into chunks spread over
                      them, one host thread per device
           chunk      slices per transform call (default 32; bounds device memory)
+          precision  table precision of lpTransform: 'reference' (default) or 'fp64'
 
 Slices with different centers get separate geometries (one precompute per
 distinct center and device).
@@ -81,6 +82,7 @@ def lprec(tomo, center, recon, theta, **kwargs):
     centers = np.broadcast_to(np.asarray(center, np.float64), (S,))
     filt = kwargs.get("filter_name", "ramp") if lpmethod == "fbp" else "none"
     interp = kwargs.get("interp_type", "cubic")
+    precision = kwargs.get("precision", "reference")
     num_iter = int(kwargs.get("num_iter", 64))
     reg_par = float(kwargs.get("reg_par", 0.001))
     gpus = [int(g) for g in kwargs.get("gpu_list", [0])]
@@ -91,21 +93,23 @@ def lprec(tomo, center, recon, theta, **kwargs):
     errors = []
 
     def work(gpu, jobs):
+        ops = {}
         try:
-            ops = {}
             for cor, a, b in jobs:
                 lp = ops.get(cor)
                 if lp is None:
-                    lp = lpTransform(N, Nproj, chunk, filt, cor, interp)
+                    lp = lpTransform(N, Nproj, chunk, filt, cor, interp, precision)
+                    ops[cor] = lp
                     lp.precompute(flg)
                     lp.initcmem(flg, gpu)
-                    ops[cor] = lp
                 recon[a:b] = method(lp, np.ascontiguousarray(recon[a:b]), np.ascontiguousarray(tomo[a:b],
                                     dtype=np.float32), num_iter, reg_par, gpu)
-            for lp in ops.values():
-                lp.close()
         except BaseException as e:  # re-raised in the caller's thread
             errors.append(e)
+        finally:
+            # the handles' device buffers are released whether or not a job failed
+            for lp in ops.values():
+                lp.close()
 
     threads = [threading.Thread(target=work, args=(g, jobs)) for g, jobs in plan.items() if jobs]
     for t in threads:

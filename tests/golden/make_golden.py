@@ -1,9 +1,9 @@
 """Generate the golden fixtures under tests/golden/ from the lprec reference.
 
-Run in a container where the lprec sources are mounted (default
-/root/reference, override with LPREC_REFERENCE):
+Run where the lprec sources are available, naming their root directory
+(the one holding src/lprec and tests/data) by argument or by LPREC_REFERENCE:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py <lprec-root>
 
 What it writes:
 
@@ -16,6 +16,10 @@ What it writes:
 * ``testdata.npz`` -- the reference's test inputs tests/data/f (512x512) and
   tests/data/R (384x512) as float32, used by the test_adj_many pins
   (tests/test_adj_many.py:53-62, tests/run_test.py:18-20).
+* ``rfoam.npz`` -- the reference's measured foam sinogram tests/data/Rfoam
+  (299 angles x 2016 samples, float32, in the [angle][s] order that
+  tests/test_foam.py:39-41 reads it into), used by the test_foam pins
+  (tests/run_test.py:28-32).
 """
 import os
 import sys
@@ -23,7 +27,6 @@ import types
 
 import numpy as np
 
-REF = os.environ.get('LPREC_REFERENCE', '/root/reference')
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 # cases: name -> (N0, Nproj, Nslices, cor, interp_type, filter_type)
@@ -32,10 +35,21 @@ CASES = {
     'n48_cor_shepp': (48, 72, 1, 21, 'cubic', 'shepp-logan'),
     'n32_os2_linear_hann': (32, 24, 1, 16, 'linear', 'hann'),
     'n64_cubic_none': (64, 64, 1, 32.0, 'cubic', 'none'),
+    # the small benchmark configuration: one slice N=256, 384 angles, centred, ramp
+    'n256_cubic_ramp': (256, 384, 1, 128, 'cubic', 'ramp'),
+    'n48_cubic_cosine': (48, 80, 1, 24, 'cubic', 'cosine'),
+    'n48_cubic_cosine2': (48, 64, 1, 25, 'cubic', 'cosine2'),
 }
 
 
-def load_reference():
+def reference_root():
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get('LPREC_REFERENCE')
+    if not ref or not os.path.isdir(os.path.join(ref, 'src', 'lprec')):
+        sys.exit('usage: make_golden.py <lprec-root>  (or set LPREC_REFERENCE)')
+    return ref
+
+
+def load_reference(REF):
     cp = types.ModuleType('cupy')
     for k in dir(np):
         try:
@@ -52,7 +66,8 @@ def load_reference():
 
 
 def main():
-    initsgl, initsfwd, initsadj = load_reference()
+    REF = reference_root()
+    initsgl, initsfwd, initsadj = load_reference(REF)
     for name, (N0, Nproj, S, cor, interp, filt) in CASES.items():
         P, glpars = initsgl.create_gl(N0, Nproj, S, cor, interp)
         _, fi, ff = initsfwd.create_fwd(P)
@@ -66,6 +81,10 @@ def main():
     f = np.fromfile(os.path.join(REF, 'tests/data/f'), dtype='<f4').reshape(512, 512)
     R = np.fromfile(os.path.join(REF, 'tests/data/R'), dtype='<f4').reshape(384, 512)
     np.savez_compressed(os.path.join(HERE, 'testdata.npz'), f=f, R=R)
+    # tests/test_foam.py:39-41: Nproj*N floats read as [Ns, N, Nproj], then swapaxes(1, 2)
+    Rfoam = np.fromfile(os.path.join(REF, 'tests/data/Rfoam'), dtype='<f4')[:299 * 2016]
+    Rfoam = Rfoam.reshape(2016, 299).T.copy()
+    np.savez_compressed(os.path.join(HERE, 'rfoam.npz'), R=Rfoam)
 
 
 if __name__ == '__main__':

@@ -1,0 +1,277 @@
+"""The reference's own geometries and tables on the GPU.
+
+* the small benchmark configuration (one slice, N=256, 384 angles, ramp) on the
+  reference-made packed arrays (tests/golden/packed_n256_cubic_ramp.npz): fwd,
+  unfiltered adj and FBP against the oracle fed the same arrays, and the dot test;
+* the reference's foam case (tests/test_foam.py: N=2016, 299 angles, so 10-fold
+  angle oversampling) and its off-centre case (tests/test_gpus_many_map.py:
+  N0=512, cor = N0/2 - 3, padded to N=528): the GPU fed the oracle's restatement
+  of the reference precompute (mode 'ref', bit-identical to the reference's
+  arrays, tests/test_oracle.py) against the oracle, this library's
+  reference-precision tables against the same oracle, and the reference's norm
+  pins (tests/run_test.py:28-32, :46-48) on the GPU solvers;
+* the cosine and cosine2 filters on reference-made arrays;
+* lpTransform.load_packed on reference-made arrays;
+* arrays handed over through __cuda_array_interface__ (device check, producer
+  stream ordering).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import lprec_oracle as O
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+NAMES = ['glpars', 'fwdparsi', 'fwdparamsf', 'adjparsi', 'adjparamsf']
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _packed(golden_dir, case, capacity=None):
+    z = np.load(os.path.join(golden_dir, 'packed_%s.npz' % case))
+    packed = [z[n] for n in NAMES]
+    if capacity is not None:
+        packed[0] = packed[0].copy()
+        packed[0][6] = capacity  # batch capacity (Nslices)
+    return packed
+
+
+def _without_filter(packed):
+    """The same reference arrays for filter 'none': create_adj computes every other
+    table independently of the filter, and savePadjpars appends the 4N filter values
+    last with a flag as the last integer (initsadj.py:205-244)."""
+    G = O.Transform.from_packed(*packed).G
+    ai, af = packed[3].copy(), packed[4]
+    assert ai[-1] == 1
+    ai[-1] = 0
+    return [packed[0], packed[1], packed[2], ai, af[:-4 * G.N].copy()]
+
+
+def _lp(packed, gpu=0):
+    from lprec_gb300.lpTransform import lpTransform
+    G = O.Transform.from_packed(*packed).G
+    lp = lpTransform(G.N0, G.Nproj0, G.Nslices, 'none', G.cor_f, 'cubic' if G.cubic else 'linear')
+    lp.load_packed(*packed)
+    lp.initcmem(1, gpu)
+    return lp
+
+
+def _run(torch, lp, op, x):
+    h = lp.clphandle[0]
+    xt = torch.as_tensor(np.float32(x)).cuda()
+    S = x.shape[0]
+    shape = (S, h.Nproj, h.N0) if op in ('fwd',) else (S, h.N0, h.N0)
+    out = torch.full(shape, float('nan'), device='cuda')
+    getattr(lp, op + 'p')(out, xt, 0)
+    torch.cuda.synchronize()
+    return out.cpu().numpy().astype(np.float64)
+
+
+def test_config1_reference_tables(torch_cuda, golden_dir):
+    """One slice N=256, 384 angles, cor 128, cubic, ramp, on lprec's own arrays: fwd of the
+    10-ellipse phantom (seed 0), FBP and unfiltered adj of its sinogram, each within 1e-5
+    of the oracle fed the same arrays; dot test with f, g ~ U[0,1) (seed 0)."""
+    torch = torch_cuda
+    ramp = _packed(golden_dir, 'n256_cubic_ramp')
+    none = _without_filter(ramp)
+    tr_r, tr_n = O.Transform.from_packed(*ramp), O.Transform.from_packed(*none)
+    lp_r, lp_n = _lp(ramp), _lp(none)
+    f = O.ellipse_phantom(256, 10, np.random.default_rng(0))[None]
+    R = _run(torch, lp_n, 'fwd', f)
+    Ro = tr_n.fwd(f)
+    assert O.rel_l2(R, Ro) < TOL, O.rel_l2(R, Ro)
+    Rf32 = np.float32(Ro).astype(np.float64)
+    fbp, fbpo = _run(torch, lp_r, 'adj', Rf32), tr_r.adj(Rf32)
+    assert O.rel_l2(fbp, fbpo) < TOL, O.rel_l2(fbp, fbpo)
+    adj, adjo = _run(torch, lp_n, 'adj', Rf32), tr_n.adj(Rf32)
+    assert O.rel_l2(adj, adjo) < TOL, O.rel_l2(adj, adjo)
+    rng = np.random.default_rng(0)
+    fr = rng.random((1, 256, 256), dtype=np.float32).astype(np.float64)
+    gr = rng.random((1, 384, 256), dtype=np.float32).astype(np.float64)
+    lhs = np.sum(_run(torch, lp_n, 'fwd', fr) * gr)
+    rhs = np.sum(fr * _run(torch, lp_n, 'adj', gr))
+    lho, rho = np.sum(tr_n.fwd(fr) * gr), np.sum(fr * tr_n.adj(gr))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-2          # tests/run_test.py:14-16 (random dot test)
+    assert abs(lhs - lho) / abs(lho) < TOL and abs(rhs - rho) / abs(rho) < TOL
+    lp_r.close()
+    lp_n.close()
+
+
+@pytest.mark.parametrize("case", ["n48_cubic_cosine", "n48_cubic_cosine2"])
+def test_cosine_filters_reference_tables(torch_cuda, golden_dir, case):
+    """FBP with the cosine and cosine2 filters (initsadj.py:159-162) on reference-made arrays."""
+    packed = _packed(golden_dir, case, capacity=2)
+    tr = O.Transform.from_packed(*packed)
+    lp = _lp(packed)
+    rng = np.random.default_rng(12)
+    f = rng.random((2, tr.G.N0, tr.G.N0), dtype=np.float32).astype(np.float64)
+    R = rng.random((2, tr.G.Nproj0, tr.G.N0), dtype=np.float32).astype(np.float64)
+    assert O.rel_l2(_run(torch_cuda, lp, 'fwd', f), tr.fwd(f)) < TOL
+    assert O.rel_l2(_run(torch_cuda, lp, 'adj', R), tr.adj(R)) < TOL
+    lp.close()
+
+
+@pytest.mark.parametrize("filt", ["cosine", "cosine2"])
+def test_cosine_filters_own_tables(torch_cuda, filt):
+    """The cosine filters from this library's precompute at a power-of-two size."""
+    from lprec_gb300 import _lib
+    packed = _lib.precompute(256, 384, 2, 128, 'cubic', filt, precision='fp64', wide=True)
+    tr = O.Transform.from_packed(*packed)
+    lp = _lp(packed)
+    rng = np.random.default_rng(13)
+    R = rng.random((2, 384, 256), dtype=np.float32).astype(np.float64)
+    assert O.rel_l2(_run(torch_cuda, lp, 'adj', R), tr.adj(R)) < TOL
+    lp.close()
+
+
+def test_load_packed_matches_handle(torch_cuda, golden_dir):
+    """lpTransform.load_packed on lprec's own arrays: fwdp/adjp equal the C-ABI handle fed
+    the same arrays bit for bit, and tables() returns the arrays unchanged."""
+    torch = torch_cuda
+    from lprec_gb300 import _lib
+    packed = _packed(golden_dir, 'n48_cor_shepp', capacity=2)
+    lp = _lp(packed)
+    for a, b in zip(lp.tables(), packed):
+        assert np.array_equal(a, b)
+    h = _lib.Handle(packed[0], 0)
+    h.init_fwd(packed[1], packed[2])
+    h.init_adj(packed[3], packed[4])
+    G = O.Transform.from_packed(*packed).G
+    rng = np.random.default_rng(14)
+    f = torch.as_tensor(rng.random((2, G.N0, G.N0), dtype=np.float32)).cuda()
+    R = torch.as_tensor(rng.random((2, G.Nproj0, G.N0), dtype=np.float32)).cuda()
+    R1, R2 = torch.empty_like(R), torch.empty_like(R)
+    f1, f2 = torch.empty_like(f), torch.empty_like(f)
+    st = torch.cuda.current_stream().cuda_stream
+    lp.fwdp(R1, f, 0)
+    lp.adjp(f1, R, 0)
+    h.fwd(R2.data_ptr(), f.data_ptr(), 2, st)
+    h.adj(f2.data_ptr(), R.data_ptr(), 2, st)
+    torch.cuda.synchronize()
+    assert torch.equal(R1, R2) and torch.equal(f1, f2)
+    lp.close()
+    h.close()
+
+
+def _ref_geometry(torch, N0, Nproj, cor, f, R):
+    """GPU on the oracle's restatement of the reference precompute (mode 'ref') against the
+    oracle, and this library's reference-precision tables against the same oracle."""
+    from lprec_gb300 import _lib
+    tref = O.Transform(N0, Nproj, 1, 'none', cor, 'cubic', mode='ref')
+    lp = _lp(list(tref.packed()))
+    Ro, fo = tref.fwd(f), tref.adj(R)
+    e = [O.rel_l2(_run(torch, lp, 'fwd', f), Ro), O.rel_l2(_run(torch, lp, 'adj', R), fo)]
+    lp.close()
+    own = _lib.precompute(N0, Nproj, 1, cor, 'cubic', 'none', precision='reference')
+    lp = _lp(own)
+    e += [O.rel_l2(_run(torch, lp, 'fwd', f), Ro), O.rel_l2(_run(torch, lp, 'adj', R), fo)]
+    lp.close()
+    return e
+
+
+def test_foam_geometry_and_pins(torch_cuda, golden_dir):
+    """tests/test_foam.py: N=2016, 299 angles (10-fold oversampling), cubic, no filter.
+    Parity on the reference's tables and on this library's reference-precision tables,
+    then the six solvers' one-sided norm pins (tests/run_test.py:28-32)."""
+    torch = torch_cuda
+    from lprec_gb300 import lpTransform, lpmethods
+    R = np.load(os.path.join(golden_dir, 'rfoam.npz'))['R'][None].astype(np.float64)
+    assert R.shape == (1, 299, 2016)
+    f = O.ellipse_phantom(2016, 10, np.random.default_rng(15))[None]
+    e = _ref_geometry(torch, 2016, 299, 1008, f, R)
+    assert max(e) < TOL, e
+    lp = lpTransform.lpTransform(2016, 299, 1, 'None', 1008, 'cubic')
+    lp.precompute(1)
+    lp.initcmem(1, 0)
+    assert lp.clphandle[0].osangles == 10
+    tomo = np.float32(R)
+    z = np.zeros((1, 2016, 2016), np.float32)
+    norms = [np.linalg.norm(lpmethods.fbp(lp, z, tomo, 0, 0, 0).astype(np.float64)),
+             np.linalg.norm(lpmethods.grad(lp, z, tomo, 64, -1, 0).astype(np.float64)),
+             np.linalg.norm(lpmethods.cg(lp, z, tomo, 16, 0, 0).astype(np.float64)),
+             np.linalg.norm(lpmethods.em(lp, z + 1e-3, tomo, 64, 0.5, 0).astype(np.float64)),
+             np.linalg.norm(lpmethods.tv(lp, z, tomo, 256, 0.001, 0).astype(np.float64)),
+             np.linalg.norm(lpmethods.tve(lp, z, tomo, 256, 0.001, 0).astype(np.float64))]
+    pins = [602.86015, 1195.5931, 1139.5114, 444.35743, 926.6204, 1003.76623]
+    print("foam norms", norms, "reference", pins)
+    assert all(np.isfinite(norms))
+    for n, p in zip(norms, pins):
+        assert n - p < 100, (norms, pins)
+    lp.close()
+
+
+def test_off_centre_geometry_and_pin(torch_cuda):
+    """tests/test_gpus_many_map.py: N0=512, 768 angles, cor = 253 (padded to N=528 =
+    16*3*11), no filter.  Parity on both table sets, then its 100 gradient iterations
+    (automatic step) on 32 slices of sin(k / (Ns*Nproj)) data and the one-sided norm pin
+    (tests/run_test.py:46-48)."""
+    torch = torch_cuda
+    from lprec_gb300 import lpTransform, lpmethods
+    rng = np.random.default_rng(16)
+    f = rng.random((1, 512, 512), dtype=np.float32).astype(np.float64)
+    R = rng.random((1, 768, 512), dtype=np.float32).astype(np.float64)
+    e = _ref_geometry(torch, 512, 768, 253, f, R)
+    assert max(e) < TOL, e
+    Ns, N, Nproj = 32, 512, 768
+    tomo = np.float32(np.sin(np.arange(0, Ns * Nproj * N) / float(Ns * Nproj))).reshape(Ns, Nproj, N)
+    lp = lpTransform.lpTransform(N, Nproj, Ns, 'None', 253, 'cubic')
+    lp.precompute(1)
+    lp.initcmem(1, 0)
+    assert lp.clphandle[0].N == 528
+    recon = lpmethods.grad(lp, np.zeros((Ns, N, N), np.float32) + 1e-3, tomo, 100, -1, 0)
+    norm = np.linalg.norm(recon.astype(np.float64))
+    print("off-centre grad norm", norm, "reference", 678.1923)
+    assert np.isfinite(norm) and norm - 678.1923 < 10
+    lp.close()
+
+
+class _CAIArray:
+    """A device array seen only through __cuda_array_interface__ (as CuPy presents one)."""
+
+    def __init__(self, t, stream=None):
+        self.t = t
+        self.__cuda_array_interface__ = {"shape": tuple(t.shape), "typestr": "<f4", "data": (t.data_ptr(), False),
+                                         "strides": None, "version": 3, "stream": stream}
+
+
+def test_cuda_array_interface_device_and_stream(torch_cuda):
+    """Arrays given through __cuda_array_interface__: the pointer's device is looked up (a
+    host pointer is refused), and the launch waits for the producer's stream."""
+    torch = torch_cuda
+    from lprec_gb300 import _lib
+    from lprec_gb300.lpTransform import lpTransform
+    assert _lib.pointer_device(torch.zeros(4, device='cuda').data_ptr()) == 0
+    with pytest.raises(_lib.LprecError):
+        _lib.pointer_device(torch.zeros(1024).data_ptr())
+    N, Nproj, S = 256, 384, 2
+    lp = lpTransform(N, Nproj, S, 'ramp', N / 2, 'cubic')
+    lp.precompute(1)
+    lp.initcmem(1, 0)
+    rng = np.random.default_rng(17)
+    f_host = torch.as_tensor(rng.random((S, N, N), dtype=np.float32))
+    R_ref = torch.empty((S, Nproj, N), device='cuda')
+    lp.fwdp(R_ref, f_host.cuda(), 0)
+    torch.cuda.synchronize()
+    # the producer fills the input on its own stream after a delay; the transform,
+    # launched on torch's default stream, must see the filled input
+    side = torch.cuda.Stream()
+    f_src = f_host.cuda()
+    f = torch.zeros((S, N, N), device='cuda')
+    R = torch.zeros((S, Nproj, N), device='cuda')
+    torch.cuda.synchronize()
+    with torch.cuda.stream(side):
+        if hasattr(torch.cuda, "_sleep"):
+            torch.cuda._sleep(50_000_000)
+        f.copy_(f_src, non_blocking=True)
+    lp.fwdp(_CAIArray(R), _CAIArray(f, stream=side.cuda_stream), 0)
+    torch.cuda.synchronize()
+    assert torch.equal(R, R_ref)
+    lp.close()
