@@ -365,3 +365,23 @@ def test_prime_radix_lengths(torch_cuda, args):
     f, R = _inputs(tr.G, 2, 6)
     assert O.rel_l2(_fwd(torch_cuda, h, f), tr.fwd(f)) < TOL
     assert O.rel_l2(_adj(torch_cuda, h, R), tr.adj(R)) < TOL
+
+
+@pytest.mark.parametrize("args", [(512, 768, 'cubic', 'shepp-logan', 253), (1008, 1512, 'linear', 'hann', 504),
+                                  (1536, 2304, 'cubic', 'ramp', 768), (2016, 3024, 'cubic', 'parzen', 1008)])
+def test_mixed_radix_lengths(torch_cuda, args):
+    """Padded sizes that are not powers of two, served by the mixed-radix register FFT:
+    N = 528 = 16*3*11 (an off-centre axis at N0 = 512), 1008 = 16*63, 1536 = 16*96 and
+    2016 = 16*126 (Nrho = 2N: 1056, 2016, 3072, 4032), one slice each against the oracle."""
+    from lprec_gb300 import _lib
+    N0, Nproj, interp, filt, cor = args
+    packed = _lib.precompute(N0, Nproj, 1, cor, interp, filt, precision='fp64')
+    h = _handle(packed)
+    tr = O.Transform.from_packed(*packed)
+    rng = np.random.default_rng(31)
+    f = O.ellipse_phantom(N0, 10, rng)[None]
+    Rg = _fwd(torch_cuda, h, f)
+    assert O.rel_l2(Rg, tr.fwd(f)) < TOL, O.rel_l2(Rg, tr.fwd(f))
+    Rn = Rg + 0.01 * np.abs(Rg).max() * rng.standard_normal(Rg.shape)
+    fa = _adj(torch_cuda, h, Rn)
+    assert O.rel_l2(fa, tr.adj(Rn)) < TOL, O.rel_l2(fa, tr.adj(Rn))

@@ -273,3 +273,24 @@ def test_cg_em_n512_against_fp64_oracle():
     assert e_cg < 1e-4, e_cg
     assert e_em < 5e-6, e_em
     lp.close()
+
+
+def test_grad_off_centre_against_oracle():
+    """The automatic-step gradient method on the off-centre geometry (N0=512, cor=253,
+    padded to N=528) for 4 iterations against the oracle's float64 solver on the same
+    float32 tables."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from lprec_gb300 import lpTransform, lpmethods
+    N, Nproj = 512, 768
+    lp = lpTransform.lpTransform(N, Nproj, 1, 'none', 253, 'cubic')
+    lp.precompute(1)
+    lp.initcmem(1, 0)
+    tr = O.Transform.from_packed(*lp.tables())
+    tomo = np.float32(np.sin(np.arange(0, Nproj * N) / float(32 * Nproj))).reshape(1, Nproj, N)
+    x0 = np.zeros((1, N, N), np.float32) + np.float32(1e-3)
+    g = lpmethods.grad(lp, x0, tomo, 4, -1, 0)
+    o = O.solve_grad(tr, x0.astype(np.float64), tomo.astype(np.float64), 4, -1)
+    assert O.rel_l2(g, o) < 1e-4, O.rel_l2(g, o)
+    lp.close()
