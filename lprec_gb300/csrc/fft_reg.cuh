@@ -101,7 +101,7 @@ __device__ __forceinline__ void reg_stage(float2 (&v)[16], float2* sm, int t, co
 #pragma unroll
   for (int m = 0; m < NB; ++m) {
     const int jp = t + m * T;
-    const int k = jp & (NS - 1);
+    const int k = (int)((unsigned)jp % (unsigned)NS);  // NS: any product of radices
     float2 x[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) x[i] = v[m + i * NB];
@@ -213,7 +213,7 @@ __device__ __forceinline__ void reg_stage2(float2 (&v0)[16], float2 (&v1)[16], f
 #pragma unroll
   for (int m = 0; m < NB; ++m) {
     const int jp = t + m * T;
-    const int k = jp & (NS - 1);
+    const int k = (int)((unsigned)jp % (unsigned)NS);  // NS: any product of radices
     if constexpr (NS > 1) {
       float2 w[R];
       if constexpr (NB > 1) {

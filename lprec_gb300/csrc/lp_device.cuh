@@ -1,0 +1,261 @@
+// Device helpers shared by the kernel translation units: fixed-point
+// coordinates, cubic B-spline weights, explicit interpolation with wrap
+// addressing, the chunked prefilter recursion, and the packing of two real
+// signals into one complex FFT.
+#pragma once
+#include "lp_kernels.cuh"
+#include "fft_mr.cuh"
+
+namespace lpgb {
+
+// cubic B-spline pole and gain (src/include/main_kernels.cuh:2, :124)
+#define LP_POLE (-0.2679491924311228f)
+#define LP_LAMBDA (6.0f)
+#define LP_WARM 16  // warm-up length of the chunked recursions: |pole|^16 < 1e-9
+
+__device__ __forceinline__ int wrapi(int i, int n) {
+  i %= n;
+  return i < 0 ? i + n : i;
+}
+
+// ---------------------------------------------------------------------------
+// Interpolation coordinates are stored as 32-bit fixed point: value = v * 2^-F
+// with F chosen per handle from the largest coordinate (F = 17 at N = 2048:
+// steps of 7.6e-6 texel, where float32 near 4096 steps by 4.9e-4).  The
+// integer tap position is v >> F (an arithmetic shift, i.e. floor) and the
+// fraction (v & (2^F - 1)) * 2^-F is exact in float32.  LP_FX_NONE marks a
+// table entry without a point.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int fx_int(int v, int F) { return v >> F; }
+__device__ __forceinline__ float fx_frac(int v, int F, float fsc) { return (float)(v & ((1 << F) - 1)) * fsc; }
+
+// cubic B-spline weights for taps i-1, i, i+1, i+2 at fraction f
+__device__ __forceinline__ void bspline_w(float f, float* w) {
+  const float one = 1.0f - f;
+  const float f2 = f * f;
+  const float o2 = one * one;
+  w[0] = (1.0f / 6.0f) * o2 * one;
+  w[1] = (2.0f / 3.0f) - 0.5f * f2 * (2.0f - f);
+  w[2] = (2.0f / 3.0f) - 0.5f * o2 * (2.0f - one);
+  w[3] = (1.0f / 6.0f) * f2 * f;
+}
+
+// 2-D interpolation of a row-major image (W columns, H rows) at index position
+// (x, y) with wrap addressing.
+__device__ __forceinline__ float interp2d_split(const float* __restrict__ img, int W, int H, int ix, float ax,
+                                                int iy, float ay, int cubic) {
+  if (cubic) {
+    float wx[4], wy[4];
+    bspline_w(ax, wx);
+    bspline_w(ay, wy);
+    int cx[4];
+    if (ix >= 1 && ix + 2 < W) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) cx[i] = ix - 1 + i;
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) cx[i] = wrapi(ix - 1 + i, W);
+    }
+    float acc = 0.f;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float* row = img + (size_t)wrapi(iy - 1 + j, H) * W;
+      const float r = wx[0] * __ldg(row + cx[0]) + wx[1] * __ldg(row + cx[1]) + wx[2] * __ldg(row + cx[2]) +
+                      wx[3] * __ldg(row + cx[3]);
+      acc += wy[j] * r;
+    }
+    return acc;
+  }
+  const int x0 = wrapi(ix, W), x1 = wrapi(ix + 1, W);
+  const float* r0 = img + (size_t)wrapi(iy, H) * W;
+  const float* r1 = img + (size_t)wrapi(iy + 1, H) * W;
+  return (1.f - ay) * ((1.f - ax) * __ldg(r0 + x0) + ax * __ldg(r0 + x1)) +
+         ay * ((1.f - ax) * __ldg(r1 + x0) + ax * __ldg(r1 + x1));
+}
+
+// 2-D interpolation at fixed-point index position (x, y)
+__device__ __forceinline__ float interp2d_fx(const float* __restrict__ img, int W, int H, int vx, int vy, int F,
+                                             float fsc, int cubic) {
+  return interp2d_split(img, W, H, fx_int(vx, F), fx_frac(vx, F, fsc), fx_int(vy, F), fx_frac(vy, F, fsc), cubic);
+}
+
+
+// Cubic B-spline sample of a 2-D texture (N x N texels, normalised
+// coordinates, wrap addressing) at index position (x, y) from four 2x2
+// texel gathers.  A gather at integer texel coordinate (i, j) returns the
+// raw texels of columns i-1, i and rows j-1, j -- no filtering weights are
+// involved, the B-spline weights are applied here in float32.  The 0.5-texel
+// margin of the integer position makes the quad selection insensitive to
+// coordinate rounding.  Gather component order: w (i-1, j-1), z (i, j-1),
+// x (i-1, j), y (i, j).
+__device__ __forceinline__ float interp_tex_cubic_split(cudaTextureObject_t tx, float invW, float invH, int ix,
+                                                       float ax, int iy, float ay) {
+  float wx[4], wy[4];
+  bspline_w(ax, wx);
+  bspline_w(ay, wy);
+  const float fx = (float)ix, fy = (float)iy;
+  const float u0 = fx * invW, u1 = (fx + 2.0f) * invW;
+  const float v0 = fy * invH, v1 = (fy + 2.0f) * invH;
+  const float4 q00 = tex2Dgather<float4>(tx, u0, v0, 0);
+  const float4 q10 = tex2Dgather<float4>(tx, u1, v0, 0);
+  const float4 q01 = tex2Dgather<float4>(tx, u0, v1, 0);
+  const float4 q11 = tex2Dgather<float4>(tx, u1, v1, 0);
+  const float r0 = wx[0] * q00.w + wx[1] * q00.z + wx[2] * q10.w + wx[3] * q10.z;
+  const float r1 = wx[0] * q00.x + wx[1] * q00.y + wx[2] * q10.x + wx[3] * q10.y;
+  const float r2 = wx[0] * q01.w + wx[1] * q01.z + wx[2] * q11.w + wx[3] * q11.z;
+  const float r3 = wx[0] * q01.x + wx[1] * q01.y + wx[2] * q11.x + wx[3] * q11.y;
+  return wy[0] * r0 + wy[1] * r1 + wy[2] * r2 + wy[3] * r3;
+}
+
+// the same at fixed-point texel coordinates (x, y)
+__device__ __forceinline__ float interp_tex_cubic_fx(cudaTextureObject_t tx, float invW, float invH, int vx, int vy,
+                                                    int F, float fsc) {
+  return interp_tex_cubic_split(tx, invW, invH, fx_int(vx, F), fx_frac(vx, F, fsc), fx_int(vy, F),
+                                fx_frac(vy, F, fsc));
+}
+
+// 1-D interpolation along a shared-memory line of length L (wrap).
+template <typename Get>
+__device__ __forceinline__ float interp1d_split(Get get, int L, int ix, float ax, int cubic) {
+  if (cubic) {
+    float w[4];
+    bspline_w(ax, w);
+    float acc = 0.f;
+    if (ix >= 1 && ix + 2 < L) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc += w[i] * get(ix - 1 + i);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc += w[i] * get(wrapi(ix - 1 + i, L));
+    }
+    return acc;
+  }
+  return (1.f - ax) * get(wrapi(ix, L)) + ax * get(wrapi(ix + 1, L));
+}
+
+// 1-D interpolation at fixed-point position v
+template <typename Get>
+__device__ __forceinline__ float interp1d_fx(Get get, int L, int v, int F, float fsc, int cubic) {
+  return interp1d_split(get, L, fx_int(v, F), fx_frac(v, F, fsc), cubic);
+}
+
+// Interpolation weights along one axis at fixed-point coordinate v: returns the first tap.
+__device__ __forceinline__ int axis_weights_fx(int v, int F, float fsc, int cubic, float* w) {
+  const int it = fx_int(v, F);
+  const float a = fx_frac(v, F, fsc);
+  if (cubic) {
+    bspline_w(a, w);
+    return it - 1;
+  }
+  w[0] = 1.f - a;
+  w[1] = a;
+  w[2] = 0.f;
+  w[3] = 0.f;
+  return it;
+}
+
+// Two complex FFT buffers (nfft signals of length L each) at the start of
+// dynamic shared memory; returns the first float after them.
+__device__ __forceinline__ float* carve(float* sm, int L, int nfft, CBuf& a, CBuf& b) {
+  const int pf = nfft * fft_plane_floats(L);
+  a = CBuf{sm, sm + pf};
+  b = CBuf{sm + 2 * pf, sm + 3 * pf};
+  return sm + 4 * pf;
+}
+
+// ---------------------------------------------------------------------------
+// Cubic B-spline prefilter of one line held in shared memory
+// (ConvertToInterpolationCoefficients, src/include/main_kernels.cuh:97-142).
+// The block splits the line into chunks; every chunk starts its causal and
+// anticausal recursions LP_WARM samples early from a zero state, which is
+// exact to |pole|^16 ~ 7e-10; the first and last chunk use the reference's
+// boundary initialisations.  `cp` is scratch of L floats.
+// ---------------------------------------------------------------------------
+// Lines are split into chunks of odd length C, so the threads walking their
+// chunks in lockstep (stride C) hit distinct shared-memory banks without any
+// padding.  The last chunks may be short or empty.
+__host__ __device__ inline int line_chunk(int L, int nth) { return ((L + nth - 1) / nth) | 1; }
+__device__ __forceinline__ int lpos(int p, int C) { return p; }
+// floats a line of L samples occupies
+__host__ __device__ inline int line_floats(int L, int nth) { return L; }
+
+static __device__ void prefilter_line(float* line, float* cp, int L, int tid, int nth) {
+  const float z = LP_POLE;
+  const int C = line_chunk(L, nth);
+  const int b = tid * C;
+  const int e = min(b + C, L);
+  if (b < L) {
+    float prev;
+    const int n0 = b - LP_WARM;
+    int n = 0;
+    if (n0 <= 0) {
+      const int hor = min(12, L);
+      float sum = line[lpos(0, C)];
+      float zn = z;
+      for (int i = 0; i < hor; ++i) {
+        sum += zn * line[lpos(i, C)];
+        zn *= z;
+      }
+      prev = LP_LAMBDA * sum;
+      if (b == 0) cp[lpos(0, C)] = prev;
+      n = 1;
+    } else {
+      prev = LP_LAMBDA * line[lpos(n0, C)];
+      n = n0 + 1;
+    }
+    for (; n < e; ++n) {
+      prev = LP_LAMBDA * line[lpos(n, C)] + z * prev;
+      if (n >= b) cp[lpos(n, C)] = prev;
+    }
+  }
+  __syncthreads();
+  if (b < L) {
+    const int n1 = e - 1 + LP_WARM;
+    float c;
+    int n;
+    if (n1 >= L - 1) {
+      c = (z / (z - 1.0f)) * cp[lpos(L - 1, C)];
+      if (L - 1 < e) line[lpos(L - 1, C)] = c;
+      n = L - 2;
+    } else {
+      c = -z * cp[lpos(n1, C)];
+      n = n1 - 1;
+    }
+    for (; n >= b; --n) {
+      c = z * (c - cp[lpos(n, C)]);
+      if (n < e) line[lpos(n, C)] = c;
+    }
+  }
+  __syncthreads();
+}
+
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+
+// Build the complex signal whose inverse FFT gives two real rho profiles
+// from their half spectra V0, V1 (kr = 0..Nrho/2); C2R semantics: the
+// imaginary parts at kr = 0 and kr = Nrho/2 are ignored.
+__device__ __forceinline__ void put_pair(const CBuf& Z, int k, int Nrho, float2 v0, float2 v1) {
+  const int half = Nrho / 2;
+  if (k == 0 || k == half) {
+    Z.set(k, make_float2(v0.x, v1.x));
+  } else {
+    Z.set(k, make_float2(v0.x - v1.y, v0.y + v1.x));
+    Z.set(Nrho - k, make_float2(v0.x + v1.y, v1.x - v0.y));
+  }
+}
+
+
+// element p of the complex signal whose inverse FFT gives two real profiles
+// with half spectra V0, V1 (C2R semantics: imaginary parts at 0 and L/2 ignored)
+__device__ __forceinline__ float2 pair_elem(int p, int L, float2 v0, float2 v1) {
+  const int half = L / 2;
+  if (p == 0 || p == half) return make_float2(v0.x, v1.x);
+  if (p < half) return make_float2(v0.x - v1.y, v0.y + v1.x);
+  return make_float2(v0.x + v1.y, v1.x - v0.y);  // conj(V0) + i conj(V1) at L - p
+}
+
+}  // namespace lpgb

@@ -16,231 +16,9 @@
 // Texture fetches are replaced by explicit interpolation with wrap addressing
 // at index position (x, y), which is what sampling the reference's textures
 // at (x+0.5, y+0.5) means (src/include/main_kernels.cuh:21-84).
-#include "lp_kernels.cuh"
-#include "fft_reg.cuh"
+#include "lp_p2.cuh"
 
 namespace lpgb {
-
-// cubic B-spline pole and gain (src/include/main_kernels.cuh:2, :124)
-#define LP_POLE (-0.2679491924311228f)
-#define LP_LAMBDA (6.0f)
-#define LP_WARM 16  // warm-up length of the chunked recursions: |pole|^16 < 1e-9
-
-__device__ __forceinline__ int wrapi(int i, int n) {
-  i %= n;
-  return i < 0 ? i + n : i;
-}
-
-// ---------------------------------------------------------------------------
-// Interpolation coordinates are stored as 32-bit fixed point: value = v * 2^-F
-// with F chosen per handle from the largest coordinate (F = 17 at N = 2048:
-// steps of 7.6e-6 texel, where float32 near 4096 steps by 4.9e-4).  The
-// integer tap position is v >> F (an arithmetic shift, i.e. floor) and the
-// fraction (v & (2^F - 1)) * 2^-F is exact in float32.  LP_FX_NONE marks a
-// table entry without a point.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ int fx_int(int v, int F) { return v >> F; }
-__device__ __forceinline__ float fx_frac(int v, int F, float fsc) { return (float)(v & ((1 << F) - 1)) * fsc; }
-
-// cubic B-spline weights for taps i-1, i, i+1, i+2 at fraction f
-__device__ __forceinline__ void bspline_w(float f, float* w) {
-  const float one = 1.0f - f;
-  const float f2 = f * f;
-  const float o2 = one * one;
-  w[0] = (1.0f / 6.0f) * o2 * one;
-  w[1] = (2.0f / 3.0f) - 0.5f * f2 * (2.0f - f);
-  w[2] = (2.0f / 3.0f) - 0.5f * o2 * (2.0f - one);
-  w[3] = (1.0f / 6.0f) * f2 * f;
-}
-
-// 2-D interpolation of a row-major image (W columns, H rows) at index position
-// (x, y) with wrap addressing.
-__device__ __forceinline__ float interp2d_split(const float* __restrict__ img, int W, int H, int ix, float ax,
-                                                int iy, float ay, int cubic) {
-  if (cubic) {
-    float wx[4], wy[4];
-    bspline_w(ax, wx);
-    bspline_w(ay, wy);
-    int cx[4];
-    if (ix >= 1 && ix + 2 < W) {
-#pragma unroll
-      for (int i = 0; i < 4; ++i) cx[i] = ix - 1 + i;
-    } else {
-#pragma unroll
-      for (int i = 0; i < 4; ++i) cx[i] = wrapi(ix - 1 + i, W);
-    }
-    float acc = 0.f;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const float* row = img + (size_t)wrapi(iy - 1 + j, H) * W;
-      const float r = wx[0] * __ldg(row + cx[0]) + wx[1] * __ldg(row + cx[1]) + wx[2] * __ldg(row + cx[2]) +
-                      wx[3] * __ldg(row + cx[3]);
-      acc += wy[j] * r;
-    }
-    return acc;
-  }
-  const int x0 = wrapi(ix, W), x1 = wrapi(ix + 1, W);
-  const float* r0 = img + (size_t)wrapi(iy, H) * W;
-  const float* r1 = img + (size_t)wrapi(iy + 1, H) * W;
-  return (1.f - ay) * ((1.f - ax) * __ldg(r0 + x0) + ax * __ldg(r0 + x1)) +
-         ay * ((1.f - ax) * __ldg(r1 + x0) + ax * __ldg(r1 + x1));
-}
-
-// 2-D interpolation at fixed-point index position (x, y)
-__device__ __forceinline__ float interp2d_fx(const float* __restrict__ img, int W, int H, int vx, int vy, int F,
-                                             float fsc, int cubic) {
-  return interp2d_split(img, W, H, fx_int(vx, F), fx_frac(vx, F, fsc), fx_int(vy, F), fx_frac(vy, F, fsc), cubic);
-}
-
-
-// Cubic B-spline sample of a 2-D texture (N x N texels, normalised
-// coordinates, wrap addressing) at index position (x, y) from four 2x2
-// texel gathers.  A gather at integer texel coordinate (i, j) returns the
-// raw texels of columns i-1, i and rows j-1, j -- no filtering weights are
-// involved, the B-spline weights are applied here in float32.  The 0.5-texel
-// margin of the integer position makes the quad selection insensitive to
-// coordinate rounding.  Gather component order: w (i-1, j-1), z (i, j-1),
-// x (i-1, j), y (i, j).
-__device__ __forceinline__ float interp_tex_cubic_split(cudaTextureObject_t tx, float invW, float invH, int ix,
-                                                       float ax, int iy, float ay) {
-  float wx[4], wy[4];
-  bspline_w(ax, wx);
-  bspline_w(ay, wy);
-  const float fx = (float)ix, fy = (float)iy;
-  const float u0 = fx * invW, u1 = (fx + 2.0f) * invW;
-  const float v0 = fy * invH, v1 = (fy + 2.0f) * invH;
-  const float4 q00 = tex2Dgather<float4>(tx, u0, v0, 0);
-  const float4 q10 = tex2Dgather<float4>(tx, u1, v0, 0);
-  const float4 q01 = tex2Dgather<float4>(tx, u0, v1, 0);
-  const float4 q11 = tex2Dgather<float4>(tx, u1, v1, 0);
-  const float r0 = wx[0] * q00.w + wx[1] * q00.z + wx[2] * q10.w + wx[3] * q10.z;
-  const float r1 = wx[0] * q00.x + wx[1] * q00.y + wx[2] * q10.x + wx[3] * q10.y;
-  const float r2 = wx[0] * q01.w + wx[1] * q01.z + wx[2] * q11.w + wx[3] * q11.z;
-  const float r3 = wx[0] * q01.x + wx[1] * q01.y + wx[2] * q11.x + wx[3] * q11.y;
-  return wy[0] * r0 + wy[1] * r1 + wy[2] * r2 + wy[3] * r3;
-}
-
-// the same at fixed-point texel coordinates (x, y)
-__device__ __forceinline__ float interp_tex_cubic_fx(cudaTextureObject_t tx, float invW, float invH, int vx, int vy,
-                                                    int F, float fsc) {
-  return interp_tex_cubic_split(tx, invW, invH, fx_int(vx, F), fx_frac(vx, F, fsc), fx_int(vy, F),
-                                fx_frac(vy, F, fsc));
-}
-
-// 1-D interpolation along a shared-memory line of length L (wrap).
-template <typename Get>
-__device__ __forceinline__ float interp1d_split(Get get, int L, int ix, float ax, int cubic) {
-  if (cubic) {
-    float w[4];
-    bspline_w(ax, w);
-    float acc = 0.f;
-    if (ix >= 1 && ix + 2 < L) {
-#pragma unroll
-      for (int i = 0; i < 4; ++i) acc += w[i] * get(ix - 1 + i);
-    } else {
-#pragma unroll
-      for (int i = 0; i < 4; ++i) acc += w[i] * get(wrapi(ix - 1 + i, L));
-    }
-    return acc;
-  }
-  return (1.f - ax) * get(wrapi(ix, L)) + ax * get(wrapi(ix + 1, L));
-}
-
-// 1-D interpolation at fixed-point position v
-template <typename Get>
-__device__ __forceinline__ float interp1d_fx(Get get, int L, int v, int F, float fsc, int cubic) {
-  return interp1d_split(get, L, fx_int(v, F), fx_frac(v, F, fsc), cubic);
-}
-
-// Interpolation weights along one axis at fixed-point coordinate v: returns the first tap.
-__device__ __forceinline__ int axis_weights_fx(int v, int F, float fsc, int cubic, float* w) {
-  const int it = fx_int(v, F);
-  const float a = fx_frac(v, F, fsc);
-  if (cubic) {
-    bspline_w(a, w);
-    return it - 1;
-  }
-  w[0] = 1.f - a;
-  w[1] = a;
-  w[2] = 0.f;
-  w[3] = 0.f;
-  return it;
-}
-
-// Two complex FFT buffers (nfft signals of length L each) at the start of
-// dynamic shared memory; returns the first float after them.
-__device__ __forceinline__ float* carve(float* sm, int L, int nfft, CBuf& a, CBuf& b) {
-  const int pf = nfft * fft_plane_floats(L);
-  a = CBuf{sm, sm + pf};
-  b = CBuf{sm + 2 * pf, sm + 3 * pf};
-  return sm + 4 * pf;
-}
-
-// ---------------------------------------------------------------------------
-// Cubic B-spline prefilter of one line held in shared memory
-// (ConvertToInterpolationCoefficients, src/include/main_kernels.cuh:97-142).
-// The block splits the line into chunks; every chunk starts its causal and
-// anticausal recursions LP_WARM samples early from a zero state, which is
-// exact to |pole|^16 ~ 7e-10; the first and last chunk use the reference's
-// boundary initialisations.  `cp` is scratch of L floats.
-// ---------------------------------------------------------------------------
-// Lines are split into chunks of odd length C, so the threads walking their
-// chunks in lockstep (stride C) hit distinct shared-memory banks without any
-// padding.  The last chunks may be short or empty.
-__host__ __device__ inline int line_chunk(int L, int nth) { return ((L + nth - 1) / nth) | 1; }
-__device__ __forceinline__ int lpos(int p, int C) { return p; }
-// floats a line of L samples occupies
-__host__ __device__ inline int line_floats(int L, int nth) { return L; }
-
-__device__ void prefilter_line(float* line, float* cp, int L, int tid, int nth) {
-  const float z = LP_POLE;
-  const int C = line_chunk(L, nth);
-  const int b = tid * C;
-  const int e = min(b + C, L);
-  if (b < L) {
-    float prev;
-    const int n0 = b - LP_WARM;
-    int n = 0;
-    if (n0 <= 0) {
-      const int hor = min(12, L);
-      float sum = line[lpos(0, C)];
-      float zn = z;
-      for (int i = 0; i < hor; ++i) {
-        sum += zn * line[lpos(i, C)];
-        zn *= z;
-      }
-      prev = LP_LAMBDA * sum;
-      if (b == 0) cp[lpos(0, C)] = prev;
-      n = 1;
-    } else {
-      prev = LP_LAMBDA * line[lpos(n0, C)];
-      n = n0 + 1;
-    }
-    for (; n < e; ++n) {
-      prev = LP_LAMBDA * line[lpos(n, C)] + z * prev;
-      if (n >= b) cp[lpos(n, C)] = prev;
-    }
-  }
-  __syncthreads();
-  if (b < L) {
-    const int n1 = e - 1 + LP_WARM;
-    float c;
-    int n;
-    if (n1 >= L - 1) {
-      c = (z / (z - 1.0f)) * cp[lpos(L - 1, C)];
-      if (L - 1 < e) line[lpos(L - 1, C)] = c;
-      n = L - 2;
-    } else {
-      c = -z * cp[lpos(n1, C)];
-      n = n1 - 1;
-    }
-    for (; n >= b; --n) {
-      c = z * (c - cp[lpos(n, C)]);
-      if (n < e) line[lpos(n, C)] = c;
-    }
-  }
-  __syncthreads();
-}
 
 // ---------------------------------------------------------------------------
 // forward: centre the image in the padded grid and prefilter along x
@@ -420,10 +198,6 @@ constexpr int kColC = 64;                          // output rows per warp
 constexpr int kColRows = kColC + 2 * LP_WARM;      // rows staged per warp
 constexpr int kColWarps = 4;                       // 4 x 96 x 32 floats = 48 KB per block
 
-__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
-}
 
 __global__ void __launch_bounds__(32 * kColWarps) k_col_prefilter_staged(ColPrefilterArgs a) {
   __shared__ float tile[kColWarps][kColRows][32];
@@ -572,19 +346,6 @@ __global__ void __launch_bounds__(256, 4) k_theta_conv(ThetaConvArgs a) {
   for (int i = threadIdx.x; i < 2 * w; i += blockDim.x) {
     const int r = i & 1, t = a.out_lo + (i >> 1);
     if (r < nrow) sp[sidx(k0 + r, t, a.Nth)] = Y.offset(r * ps).get(t);
-  }
-}
-
-// Build the complex signal whose inverse FFT gives two real rho profiles
-// from their half spectra V0, V1 (kr = 0..Nrho/2); C2R semantics: the
-// imaginary parts at kr = 0 and kr = Nrho/2 are ignored.
-__device__ __forceinline__ void put_pair(const CBuf& Z, int k, int Nrho, float2 v0, float2 v1) {
-  const int half = Nrho / 2;
-  if (k == 0 || k == half) {
-    Z.set(k, make_float2(v0.x, v1.x));
-  } else {
-    Z.set(k, make_float2(v0.x - v1.y, v0.y + v1.x));
-    Z.set(Nrho - k, make_float2(v0.x + v1.y, v1.x - v0.y));
   }
 }
 
@@ -903,14 +664,11 @@ static size_t smem_polar2lp(int Nrho, int N) { return fft_bytes(Nrho, 1) + 2 * (
 
 static int g_smem_optin = 48 * 1024;
 static cudaError_t smem_ok(size_t need);
-cudaError_t configure_p2_kernels(int optin);
-bool p2_fwd_c2lp(const FwdC2LPArgs& a, int S, cudaStream_t st, cudaError_t* err);
-bool p2_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st, cudaError_t* err);
-bool p2_fwd_lp2polar(const FwdLP2PolarArgs& a, int S, cudaStream_t st, cudaError_t* err);
-bool p2_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st, cudaError_t* err);
-bool p2_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st, cudaError_t* err);
-bool p2_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st, cudaError_t* err);
-// generic (any N) kernels are used when g_use_p2 is false or the size is not a power of two
+bool smem_fits(size_t need) { return smem_ok(need) == cudaSuccess; }
+// the register-FFT kernels: powers of two here, mixed lengths in lp_kernels_mr.cu
+using Pow2Lengths = Lengths<256, 512, 1024, 2048, 4096, 8192>;
+LP_DEFINE_LENGTH_SET(p2, Pow2Lengths)
+// generic (any N) kernels are used when g_use_p2 is false or no register-FFT length fits
 static bool g_use_p2 = true;
 
 // Allow every kernel the device's opt-in shared memory; launches check their
@@ -930,7 +688,8 @@ cudaError_t configure_kernels(int N) {
     e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     if (e != cudaSuccess) return e;
   }
-  return configure_p2_kernels(optin);
+  e = p2_configure(optin);
+  return e == cudaSuccess ? mr_configure(optin) : e;
 }
 
 void set_use_p2(bool on) { g_use_p2 = on; }
@@ -965,7 +724,7 @@ cudaError_t launch_col_prefilter(const ColPrefilterArgs& a, int S, cudaStream_t 
 
 cudaError_t launch_fwd_c2lp(const FwdC2LPArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && p2_fwd_c2lp(a, S, st, &pe)) return pe;
+  if (g_use_p2 && (p2_fwd_c2lp(a, S, st, &pe) || mr_fwd_c2lp(a, S, st, &pe))) return pe;
   if (smem_ok(smem_c2lp(a.Nrho)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.Nth + 1) / 2);
   k_fwd_c2lp<<<grid, kFFTThreads, smem_c2lp(a.Nrho), st>>>(a);
@@ -974,7 +733,7 @@ cudaError_t launch_fwd_c2lp(const FwdC2LPArgs& a, int S, cudaStream_t st) {
 
 cudaError_t launch_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && p2_theta_conv(a, S, st, &pe)) return pe;
+  if (g_use_p2 && (p2_theta_conv(a, S, st, &pe) || mr_theta_conv(a, S, st, &pe))) return pe;
   if (smem_ok(smem_theta(a.Nth)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.Nk + 1) / 2);
   k_theta_conv<<<grid, kFFTThreads, smem_theta(a.Nth), st>>>(a);
@@ -983,7 +742,7 @@ cudaError_t launch_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st) {
 
 cudaError_t launch_fwd_lp2polar(const FwdLP2PolarArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && p2_fwd_lp2polar(a, S, st, &pe)) return pe;
+  if (g_use_p2 && (p2_fwd_lp2polar(a, S, st, &pe) || mr_fwd_lp2polar(a, S, st, &pe))) return pe;
   if (a.nrows <= 0) return cudaSuccess;
   if (smem_ok(smem_c2lp(a.Nrho)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.nrows + 1) / 2);
@@ -993,7 +752,7 @@ cudaError_t launch_fwd_lp2polar(const FwdLP2PolarArgs& a, int S, cudaStream_t st
 
 cudaError_t launch_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && p2_adj_ingest(a, S, st, &pe)) return pe;
+  if (g_use_p2 && (p2_adj_ingest(a, S, st, &pe) || mr_adj_ingest(a, S, st, &pe))) return pe;
   if (smem_ok(smem_adj_ingest(a.N, a.H != nullptr)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.Nproj0 + 1) / 2);
   k_adj_ingest<<<grid, kFFTThreads, smem_adj_ingest(a.N, a.H != nullptr), st>>>(a);
@@ -1002,7 +761,7 @@ cudaError_t launch_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st) {
 
 cudaError_t launch_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && p2_adj_polar2lp(a, S, st, &pe)) return pe;
+  if (g_use_p2 && (p2_adj_polar2lp(a, S, st, &pe) || mr_adj_polar2lp(a, S, st, &pe))) return pe;
   if (a.chi < a.clo) return cudaSuccess;
   if (smem_ok(smem_polar2lp(a.Nrho, a.N)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.chi - a.clo + 2) / 2);
@@ -1012,7 +771,7 @@ cudaError_t launch_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st
 
 cudaError_t launch_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && p2_adj_lpcols(a, S, st, &pe)) return pe;
+  if (g_use_p2 && (p2_adj_lpcols(a, S, st, &pe) || mr_adj_lpcols(a, S, st, &pe))) return pe;
   if (smem_ok(smem_c2lp(a.Nrho)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.hi2 - a.lo2 + 2) / 2);
   k_adj_lpcols<<<grid, kFFTThreads, smem_c2lp(a.Nrho), st>>>(a);
@@ -1035,683 +794,6 @@ cudaError_t launch_adj_lp2cart(const AdjLP2CartArgs& a, int S, cudaStream_t st) 
 // threads carry 256/T signals when L < 4096.
 // ===========================================================================
 namespace lpgb {
-
-template <int L>
-struct P2 {
-  static constexpr int T = L / 16;                  // threads per signal
-  static constexpr int NSIG = T >= 256 ? 1 : 256 / T;
-  static constexpr int BLOCK = T * NSIG;
-  static constexpr int SLOTS = reg_fft_slots(L);
-  // resident blocks per SM to size registers for: as many threads as k blocks of 256
-  static constexpr int blocks(int k) { return k * 256 / BLOCK > 0 ? k * 256 / BLOCK : 1; }
-};
-
-// forward, per span: Cartesian -> log-polar gather for column pairs, e^rho, FFT along rho.
-// The disk points of a column form one rho interval (a.ival), so the two
-// columns' points are enumerated as one compact list and gathered in
-// straight-line groups of kGatherUnroll per thread (the four quads of a sample
-// in flight together) and no fetch is spent outside the disk.  Values land in
-// the zeroed shared buffer at their rho position (real part: column th,
-// imaginary part: column th+1), from which the register FFT takes its inputs.
-// Measured at N=2048: one sample per group with 6 resident blocks per SM
-// (40 registers, the shared-memory limit; 8.7 ms per step against 9.0 at 5
-// and 9.3 at 4) beats 2, 4 or 8 samples per group with 2-4 blocks: the
-// gathers' latency is hidden by more warps rather than by depth per thread.
-constexpr int kGatherUnroll = 1;
-
-template <int L>
-__global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(6)) k_fwd_c2lp_p2(FwdC2LPArgs a) {
-  extern __shared__ float2 sm2[];
-  constexpr int T = P2<L>::T;
-  const int sig = threadIdx.x / T, t = threadIdx.x % T;
-  float2* sm = sm2 + sig * P2<L>::SLOTS;
-  const int s = blockIdx.x;
-  const int th = 2 * ((a.col_lo >> 1) + blockIdx.y * P2<L>::NSIG + sig);
-  const bool live = th <= a.col_hi && th < a.Nth;
-  const bool has_b = live && th + 1 < a.Nth;
-  const int2 ia = live ? __ldg(a.ival + th) : make_int2(1, 0);
-  const int2 ib = has_b ? __ldg(a.ival + th + 1) : make_int2(1, 0);
-  const int na = max(0, ia.y - ia.x + 1), nb = max(0, ib.y - ib.x + 1);
-  const int n = na + nb;
-  const float* img = a.fbuf + (size_t)s * a.N * a.N;
-  const bool use_tex = a.tex != nullptr;
-  const cudaTextureObject_t tx = use_tex ? a.tex[s] : 0;
-  const float invN = 1.0f / (float)a.N;
-#pragma unroll
-  for (int i = 0; i < 16; ++i) sm[spad(t + i * T)] = make_float2(0.f, 0.f);
-  __syncthreads();
-  float* smf = reinterpret_cast<float*>(sm);
-  for (int j0 = 0; j0 < n; j0 += kGatherUnroll * T) {
-    float val[kGatherUnroll];
-    int pos[kGatherUnroll];
-#pragma unroll
-    for (int u = 0; u < kGatherUnroll; ++u) {
-      const int j = j0 + u * T + t;
-      const bool inb = j < n;
-      const bool isa = j < na;
-      const int r = inb ? (isa ? ia.x + j : ib.x + (j - na)) : 0;
-      const int col = (inb && !isa) ? th + 1 : th;
-      int2 p = __ldg(a.c2lp + (size_t)col * L + r);
-      const bool ok = inb && p.x != LP_FX_NONE;
-      if (!ok) p = make_int2(0, 0);
-      const float e = __ldg(a.erho + r);
-      const float v = use_tex ? interp_tex_cubic_fx(tx, invN, invN, p.x, p.y, a.F, a.fsc)
-                              : interp2d_fx(img, a.N, a.N, p.x, p.y, a.F, a.fsc, a.cubic);
-      val[u] = ok ? e * v : 0.f;
-      pos[u] = inb ? 2 * spad(r) + (isa ? 0 : 1) : -1;
-    }
-#pragma unroll
-    for (int u = 0; u < kGatherUnroll; ++u)
-      if (pos[u] >= 0) smf[pos[u]] = val[u];
-  }
-  __syncthreads();
-  float2 v[16];
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = sm[spad(t + i * T)];
-  __syncthreads();
-  reg_fft<L, -1>(v, sm, t);
-  if (!live) return;
-  float2* out = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
-  // two consecutive rho frequencies per thread and column: 16-byte stores (the
-  // pair k, k+1 of a column is adjacent in the tiled layout; k + 1 = Nk lands
-  // in the tile's padding)
-  for (int k = 2 * t; k < a.Nk; k += 2 * T) {
-    const float2 z1 = sm[spad(k)], z2 = sm[spad((L - k) & (L - 1))];
-    const float2 y1 = sm[spad(k + 1)], y2 = sm[spad(L - k - 1)];
-    *reinterpret_cast<float4*>(out + sidx(k, th, a.Nth)) =
-        make_float4(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y), 0.5f * (y1.x + y2.x), 0.5f * (y1.y - y2.y));
-    if (has_b)
-      *reinterpret_cast<float4*>(out + sidx(k, th + 1, a.Nth)) =
-          make_float4(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x), 0.5f * (y1.y + y2.y), 0.5f * (y2.x - y1.x));
-  }
-}
-
-// Theta convolution launch shape: BLK threads (256 or 512, picked per
-// geometry by the autotuner) carry NSIG = BLK / T rows (rho frequencies).  Threads are assigned so that the KT = min(4, NSIG) rows of one
-// spectrum tile alternate fastest: lane l works on row (l % KT) of the tile and
-// theta position t = l / KT, so a warp access covers 32 / KT consecutive theta
-// columns of all KT rows -- one contiguous run in the tiled layout.  The rows'
-// shared buffers are spaced by 32 / KT extra banks so that the KT rows' accesses
-// of one half-warp fall in distinct banks.
-template <int L, int BLK>
-struct TC {
-  static constexpr int T = L / 16;
-  static constexpr int BLOCK = BLK > T ? BLK : T;
-  static constexpr int NSIG = BLOCK / T;
-  static constexpr int KT = NSIG < kSpecTile ? NSIG : kSpecTile;
-  static constexpr int SLOTS = reg_fft_slots(L) + (KT > 1 ? 16 / KT : 0);
-};
-
-// per rho frequency: FFT along theta, multiply by the kernel (which carries the
-// 1/(Nrho*Ntheta) of the two unnormalised transforms), inverse; NSIG rows per block
-template <int L, int BLK>
-__global__ void __launch_bounds__(TC<L, BLK>::BLOCK, 768 / TC<L, BLK>::BLOCK) k_theta_conv_p2(ThetaConvArgs a) {
-  extern __shared__ float2 sm2[];
-  using C = TC<L, BLK>;
-  constexpr int T = C::T, KT = C::KT;
-  const int g = threadIdx.x / (KT * T), r = threadIdx.x % (KT * T);
-  const int sig = g * KT + r % KT, t = r / KT;
-  float2* sm = sm2 + sig * C::SLOTS;
-  const int s = blockIdx.x;
-  const int k = blockIdx.y * C::NSIG + sig;
-  const bool live = k < a.Nk;
-  float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, L);
-  float2 v[16];
-#pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    const int c = t + i * T;
-    v[i] = (live && c >= a.in_lo && c <= a.in_hi) ? sp[sidx(k, c, L)] : make_float2(0.f, 0.f);
-  }
-  // the forward transform leaves X[t + i*T] in v[i]: the kernel multiply needs no
-  // shared-memory round trip
-  reg_fft<L, -1, kOutRegs>(v, sm, t);
-  const int kf = live ? k : 0;
-#pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    const int c = t + i * T;
-    float2 w = __ldg(a.fz + sidx(kf, c, L));
-    if (a.conj_fz) w.y = -w.y;
-    v[i] = cmul(v[i], w);
-  }
-  reg_fft<L, 1>(v, sm, t);
-  if (!live) return;
-  for (int c = a.out_lo + t; c <= a.out_hi; c += T) sp[sidx(k, c, L)] = sm[spad(c)];
-}
-
-// Two rows per thread (used for L <= 4096; at L = 8192 the two rows spill and the
-// one-row kernel runs): the thread owns rho frequencies k, k+1 (k even, the same
-// tile, adjacent in memory), so one 16-byte access moves both rows' element of a
-// theta column, and the two transforms share their twiddles (reg_fft2).  256
-// threads carry NP = 256/T row pairs; KP = min(2, NP) pairs alternate fastest
-// across lanes (lane l: pair l % KP, position l / KP), so a warp access covers
-// 32/KP consecutive columns of 2*KP rows -- contiguous in the tiled layout.  The
-// 2*NP row buffers are signal-major (buffer j*NP + p for signal j of pair p) and
-// spaced by SLOTS (padded by 8 float2 when KP = 2) so that the pairs of a
-// half-warp fall in distinct banks.
-template <int L>
-struct TC2 {
-  static constexpr int T = L / 16;
-  static constexpr int BLOCK = 256 > T ? 256 : T;
-  static constexpr int NP = BLOCK / T;
-  static constexpr int KP = NP < 2 ? NP : 2;
-  static constexpr int SLOTS = reg_fft_slots(L) + (KP > 1 ? 8 : 0);
-  static constexpr size_t SMEM = (size_t)2 * NP * SLOTS * sizeof(float2);
-};
-
-template <int L>
-__global__ void __launch_bounds__(TC2<L>::BLOCK, 512 / TC2<L>::BLOCK) k_theta_conv2_p2(ThetaConvArgs a) {
-  extern __shared__ float2 sm2[];
-  using C = TC2<L>;
-  constexpr int T = C::T, KP = C::KP;
-  const int g = threadIdx.x / (KP * T), r = threadIdx.x % (KP * T);
-  const int pr = g * KP + r % KP, t = r / KP;
-  float2* sm0 = sm2 + pr * C::SLOTS;
-  float2* sm1 = sm2 + (C::NP + pr) * C::SLOTS;
-  const int s = blockIdx.x;
-  const int k = (blockIdx.y * C::NP + pr) * 2;
-  const bool live0 = k < a.Nk, live1 = k + 1 < a.Nk;
-  float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, L);
-  float2 v0[16], v1[16];
-#pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    const int c = t + i * T;
-    float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (live0 && c >= a.in_lo && c <= a.in_hi) q = *reinterpret_cast<const float4*>(sp + sidx(k, c, L));
-    v0[i] = make_float2(q.x, q.y);
-    v1[i] = live1 ? make_float2(q.z, q.w) : make_float2(0.f, 0.f);
-  }
-  reg_fft2<L, -1, kOutRegs>(v0, v1, sm0, sm1, t);
-  const int kf = live0 ? k : 0;
-#pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    const int c = t + i * T;
-    float4 w = __ldg(reinterpret_cast<const float4*>(a.fz + sidx(kf, c, L)));
-    if (a.conj_fz) {
-      w.y = -w.y;
-      w.w = -w.w;
-    }
-    v0[i] = cmul(v0[i], make_float2(w.x, w.y));
-    v1[i] = cmul(v1[i], make_float2(w.z, w.w));
-  }
-  reg_fft2<L, 1>(v0, v1, sm0, sm1, t);
-  if (!live0) return;
-  for (int c = a.out_lo + t; c <= a.out_hi; c += T) {
-    const float2 y0 = sm0[spad(c)];
-    if (live1) {
-      const float2 y1 = sm1[spad(c)];
-      *reinterpret_cast<float4*>(sp + sidx(k, c, L)) = make_float4(y0.x, y0.y, y1.x, y1.y);
-    } else {
-      sp[sidx(k, c, L)] = y0;
-    }
-  }
-}
-
-// element p of the complex signal whose inverse FFT gives two real profiles
-// with half spectra V0, V1 (C2R semantics: imaginary parts at 0 and L/2 ignored)
-__device__ __forceinline__ float2 pair_elem(int p, int L, float2 v0, float2 v1) {
-  const int half = L / 2;
-  if (p == 0 || p == half) return make_float2(v0.x, v1.x);
-  if (p < half) return make_float2(v0.x - v1.y, v0.y + v1.x);
-  return make_float2(v0.x + v1.y, v1.x - v0.y);  // conj(V0) + i conj(V1) at L - p
-}
-
-// forward, per span: two angle rows per signal, theta taps combined in frequency,
-// inverse FFT along rho, rho interpolation into the caller's sinogram
-template <int L>
-__global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(3)) k_fwd_lp2polar_p2(FwdLP2PolarArgs a) {
-  extern __shared__ float2 sm2[];
-  constexpr int T = P2<L>::T;
-  const int sig = threadIdx.x / T, t = threadIdx.x % T;
-  float2* sm = sm2 + sig * P2<L>::SLOTS;
-  const int s = blockIdx.x;
-  const int i0 = 2 * (blockIdx.y * P2<L>::NSIG + sig);
-  const bool live = i0 < a.nrows;
-  const int r0 = live ? a.rows[i0] : 0;
-  const int r1 = (live && i0 + 1 < a.nrows) ? a.rows[i0 + 1] : -1;
-  float w0[4], w1[4];
-  const int c0 = axis_weights_fx(__ldg(a.thc + r0), a.F, a.fsc, a.cubic, w0);
-  int c1 = 0;
-  if (r1 >= 0) {
-    c1 = axis_weights_fx(__ldg(a.thc + r1), a.F, a.fsc, a.cubic, w1);
-  } else {
-    w1[0] = w1[1] = w1[2] = w1[3] = 0.f;
-  }
-  if (!live) w0[0] = w0[1] = w0[2] = w0[3] = 0.f;
-  int t0[4], t1[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    t0[j] = wrapi(c0 + j, a.Nth);
-    t1[j] = wrapi(c1 + j, a.Nth);
-  }
-  const int ntap = a.cubic ? 4 : 2;
-  const float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
-  // both rows' taps as offsets into one run of consecutive columns starting at cu
-  const int cu = min(c0, r1 >= 0 ? c1 : c0);
-  const int nu = max(c0, r1 >= 0 ? c1 : c0) - cu + ntap;
-  const bool run = nu <= 8 && cu >= 0 && cu + nu <= a.Nth;
-  float u0[8], u1[8];
-#pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    const int j0 = cu + q - c0, j1 = cu + q - c1;
-    u0[q] = (j0 >= 0 && j0 < ntap) ? w0[j0] : 0.f;
-    u1[q] = (r1 >= 0 && j1 >= 0 && j1 < ntap) ? w1[j1] : 0.f;
-  }
-  // two consecutive rho frequencies per thread: one 16-byte load per column
-  // (frequencies kk, kk+1 of a column are adjacent in the tiled layout)
-#pragma unroll 1
-  for (int kk = 2 * t; kk <= L / 2; kk += 2 * T) {
-    float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (run) {
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        if (q < nu) {
-          const float4 z = *reinterpret_cast<const float4*>(sp + sidx(kk, cu + q, a.Nth));
-          v0.x += u0[q] * z.x; v0.y += u0[q] * z.y; v0.z += u0[q] * z.z; v0.w += u0[q] * z.w;
-          v1.x += u1[q] * z.x; v1.y += u1[q] * z.y; v1.z += u1[q] * z.z; v1.w += u1[q] * z.w;
-        }
-      }
-    } else {
-      for (int j = 0; j < ntap; ++j) {
-        const float4 q0 = *reinterpret_cast<const float4*>(sp + sidx(kk, t0[j], a.Nth));
-        v0.x += w0[j] * q0.x; v0.y += w0[j] * q0.y; v0.z += w0[j] * q0.z; v0.w += w0[j] * q0.w;
-        if (r1 >= 0) {
-          const float4 q1 = *reinterpret_cast<const float4*>(sp + sidx(kk, t1[j], a.Nth));
-          v1.x += w1[j] * q1.x; v1.y += w1[j] * q1.y; v1.z += w1[j] * q1.z; v1.w += w1[j] * q1.w;
-        }
-      }
-    }
-    const float2 a0 = make_float2(v0.x, v0.y), a1 = make_float2(v1.x, v1.y);
-    sm[spad(kk)] = pair_elem(kk, L, a0, a1);
-    if (kk > 0) sm[spad(L - kk)] = pair_elem(L - kk, L, a0, a1);
-    if (kk + 1 <= L / 2) {  // kk + 1 < L / 2 here since kk is even and L / 2 is even
-      const float2 b0 = make_float2(v0.z, v0.w), b1 = make_float2(v1.z, v1.w);
-      sm[spad(kk + 1)] = pair_elem(kk + 1, L, b0, b1);
-      sm[spad(L - kk - 1)] = pair_elem(L - kk - 1, L, b0, b1);
-    }
-  }
-  __syncthreads();
-  float2 v[16];
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = sm[spad(t + i * T)];
-  __syncthreads();
-  // rho coordinates of both rows' N = 8 T polar points, loaded while the FFT runs
-  int tr0[8], tr1[8];
-#pragma unroll
-  for (int m = 0; m < 8; ++m) {
-    tr0[m] = __ldg(a.rhoc + (size_t)r0 * a.N + t + m * T);
-    tr1[m] = __ldg(a.rhoc + (size_t)max(r1, 0) * a.N + t + m * T);
-  }
-  reg_fft<L, 1>(v, sm, t);
-  if (!live) return;
-  const bool o0 = r0 % a.os == 0, o1 = r1 >= 0 && r1 % a.os == 0;
-  float* out0 = a.Rout + ((size_t)s * a.Nproj0 + r0 / a.os) * a.N0;
-  float* out1 = a.Rout + ((size_t)s * a.Nproj0 + max(r1, 0) / a.os) * a.N0;
-#pragma unroll
-  for (int m = 0; m < 8; ++m) {
-    const int x = t + m * T;
-    const int xo = x - a.cor_off;
-    if (xo < 0 || xo >= a.N0) continue;
-    if (o0) out0[xo] = interp1d_fx([&](int i) { return sm[spad(i)].x; }, L, tr0[m], a.F, a.fsc, a.cubic);
-    if (o1) out1[xo] = interp1d_fx([&](int i) { return sm[spad(i)].y; }, L, tr1[m], a.F, a.fsc, a.cubic);
-  }
-}
-
-// adjoint ingest for N = L/2: one pair of input rows per block of T threads
-template <int L>
-__global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(3)) k_adj_ingest_p2(AdjIngestArgs a) {
-  extern __shared__ float2 sm2[];
-  constexpr int T = P2<L>::T;
-  const int N = L / 2;
-  const bool filt = a.H != nullptr;
-  float2* sm = sm2;
-  const int half = T / 2;
-  const int C = line_chunk(N, half);
-  const int LF = line_floats(N, half);
-  float* lines = reinterpret_cast<float*>(sm2 + (filt ? P2<L>::SLOTS : 0));  // 2 rows, chunked layout
-  float* cp = lines + 2 * LF;
-  const int t = threadIdx.x;
-  const int s = blockIdx.x;
-  const int q0 = 2 * blockIdx.y;
-  const int q1 = q0 + 1 < a.Nproj0 ? q0 + 1 : -1;
-  const float* in0 = a.Rin + ((size_t)s * a.Nproj0 + q0) * a.N0;
-  const float* in1 = a.Rin + ((size_t)s * a.Nproj0 + max(q1, 0)) * a.N0;
-  if (filt) {
-    float2 v[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      const int x = t + i * T;
-      const int xi = min(max(x - a.cor_off, 0), a.N0 - 1);
-      v[i] = x < N ? make_float2(__ldg(in0 + xi), q1 >= 0 ? __ldg(in1 + xi) : 0.f) : make_float2(0.f, 0.f);
-    }
-    // filter spectrum multiply and line stores straight from registers (v[i] = X[t + i*T])
-    reg_fft<L, -1, kOutRegs>(v, sm, t);
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = cscale(v[i], __ldg(a.H + t + i * T));
-    reg_fft<L, 1, kOutRegs>(v, sm, t);
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      const int x = t + i * T;
-      if (x < N) {
-        lines[lpos(x, C)] = v[i].x;
-        lines[LF + lpos(x, C)] = v[i].y;
-      }
-    }
-  } else {
-    for (int x = t; x < N; x += T) {
-      const int xi = min(max(x - a.cor_off, 0), a.N0 - 1);
-      lines[lpos(x, C)] = __ldg(in0 + xi);
-      lines[LF + lpos(x, C)] = q1 >= 0 ? __ldg(in1 + xi) : 0.f;
-    }
-  }
-  __syncthreads();
-  if (a.cubic) {
-    const int which = t >= half;
-    prefilter_line(lines + which * LF, cp + which * LF, N, t - which * half, half);
-  }
-  for (int rr = 0; rr < 2; ++rr) {
-    const int q = rr == 0 ? q0 : q1;
-    if (q < 0) break;
-    for (int j = 0; j < a.os; ++j) {
-      float* dst = a.rbuf + ((size_t)s * a.Nproj + (size_t)q * a.os + j) * N;
-      for (int x = t; x < N; x += T) dst[x] = j == 0 ? lines[rr * LF + lpos(x, C)] : 0.f;
-    }
-  }
-}
-
-// adjoint, per span: polar -> log-polar for a column pair per signal, FFT along rho
-template <int L>
-__global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(4)) k_adj_polar2lp_p2(AdjPolar2LPArgs a) {
-  extern __shared__ float2 sm2[];
-  constexpr int T = P2<L>::T;
-  const int N = L / 2;
-  const int sig = threadIdx.x / T, t = threadIdx.x % T;
-  float2* sm = sm2 + sig * P2<L>::SLOTS;
-  float* prof = reinterpret_cast<float*>(sm2 + P2<L>::NSIG * P2<L>::SLOTS) + sig * 2 * N;
-  const int s = blockIdx.x;
-  const int th0 = a.clo + 2 * (blockIdx.y * P2<L>::NSIG + sig);
-  const bool live = th0 <= a.chi;
-  const int th1 = (live && th0 + 1 <= a.chi) ? th0 + 1 : -1;
-  const float* img = a.rbuf + (size_t)s * a.Nproj * N;
-  const int ta0 = live ? __ldg(a.ta + th0) : LP_FX_NONE;
-  const int ta1 = th1 >= 0 ? __ldg(a.ta + th1) : LP_FX_NONE;
-  float w0[4], w1[4];
-  int rw0[4], rw1[4];
-  const bool has0 = ta0 != LP_FX_NONE, has1 = ta1 != LP_FX_NONE;
-  const int ntap = a.cubic ? 4 : 2;
-  {
-    const int c0 = has0 ? axis_weights_fx(ta0, a.F, a.fsc, a.cubic, w0) : 0;
-    const int c1 = has1 ? axis_weights_fx(ta1, a.F, a.fsc, a.cubic, w1) : 0;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      rw0[j] = wrapi(c0 + j, a.Nproj);
-      rw1[j] = wrapi(c1 + j, a.Nproj);
-    }
-  }
-  // N / T = 8 profile points per thread; the loads of all taps are issued
-  // before any is used (straight-line, no per-point branches)
-  if (!has0) w0[0] = w0[1] = w0[2] = w0[3] = 0.f;
-  if (!has1) w1[0] = w1[1] = w1[2] = w1[3] = 0.f;
-#pragma unroll
-  for (int m = 0; m < N / T; ++m) {
-    const int x = t + m * T;
-    float p0 = 0.f, p1 = 0.f;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (j < ntap) {
-        p0 += w0[j] * (has0 ? __ldg(img + (size_t)rw0[j] * N + x) : 0.f);
-        p1 += w1[j] * (has1 ? __ldg(img + (size_t)rw1[j] * N + x) : 0.f);
-      }
-    }
-    prof[x] = p0;
-    prof[N + x] = p1;
-  }
-  __syncthreads();
-  const int* sx0 = a.sx + (size_t)(live ? th0 : 0) * L;
-  const int* sx1 = a.sx + (size_t)max(th1, 0) * L;
-  int xs0[16], xs1[16];
-#pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    xs0[i] = live ? __ldg(sx0 + t + i * T) : LP_FX_NONE;
-    xs1[i] = th1 >= 0 ? __ldg(sx1 + t + i * T) : LP_FX_NONE;
-  }
-#pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    const bool ok0 = xs0[i] != LP_FX_NONE, ok1 = xs1[i] != LP_FX_NONE;
-    const float v0 = interp1d_fx([&](int q) { return prof[q]; }, N, ok0 ? xs0[i] : 0, a.F, a.fsc, a.cubic);
-    const float v1 = interp1d_fx([&](int q) { return prof[N + q]; }, N, ok1 ? xs1[i] : 0, a.F, a.fsc, a.cubic);
-    sm[spad(t + i * T)] = make_float2(ok0 ? v0 : 0.f, ok1 ? v1 : 0.f);
-  }
-  __syncthreads();
-  // wrap points (distinct rho within a column) add a direct 2-D sample
-  for (int c = 0; c < 2; ++c) {
-    const int th = c == 0 ? th0 : th1;
-    if (!live || th < 0) continue;
-    const int wb = __ldg(a.woff + th), we = __ldg(a.woff + th + 1);
-    for (int w = wb + t; w < we; w += T) {
-      const int4 p = __ldg(a.wpt + w);
-      const int r = p.x;
-      const float val = interp2d_fx(img, N, a.Nproj, p.y, p.z, a.F, a.fsc, a.cubic);
-      if (c == 0) sm[spad(r)].x += val;
-      else sm[spad(r)].y += val;
-    }
-  }
-  __syncthreads();
-  float2 v[16];
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = sm[spad(t + i * T)];
-  __syncthreads();
-  reg_fft<L, -1>(v, sm, t);
-  if (!live) return;
-  float2* out = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
-  // frequencies k, k+1 of a column in one 16-byte store (k + 1 = Nk: tile padding)
-  for (int k = 2 * t; k < a.Nk; k += 2 * T) {
-    const float2 z1 = sm[spad(k)], z2 = sm[spad((L - k) & (L - 1))];
-    const float2 y1 = sm[spad(k + 1)], y2 = sm[spad(L - k - 1)];
-    *reinterpret_cast<float4*>(out + sidx(k, th0, a.Nth)) =
-        make_float4(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y), 0.5f * (y1.x + y2.x), 0.5f * (y1.y - y2.y));
-    if (th1 >= 0)
-      *reinterpret_cast<float4*>(out + sidx(k, th1, a.Nth)) =
-          make_float4(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x), 0.5f * (y1.y + y2.y), 0.5f * (y2.x - y1.x));
-  }
-}
-
-// adjoint, per span: inverse FFT along rho for a column pair per signal
-template <int L>
-__global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(4)) k_adj_lpcols_p2(AdjLPColsArgs a) {
-  extern __shared__ float2 sm2[];
-  constexpr int T = P2<L>::T;
-  const int sig = threadIdx.x / T, t = threadIdx.x % T;
-  float2* sm = sm2 + sig * P2<L>::SLOTS;
-  const int s = blockIdx.x;
-  const int th0 = a.lo2 + 2 * (blockIdx.y * P2<L>::NSIG + sig);
-  const bool live = th0 <= a.hi2;
-  const int th1 = (live && th0 + 1 <= a.hi2) ? th0 + 1 : -1;
-  const float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
-  // frequencies kk, kk+1 of each column in one 16-byte load (kk even)
-#pragma unroll
-  for (int m = 0; m <= L / 4 / T; ++m) {
-    const int kk = 2 * (t + m * T);
-    if (kk > L / 2) break;
-    float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (live) q0 = *reinterpret_cast<const float4*>(sp + sidx(kk, th0, a.Nth));
-    if (th1 >= 0) q1 = *reinterpret_cast<const float4*>(sp + sidx(kk, th1, a.Nth));
-    const float2 a0 = make_float2(q0.x, q0.y), a1 = make_float2(q1.x, q1.y);
-    sm[spad(kk)] = pair_elem(kk, L, a0, a1);
-    if (kk > 0) sm[spad(L - kk)] = pair_elem(L - kk, L, a0, a1);
-    if (kk + 1 <= L / 2) {
-      const float2 b0 = make_float2(q0.z, q0.w), b1 = make_float2(q1.z, q1.w);
-      sm[spad(kk + 1)] = pair_elem(kk + 1, L, b0, b1);
-      sm[spad(L - kk - 1)] = pair_elem(L - kk - 1, L, b0, b1);
-    }
-  }
-  __syncthreads();
-  float2 v[16];
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = sm[spad(t + i * T)];
-  __syncthreads();
-  reg_fft<L, 1>(v, sm, t);
-  if (!live) return;
-  float* g0 = a.G + ((size_t)s * a.W2 + (th0 - a.lo2)) * L;
-  for (int r = t; r < L; r += T) {
-    const float2 z = sm[spad(r)];
-    if (a.surf) {
-      surf2Dwrite(z.x, a.surf[s], r * (int)sizeof(float), th0 - a.lo2);
-      if (th1 >= 0) surf2Dwrite(z.y, a.surf[s], r * (int)sizeof(float), th1 - a.lo2);
-    } else {
-      g0[r] = z.x;
-      if (th1 >= 0) g0[L + r] = z.y;
-    }
-  }
-}
-
-// ---- dispatch ----------------------------------------------------------------
-static bool p2_ok(int L) { return L >= 256 && L <= 8192 && (L & (L - 1)) == 0; }
-
-template <int L>
-static void set_p2_attrs(int optin) {
-  cudaFuncSetAttribute(k_fwd_c2lp_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-  cudaFuncSetAttribute(k_theta_conv_p2<L, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-  cudaFuncSetAttribute(k_theta_conv_p2<L, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-  cudaFuncSetAttribute(k_theta_conv2_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-  cudaFuncSetAttribute(k_fwd_lp2polar_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-  cudaFuncSetAttribute(k_adj_ingest_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-  cudaFuncSetAttribute(k_adj_polar2lp_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-  cudaFuncSetAttribute(k_adj_lpcols_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-}
-
-cudaError_t configure_p2_kernels(int optin) {
-  set_p2_attrs<256>(optin);
-  set_p2_attrs<512>(optin);
-  set_p2_attrs<1024>(optin);
-  set_p2_attrs<2048>(optin);
-  set_p2_attrs<4096>(optin);
-  set_p2_attrs<8192>(optin);
-  return cudaGetLastError();
-}
-
-bool p2_fwd_c2lp(const FwdC2LPArgs& a, int S, cudaStream_t st, cudaError_t* err) {
-  const int L = a.Nrho;
-  if (!p2_ok(L) || a.ival == nullptr) return false;
-  if (a.col_lo < 0 || a.col_hi >= a.Nth) { *err = cudaErrorInvalidValue; return true; }
-  const int npairs = a.col_hi < a.col_lo ? 0 : (a.col_hi >> 1) - (a.col_lo >> 1) + 1;
-  if (npairs == 0) { *err = cudaSuccess; return true; }
-#define CALL(LL)                                                                              \
-  {                                                                                           \
-    const size_t sm = (size_t)P2<LL>::NSIG * P2<LL>::SLOTS * sizeof(float2);                 \
-    if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; }   \
-    dim3 grid(S, (npairs + P2<LL>::NSIG - 1) / P2<LL>::NSIG);                                  \
-    k_fwd_c2lp_p2<LL><<<grid, P2<LL>::BLOCK, sm, st>>>(a);                                    \
-  }
-  switch (L) { case 256: CALL(256) break; case 512: CALL(512) break; case 1024: CALL(1024) break;
-               case 2048: CALL(2048) break; case 4096: CALL(4096) break; case 8192: CALL(8192) break; }
-#undef CALL
-  *err = cudaGetLastError();
-  return true;
-}
-
-bool p2_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st, cudaError_t* err) {
-  const int L = a.Nth;
-  if (!p2_ok(L)) return false;
-#define CALL(LL)                                                                              \
-  {                                                                                           \
-    if (a.block == 512) {                                                                     \
-      using C = TC<LL, 512>;                                                                  \
-      const size_t sm = (size_t)C::NSIG * C::SLOTS * sizeof(float2);                          \
-      if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; } \
-      dim3 grid(S, (a.Nk + C::NSIG - 1) / C::NSIG);                                           \
-      k_theta_conv_p2<LL, 512><<<grid, C::BLOCK, sm, st>>>(a);                                \
-    } else if (LL <= 4096) {                                                                  \
-      using C = TC2<LL>;                                                                      \
-      if (smem_ok(C::SMEM) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; } \
-      dim3 grid(S, (a.Nk + 2 * C::NP - 1) / (2 * C::NP));                                     \
-      k_theta_conv2_p2<LL><<<grid, C::BLOCK, C::SMEM, st>>>(a);                               \
-    } else {                                                                                  \
-      using C = TC<LL, 256>;                                                                  \
-      const size_t sm = (size_t)C::NSIG * C::SLOTS * sizeof(float2);                          \
-      if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; } \
-      dim3 grid(S, (a.Nk + C::NSIG - 1) / C::NSIG);                                           \
-      k_theta_conv_p2<LL, 256><<<grid, C::BLOCK, sm, st>>>(a);                                \
-    }                                                                                         \
-  }
-  switch (L) { case 256: CALL(256) break; case 512: CALL(512) break; case 1024: CALL(1024) break;
-               case 2048: CALL(2048) break; case 4096: CALL(4096) break; case 8192: CALL(8192) break; }
-#undef CALL
-  *err = cudaGetLastError();
-  return true;
-}
-
-bool p2_fwd_lp2polar(const FwdLP2PolarArgs& a, int S, cudaStream_t st, cudaError_t* err) {
-  const int L = a.Nrho;
-  if (!p2_ok(L)) return false;
-  if (a.nrows <= 0) { *err = cudaSuccess; return true; }
-#define CALL(LL)                                                                              \
-  {                                                                                           \
-    const size_t sm = (size_t)P2<LL>::NSIG * P2<LL>::SLOTS * sizeof(float2);                 \
-    if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; }   \
-    const int pairs = (a.nrows + 1) / 2;                                                      \
-    dim3 grid(S, (pairs + P2<LL>::NSIG - 1) / P2<LL>::NSIG);                                   \
-    k_fwd_lp2polar_p2<LL><<<grid, P2<LL>::BLOCK, sm, st>>>(a);                                \
-  }
-  switch (L) { case 256: CALL(256) break; case 512: CALL(512) break; case 1024: CALL(1024) break;
-               case 2048: CALL(2048) break; case 4096: CALL(4096) break; case 8192: CALL(8192) break; }
-#undef CALL
-  *err = cudaGetLastError();
-  return true;
-}
-
-bool p2_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st, cudaError_t* err) {
-  const int L = 2 * a.N;
-  if (!p2_ok(L) || L < 1024) return false;  // needs T = L/16 >= 64 threads per row pair
-#define CALL(LL)                                                                              \
-  {                                                                                           \
-    const size_t sm = (a.H ? (size_t)P2<LL>::SLOTS * sizeof(float2) : 0) + 4 * (size_t)line_floats(LL / 2, P2<LL>::T / 2) * sizeof(float); \
-    if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; }   \
-    dim3 grid(S, (a.Nproj0 + 1) / 2);                                                         \
-    k_adj_ingest_p2<LL><<<grid, P2<LL>::T, sm, st>>>(a);                                      \
-  }
-  switch (L) { case 1024: CALL(1024) break; case 2048: CALL(2048) break; case 4096: CALL(4096) break;
-               case 8192: CALL(8192) break; default: return false; }
-#undef CALL
-  *err = cudaGetLastError();
-  return true;
-}
-
-bool p2_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st, cudaError_t* err) {
-  const int L = a.Nrho;
-  if (!p2_ok(L)) return false;
-  if (a.chi < a.clo) { *err = cudaSuccess; return true; }
-#define CALL(LL)                                                                              \
-  {                                                                                           \
-    const size_t sm = (size_t)P2<LL>::NSIG * (P2<LL>::SLOTS * sizeof(float2) + (size_t)LL * sizeof(float)); \
-    if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; }   \
-    const int pairs = (a.chi - a.clo + 2) / 2;                                                \
-    dim3 grid(S, (pairs + P2<LL>::NSIG - 1) / P2<LL>::NSIG);                                   \
-    k_adj_polar2lp_p2<LL><<<grid, P2<LL>::BLOCK, sm, st>>>(a);                                \
-  }
-  switch (L) { case 256: CALL(256) break; case 512: CALL(512) break; case 1024: CALL(1024) break;
-               case 2048: CALL(2048) break; case 4096: CALL(4096) break; case 8192: CALL(8192) break; }
-#undef CALL
-  *err = cudaGetLastError();
-  return true;
-}
-
-bool p2_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st, cudaError_t* err) {
-  const int L = a.Nrho;
-  if (!p2_ok(L)) return false;
-#define CALL(LL)                                                                              \
-  {                                                                                           \
-    const size_t sm = (size_t)P2<LL>::NSIG * P2<LL>::SLOTS * sizeof(float2);                 \
-    if (smem_ok(sm) != cudaSuccess) { *err = cudaErrorInvalidConfiguration; return true; }   \
-    const int pairs = (a.hi2 - a.lo2 + 2) / 2;                                                \
-    dim3 grid(S, (pairs + P2<LL>::NSIG - 1) / P2<LL>::NSIG);                                   \
-    k_adj_lpcols_p2<LL><<<grid, P2<LL>::BLOCK, sm, st>>>(a);                                  \
-  }
-  switch (L) { case 256: CALL(256) break; case 512: CALL(512) break; case 1024: CALL(1024) break;
-               case 2048: CALL(2048) break; case 4096: CALL(4096) break; case 8192: CALL(8192) break; }
-#undef CALL
-  *err = cudaGetLastError();
-  return true;
-}
 
 }  // namespace lpgb
 
