@@ -124,7 +124,9 @@ int lp_adj(lp_handle* h, float* f, const float* R, int S0, void* stream);
  * with respect to f (used as the autograd backward).  No counterpart in the
  * reference, whose adjoint execAdjManyPtr is a different discretisation
  * (its own kernel fZadj and grids, src/lprec/initsadj.py) and only
- * approximately the transpose.  R is read only.
+ * approximately the transpose.  R is read only.  No atomics: repeated calls give
+ * the same bits.  The first call on a handle builds the gather tables and
+ * allocates their buffers (make it outside stream capture).
  */
 int lp_fwd_transpose(lp_handle* h, float* f, const float* R, int S0, void* stream);
 

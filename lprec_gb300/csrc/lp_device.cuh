@@ -258,4 +258,70 @@ __device__ __forceinline__ float2 pair_elem(int p, int L, float2 v0, float2 v1) 
   return make_float2(v0.x + v1.y, v1.x - v0.y);  // conj(V0) + i conj(V1) at L - p
 }
 
+// Transposed 1-D interpolation along rho of the internal sinogram rows r0 and r1
+// (r1 < 0: none) of slice s, added into acc(q, bin) for row q = 0, 1.  Called by
+// all threads of the block (the same number of barriers on every path); thread
+// tid of nth takes points x = tid, tid + nth, ...  With strictly monotone first
+// taps (a.mono) the points of one tap index and one window of Nrho first taps hit
+// distinct bins, so tap j of those points is added in one pass without
+// conflicts, in a fixed order; otherwise one thread per row adds its points' taps
+// in x order.
+template <class ArgsT, class Acc>
+__device__ __forceinline__ void rho_scatter_T(const ArgsT& a, int s, int r0, int r1, int tid, int nth, Acc acc) {
+  const int ntap = a.cubic ? 4 : 2;
+  const int L = a.Nrho;
+  if (a.mono) {
+    // pass (j, h): tap j of the points whose first tap is below (h = 0) or from (h = 1)
+    // the row's smallest first tap + L, so no two points of a pass meet modulo L
+    for (int j = 0; j < ntap; ++j) {
+      for (int h = 0; h < 2; ++h) {
+        for (int q = 0; q < 2; ++q) {
+          const int r = q == 0 ? r0 : r1;
+          if (r < 0) continue;
+          const float* row = a.Rin + ((size_t)s * a.Nproj0 + r / a.os) * a.N0;
+          const int top = __ldg(a.rbase + r) + L;
+          for (int x = tid; x < a.N; x += nth) {
+            const int xo = x - a.cor_off;
+            if (xo < 0 || xo >= a.N0) continue;
+            float w[4];
+            const int c = axis_weights_fx(__ldg(a.rhoc + (size_t)r * a.N + x), a.F, a.fsc, a.cubic, w);
+            if ((c >= top) != (h == 1)) continue;
+            acc(q, wrapi(c + j, L)) += w[j] * __ldg(row + xo);
+          }
+        }
+        __syncthreads();
+      }
+    }
+  } else {
+    const int r = tid == 0 ? r0 : (tid == 1 ? r1 : -1);
+    if (r >= 0) {
+      const float* row = a.Rin + ((size_t)s * a.Nproj0 + r / a.os) * a.N0;
+      for (int x = 0; x < a.N; ++x) {
+        const int xo = x - a.cor_off;
+        if (xo < 0 || xo >= a.N0) continue;
+        float w[4];
+        const int c = axis_weights_fx(__ldg(a.rhoc + (size_t)r * a.N + x), a.F, a.fsc, a.cubic, w);
+        const float val = __ldg(row + xo);
+        for (int j = 0; j < ntap; ++j) acc(tid, wrapi(c + j, L)) += w[j] * val;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// The two rows' half spectra from the complex FFT Z of (row 0) + i (row 1), each
+// times a_k (1 at k = 0 and L/2, else 2; the imaginary parts of those two bins
+// dropped): the transpose of the forward's C2R of one row.
+__device__ __forceinline__ void split_rows_T(float2 z1, float2 z2, int k, int L, float2* va, float2* vb) {
+  const float ak = (k == 0 || k == L / 2) ? 1.f : 2.f;
+  float2 x = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+  float2 y = make_float2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
+  if (ak == 1.f) {
+    x.y = 0.f;
+    y.y = 0.f;
+  }
+  *va = cscale(x, ak);
+  *vb = cscale(y, ak);
+}
+
 }  // namespace lpgb

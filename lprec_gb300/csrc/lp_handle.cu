@@ -118,6 +118,16 @@ struct FwdDev {
   int nblk[3] = {0, 0, 0};
   int dlo = 0, dhi = -1;
   DevBuf<int2> ival;       // [Nth] rho interval of each column's disk points (same for every span)
+  int rho_mono = 1;        // every row's first rho tap strictly monotone over the row (see FwdTRowsArgs)
+  DevBuf<int> rbase;       // [Nproj] per internal row: its smallest first rho tap
+  // exact transpose, built by its first call: the image cells' lists of log-polar
+  // points of all spans (CSR), the spans' real log-polar values (FwdTColsArgs) and
+  // the row spectra [Nslices][rows of a span][Nk]
+  bool gather_ready = false;
+  DevBuf<int> cell_off;
+  DevBuf<int4> cell_pts;
+  DevBuf<float> lpg;
+  DevBuf<float2> rowspec;
 };
 static const int kTransposeCW = 8;
 
@@ -156,16 +166,18 @@ enum KernelId {
   K_ADJ_POLAR2LP,
   K_ADJ_LPCOLS,
   K_ADJ_LP2CART,
-  K_FWDT_POLAR,
-  K_FWDT_CART,
+  K_FWDT_ROWS,
+  K_FWDT_COLSUM,
+  K_FWDT_COLS,
+  K_FWDT_GATHER,
   K_PREFILTER_T,
   K_CROP,
   K_COUNT
 };
 static const char* kKernelNames[K_COUNT] = {"fwd_ingest",   "col_prefilter", "fwd_c2lp",   "theta_conv",
                                              "fwd_lp2polar", "adj_ingest",    "adj_polar2lp", "adj_lpcols",
-                                             "adj_lp2cart",  "fwdT_polar",    "fwdT_cart",  "prefilter_T",
-                                             "crop"};
+                                             "adj_lp2cart",  "fwdT_rows",     "fwdT_colsum", "fwdT_cols",  "fwdT_gather",
+                                             "prefilter_T", "crop"};
 
 static std::atomic<long long> g_launches(0);
 
@@ -208,6 +220,11 @@ static void free_fwd(FwdDev* f) {
     f->rows[k].free_();
     f->blk[k].free_();
   }
+  f->rbase.free_();
+  f->cell_off.free_();
+  f->cell_pts.free_();
+  f->lpg.free_();
+  f->rowspec.free_();
   f->thc.free_();
   f->rhoc.free_();
   f->fz.free_();
@@ -699,6 +716,34 @@ static int init_fwd_impl(lp_handle* h, const int32_t* pi, int64_t ni, const Real
   }
   F->lo = lo;
   F->hi = hi;
+  // the transposed rho interpolation adds tap j of every point of a row in two passes
+  // (first taps below and from rbase + Nrho): that needs the rows' first taps strictly
+  // monotone in x (the log-polar rho of a polar point is the log of an affine function
+  // of s, and it steps by more than one texel per detector sample) spanning fewer than
+  // 2 Nrho bins -- a row's points at the low end of the rho range wrap onto its high end
+  std::vector<int> rbase(Nproj, 0);
+  {
+    const int coff = N / 2 - h->cor;
+    for (int k = 0; k < 3 && F->rho_mono; ++k)
+      for (int row : rows[k]) {
+        int prev = 0, dir = 0, cmin = INT32_MAX, cmax = INT32_MIN, npt = 0;
+        for (int x = std::max(0, coff); x < std::min(N, coff + h->N0); ++x) {
+          const int c = first_tap(rhoc[(size_t)row * N + x], FB, h->cubic);
+          if (npt > 0) {
+            const int d = c > prev ? 1 : (c < prev ? -1 : 0);
+            if (d == 0 || (dir != 0 && d != dir)) F->rho_mono = 0;
+            dir = d;
+          }
+          prev = c;
+          cmin = std::min(cmin, c);
+          cmax = std::max(cmax, c);
+          ++npt;
+        }
+        if (npt > 0 && cmax - cmin >= 2 * Nrho) F->rho_mono = 0;
+        rbase[row] = npt > 0 ? cmin : 0;
+        if (!F->rho_mono) break;
+      }
+  }
   // column blocks for the transpose
   std::vector<int2> blk[3];
   {
@@ -732,6 +777,7 @@ static int init_fwd_impl(lp_handle* h, const int32_t* pi, int64_t ni, const Real
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
       F->nrows[k] = (int)rows[k].size();
       e = dev_upload(F->rows[k], rows[k]);
+      if (e == cudaSuccess && k == 0) e = dev_upload(F->rbase, rbase);
       if (e == cudaSuccess) e = dev_upload(F->blk[k], blk[k]);
       F->nblk[k] = (int)blk[k].size();
     }
@@ -969,6 +1015,9 @@ int lp_debug_fill_scratch(lp_handle* h, float value, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = fill_async((float*)h->spec.p, h->spec.n * 2, value, st);
   if (e == cudaSuccess && h->fwd) e = fill_async(h->fwd->fbuf.p, h->fwd->fbuf.n, value, st);
+  if (e == cudaSuccess && h->fwd && h->fwd->lpg.p) e = fill_async(h->fwd->lpg.p, h->fwd->lpg.n, value, st);
+  if (e == cudaSuccess && h->fwd && h->fwd->rowspec.p)
+    e = fill_async((float*)h->fwd->rowspec.p, 2 * h->fwd->rowspec.n, value, st);
   if (e == cudaSuccess && h->adj) {
     e = fill_async(h->adj->rbuf.p, h->adj->rbuf.n, value, st);
     if (e == cudaSuccess && h->adj->rin.p) e = fill_async(h->adj->rin.p, h->adj->rin.n, value, st);
@@ -1125,6 +1174,53 @@ int lp_fwd(lp_handle* h, float* R, const float* f, int S0, void* stream) {
                     [&](int s0, int n, cudaStream_t st) { return fwd_slices(h, R, f, s0, n, st, n == S0); });
 }
 
+// Tables of the exact transpose's gather (built on its first call, from the
+// forward's device tables): the log-polar points of all spans with coordinates,
+// grouped by image cell (the integer part of the coordinates, wrapped onto the
+// grid) in (span, theta, rho) order; the buffers of real log-polar values and of
+// row spectra.  Allocates device memory, so make the first call outside stream
+// capture.
+static int build_transpose_tables(lp_handle* h) {
+  FwdDev* F = h->fwd;
+  const int N = h->N, Nth = h->Nth, Nrho = h->Nrho;
+  const int W = F->dhi - F->dlo + 1;
+  if (W > 0) {
+    std::vector<int2> c2[3];
+    for (int k = 0; k < 3; ++k) {
+      c2[k].resize((size_t)Nth * Nrho);
+      CUDA_TRY(cudaMemcpy(c2[k].data(), F->c2lp[k].p, c2[k].size() * sizeof(int2), cudaMemcpyDeviceToHost));
+    }
+    std::vector<int> off((size_t)N * N + 1, 0);
+    auto cell = [&](int2 p) {
+      const int ix = p.x >> F->F, iy = p.y >> F->F;
+      return (size_t)(((iy % N) + N) % N) * N + (((ix % N) + N) % N);
+    };
+    for (int k = 0; k < 3; ++k)
+      for (int t = F->dlo; t <= F->dhi; ++t)
+        for (int r = 0; r < Nrho; ++r) {
+          const int2 p = c2[k][(size_t)t * Nrho + r];
+          if (p.x != LP_FX_NONE) off[cell(p) + 1]++;
+        }
+    for (size_t c = 0; c < (size_t)N * N; ++c) off[c + 1] += off[c];
+    std::vector<int4> pts(std::max(off[(size_t)N * N], 1), make_int4(0, 0, 0, 0));
+    std::vector<int> fill(off.begin(), off.end() - 1);
+    for (int k = 0; k < 3; ++k)
+      for (int t = F->dlo; t <= F->dhi; ++t)
+        for (int r = 0; r < Nrho; ++r) {
+          const int2 p = c2[k][(size_t)t * Nrho + r];
+          if (p.x != LP_FX_NONE) pts[fill[cell(p)]++] = make_int4(p.x, p.y, (t - F->dlo) * Nrho + r, k);
+        }
+    CUDA_TRY(dev_upload(F->cell_off, off));
+    CUDA_TRY(dev_upload(F->cell_pts, pts));
+    const size_t groups = (h->Nslices + kGatherSlices - 1) / kGatherSlices;
+    CUDA_TRY(dev_alloc(F->lpg, 3 * groups * kGatherSlices * W * Nrho));
+  }
+  const int nr = std::max(F->nrows[0], std::max(F->nrows[1], F->nrows[2]));
+  CUDA_TRY(dev_alloc(F->rowspec, (size_t)h->Nslices * std::max(nr, 1) * h->Nk));
+  F->gather_ready = true;
+  return LP_OK;
+}
+
 int lp_fwd_transpose(lp_handle* h, float* f, const float* R, int S0, void* stream) {
   if (!h) return set_err(LP_ERR_ARG, "lp_fwd_transpose: null handle");
   if (!h->fwd) return set_err(LP_ERR_STATE, "lp_fwd_transpose: forward tables not initialised (lp_init_fwd)");
@@ -1135,21 +1231,33 @@ int lp_fwd_transpose(lp_handle* h, float* f, const float* R, int S0, void* strea
   DeviceGuard g(h->device);
   cudaStream_t st = (cudaStream_t)stream;
   FwdDev* F = h->fwd;
+  if (!F->gather_ready) {
+    int rc = build_transpose_tables(h);
+    if (rc != LP_OK) return rc;
+  }
   float* acc = F->fbuf.p;
-  CUDA_TRY(cudaMemsetAsync(acc, 0, (size_t)S0 * h->N * h->N * sizeof(float), st));
-  for (int k = 0; k < 3; ++k) {
-    CUDA_TRY(cudaMemsetAsync(h->spec.p, 0, (size_t)S0 * spec_slice(h->Nk, h->Nth) * sizeof(float2), st));
-    FwdTPolarArgs a1{R, h->spec.p, F->thc.p, F->rhoc.p, F->rows[k].p, F->blk[k].p, h->N, h->N0, h->Nth, h->Nrho,
-                     h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, F->lo, kTransposeCW, h->plan_rho,
-                     F->F, F->fsc};
-    CUDA_TRY(launch(h, K_FWDT_POLAR, st, [&] { return launch_fwdT_polar(a1, S0, F->nblk[k], st); }));
+  const int W = F->dhi - F->dlo + 1;
+  if (W <= 0) CUDA_TRY(cudaMemsetAsync(acc, 0, (size_t)S0 * h->N * h->N * sizeof(float), st));
+  const size_t span_stride =
+      (size_t)(h->Nslices + kGatherSlices - 1) / kGatherSlices * kGatherSlices * (W > 0 ? W : 1) * h->Nrho;
+  for (int k = 0; k < 3 && W > 0; ++k) {
+    FwdTRowsArgs a0{R, F->rowspec.p, F->rhoc.p, F->rows[k].p, F->rbase.p, F->nrows[k], h->N, h->N0, h->Nrho,
+                    h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho, F->F, F->fsc, F->rho_mono};
+    CUDA_TRY(launch(h, K_FWDT_ROWS, st, [&] { return launch_fwdT_rows(a0, S0, st); }));
+    FwdTColSumArgs a1{F->rowspec.p, h->spec.p, F->thc.p, F->rows[k].p, F->blk[k].p, F->nrows[k], h->Nth, h->Nk,
+                      F->lo, F->hi, kTransposeCW, h->cubic, F->F, F->fsc};
+    CUDA_TRY(launch(h, K_FWDT_COLSUM, st, [&] { return launch_fwdT_colsum(a1, S0, F->nblk[k], st); }));
     ThetaConvArgs a2{h->spec.p, F->fz.p, h->Nth, h->Nk, F->lo, F->hi,
                      F->dlo, F->dhi, 1, h->plan_th, h->fwd_tblock};
-    if (F->dhi >= F->dlo)
-      CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
-    FwdTCartArgs a3{h->spec.p, acc, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, F->dlo, F->dhi,
-                    h->cubic, h->plan_rho, F->F, F->fsc};
-    CUDA_TRY(launch(h, K_FWDT_CART, st, [&] { return launch_fwdT_cart(a3, S0, st); }));
+    CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
+    FwdTColsArgs a3{h->spec.p, F->lpg.p + k * span_stride, h->erho.p, h->Nth, h->Nrho, h->Nk, F->dlo, F->dhi,
+                    h->plan_rho};
+    CUDA_TRY(launch(h, K_FWDT_COLS, st, [&] { return launch_fwdT_cols(a3, S0, st); }));
+  }
+  if (W > 0) {
+    FwdTGatherArgs a4{F->lpg.p, span_stride, acc, F->cell_off.p, F->cell_pts.p, h->N, W, h->Nrho, h->cubic,
+                      F->F, F->fsc};
+    CUDA_TRY(launch(h, K_FWDT_GATHER, st, [&] { return launch_fwdT_gather(a4, S0, st); }));
   }
   if (h->cubic) {
     // transposed column prefilter acc -> the spectrum buffer (free now; it holds S0 N x N

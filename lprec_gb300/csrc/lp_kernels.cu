@@ -807,103 +807,78 @@ namespace lpgb {
 // ===========================================================================
 namespace lpgb {
 
-__global__ void __launch_bounds__(256) k_fwdT_polar(FwdTPolarArgs a) {
+// Rows: per pair of internal rows of a span, the transposed rho interpolation, one
+// complex FFT along rho and the split into the two rows' half spectra (the
+// transpose of the forward's C2R), written to the row-spectrum buffer.  The
+// power-of-two and mixed lengths run k_fwdT_rows_p2 on the register FFT.
+__global__ void __launch_bounds__(256) k_fwdT_rows(FwdTRowsArgs a) {
   extern __shared__ float smf[];
   CBuf A, B;
   float* u = carve(smf, a.Nrho, 1, A, B);  // 2 x Nrho transposed-interpolation accumulators
   const int s = blockIdx.x;
-  const int b = blockIdx.y;
-  const int c0 = a.lo + b * a.CW;
-  const int2 rr = __ldg(a.blk + b);
-  const int ntap = a.cubic ? 4 : 2;
-  float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
+  const int i0 = 2 * blockIdx.y;
+  const int r0 = a.rows[i0];
+  const int r1 = i0 + 1 < a.nrows ? a.rows[i0 + 1] : -1;
   const int L = a.Nrho;
-  for (int i0 = rr.x; i0 < rr.y; i0 += 2) {
-    const int r0 = a.rows[i0];
-    const int r1 = (i0 + 1 < rr.y) ? a.rows[i0 + 1] : -1;
-    for (int i = threadIdx.x; i < 2 * L; i += blockDim.x) u[i] = 0.f;
-    __syncthreads();
-    // transposed 1-D interpolation along rho of the two rows
-    for (int q = 0; q < 2; ++q) {
-      const int r = q == 0 ? r0 : r1;
-      if (r < 0) continue;
-      const float* row = a.Rin + ((size_t)s * a.Nproj0 + r / a.os) * a.N0;
-      for (int x = threadIdx.x; x < a.N; x += blockDim.x) {
-        const int xo = x - a.cor_off;
-        if (xo < 0 || xo >= a.N0) continue;
-        const float val = __ldg(row + xo);
-        float w[4];
-        const int c = axis_weights_fx(__ldg(a.rhoc + (size_t)r * a.N + x), a.F, a.fsc, a.cubic, w);
-        for (int j = 0; j < ntap; ++j) atomicAdd(u + q * L + wrapi(c + j, L), w[j] * val);
-      }
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < L; i += blockDim.x) A.set(i, make_float2(u[i], u[L + i]));
-    __syncthreads();
-    const CBuf Z = fft_block<-1>(A, B, a.plan, 1, 0);
-    float w0[4], w1[4];
-    const int t0 = axis_weights_fx(__ldg(a.thc + r0), a.F, a.fsc, a.cubic, w0);
-    int t1 = 0;
-    if (r1 >= 0) t1 = axis_weights_fx(__ldg(a.thc + r1), a.F, a.fsc, a.cubic, w1);
-    for (int k = threadIdx.x; k < a.Nk; k += blockDim.x) {
-      const float2 z1 = Z.get(k);
-      const float2 z2 = Z.get(k == 0 ? 0 : L - k);
-      const float ak = (k == 0 || k == L / 2) ? 1.f : 2.f;
-      float2 va = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
-      float2 vb = make_float2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
-      if (ak == 1.f) {
-        va.y = 0.f;
-        vb.y = 0.f;
-      }
-      va = cscale(va, ak);
-      vb = cscale(vb, ak);
-      for (int j = 0; j < ntap; ++j) {
-        const int ca = wrapi(t0 + j, a.Nth);
-        if (ca >= c0 && ca < c0 + a.CW) {
-          float2& o = sp[sidx(k, ca, a.Nth)];
-          o.x += w0[j] * va.x;
-          o.y += w0[j] * va.y;
-        }
-        if (r1 >= 0) {
-          const int cb = wrapi(t1 + j, a.Nth);
-          if (cb >= c0 && cb < c0 + a.CW) {
-            float2& o = sp[sidx(k, cb, a.Nth)];
-            o.x += w1[j] * vb.x;
-            o.y += w1[j] * vb.y;
+  for (int i = threadIdx.x; i < 2 * L; i += blockDim.x) u[i] = 0.f;
+  __syncthreads();
+  rho_scatter_T(a, s, r0, r1, threadIdx.x, blockDim.x, [&](int q, int bin) -> float& { return u[q * L + bin]; });
+  for (int i = threadIdx.x; i < L; i += blockDim.x) A.set(i, make_float2(u[i], u[L + i]));
+  __syncthreads();
+  const CBuf Z = fft_block<-1>(A, B, a.plan, 1, 0);
+  float2* o0 = a.rowspec + ((size_t)s * a.nrows + i0) * a.Nk;
+  for (int k = threadIdx.x; k < a.Nk; k += blockDim.x) {
+    float2 va, vb;
+    split_rows_T(Z.get(k), Z.get(k == 0 ? 0 : L - k), k, L, &va, &vb);
+    o0[k] = va;
+    if (r1 >= 0) o0[a.Nk + k] = vb;
+  }
+}
+
+// Columns: per block of CW spectrum columns from lo, every rho frequency sums the
+// half spectra of the rows whose theta taps reach the column, times the tap
+// weight, in row order (no atomics: the same bits on every run).  Writes every
+// column of [lo, hi], zero where no row reaches it.
+constexpr int kColSumCW = 8;
+
+__global__ void __launch_bounds__(256) k_fwdT_colsum(FwdTColSumArgs a) {
+  const int s = blockIdx.x;
+  const int c0 = a.lo + blockIdx.y * kColSumCW;
+  const int2 rr = __ldg(a.blk + blockIdx.y);
+  const int ntap = a.cubic ? 4 : 2;
+  const float2* rs = a.rowspec + (size_t)s * a.nrows * a.Nk;
+  float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
+  for (int k = threadIdx.x; k < a.Nk; k += blockDim.x) {
+    float2 acc[kColSumCW];
+#pragma unroll
+    for (int c = 0; c < kColSumCW; ++c) acc[c] = make_float2(0.f, 0.f);
+    for (int i = rr.x; i < rr.y; ++i) {
+      float w[4];
+      const int t0 = axis_weights_fx(__ldg(a.thc + __ldg(a.rows + i)), a.F, a.fsc, a.cubic, w);
+      const float2 z = __ldg(rs + (size_t)i * a.Nk + k);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (j >= ntap) break;
+        const int c = wrapi(t0 + j, a.Nth) - c0;
+#pragma unroll
+        for (int cc = 0; cc < kColSumCW; ++cc)
+          if (c == cc) {
+            acc[cc].x += w[j] * z.x;
+            acc[cc].y += w[j] * z.y;
           }
-        }
       }
     }
-    __syncthreads();
+#pragma unroll
+    for (int cc = 0; cc < kColSumCW; ++cc)
+      if (c0 + cc <= a.hi) sp[sidx(k, c0 + cc, a.Nth)] = acc[cc];
   }
 }
 
-// transposed 2-D interpolation: scatter val with the weights of the sample at fixed-point (x, y)
-__device__ __forceinline__ void scatter2d_fx(float* img, int W, int H, int vx, int vy, int F, float fsc, float val,
-                                             int cubic) {
-  const int ix = fx_int(vx, F), iy = fx_int(vy, F);
-  const float ax = fx_frac(vx, F, fsc), ay = fx_frac(vy, F, fsc);
-  float wx[4], wy[4];
-  int nt;
-  if (cubic) {
-    bspline_w(ax, wx);
-    bspline_w(ay, wy);
-    nt = 4;
-  } else {
-    wx[0] = 1.f - ax;
-    wx[1] = ax;
-    wy[0] = 1.f - ay;
-    wy[1] = ay;
-    nt = 2;
-  }
-  const int ox = cubic ? 1 : 0;
-  for (int j = 0; j < nt; ++j) {
-    float* row = img + (size_t)wrapi(iy - ox + j, H) * W;
-    for (int i = 0; i < nt; ++i) atomicAdd(row + wrapi(ix - ox + i, W), wy[j] * wx[i] * val);
-  }
-}
-
-__global__ void __launch_bounds__(256) k_fwdT_cart(FwdTCartArgs a) {
+// Transpose of the column stage of the forward: per pair of disk columns, the
+// transposes of R2C (C2R of b_k * Y, b_k = 1/2 except at k = 0 and Nrho/2) and of
+// the e^rho multiply, written slice-interleaved as real log-polar values for the
+// gather below.
+__global__ void __launch_bounds__(256) k_fwdT_cols(FwdTColsArgs a) {
   extern __shared__ float smf[];
   CBuf A, B;
   carve(smf, a.Nrho, 1, A, B);
@@ -920,19 +895,69 @@ __global__ void __launch_bounds__(256) k_fwdT_cart(FwdTCartArgs a) {
   }
   __syncthreads();
   const CBuf z = fft_block<1>(A, B, a.plan, 1, 0);
-  float* img = a.acc + (size_t)s * a.N * a.N;
-  for (int q = 0; q < 2; ++q) {
-    const int th = q == 0 ? th0 : th1;
-    if (th < 0) break;
-    const int2* cc = a.c2lp + (size_t)th * L;
-    for (int r = threadIdx.x; r < L; r += blockDim.x) {
-      const int2 p = __ldg(cc + r);
-      if (p.x == LP_FX_NONE) continue;
-      const float2 zv = z.get(r);
-      const float val = __ldg(a.erho + r) * (q == 0 ? zv.x : zv.y);
-      scatter2d_fx(img, a.N, a.N, p.x, p.y, a.F, a.fsc, val, a.cubic);
+  const int W = a.dhi - a.dlo + 1;
+  float* g0 = a.G + (((size_t)(s / kGatherSlices) * W + (th0 - a.dlo)) * L) * kGatherSlices + s % kGatherSlices;
+  for (int r = threadIdx.x; r < L; r += blockDim.x) {
+    const float2 zv = z.get(r);
+    const float e = __ldg(a.erho + r);
+    g0[(size_t)r * kGatherSlices] = e * zv.x;
+    if (th1 >= 0) g0[(size_t)(L + r) * kGatherSlices] = e * zv.y;
+  }
+}
+
+// Transposed Cartesian interpolation as a gather: output pixel (X, Y) of the padded
+// grid sums, over the cells of the points whose taps reach it (cell = the integer
+// part of a point's coordinates), each point's value times its tap weight, in cell
+// and list order.  No atomics: the result is the same bits on every run.  A point
+// with integer part (ix, iy) reaches columns ix - o .. ix - o + n - 1 (o = 1, n = 4
+// cubic; o = 0, n = 2 linear), so pixel X reads cells ix = X + o - i for tap i.
+// A thread computes one pixel for the kGatherSlices slices of a group.
+__global__ void __launch_bounds__(256) k_fwdT_gather(FwdTGatherArgs a, int S) {
+  const int X = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int Y = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (X >= a.N || Y >= a.N) return;
+  const int s0 = blockIdx.z * kGatherSlices;
+  const int ns = min(kGatherSlices, S - s0);
+  const size_t plane = (size_t)a.N * a.N;
+  float acc[kGatherSlices];
+#pragma unroll
+  for (int q = 0; q < kGatherSlices; ++q) acc[q] = 0.f;
+  const int o = a.cubic ? 1 : 0;
+  const int n = a.cubic ? 4 : 2;
+  // this slice group's values: [W][Nrho][kGatherSlices] per span
+  const float* G = a.G + (size_t)blockIdx.z * a.W * a.Nrho * kGatherSlices;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    if (j >= n) break;
+    const int cy = wrapi(Y + o - j, a.N);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (i >= n) break;
+      const int c = cy * a.N + wrapi(X + o - i, a.N);
+      const int e1 = __ldg(a.cell_off + c + 1);
+      for (int e = __ldg(a.cell_off + c); e < e1; ++e) {
+        const int4 p = __ldg(a.pts + e);
+        float wx[4], wy[4];
+        axis_weights_fx(p.x, a.F, a.fsc, a.cubic, wx);
+        axis_weights_fx(p.y, a.F, a.fsc, a.cubic, wy);
+        const float w = wy[j] * wx[i];
+        const float4* g = reinterpret_cast<const float4*>(G + p.w * a.span_stride + (size_t)p.z * kGatherSlices);
+        const float4 u = __ldg(g), v = __ldg(g + 1);
+        acc[0] += w * u.x;
+        acc[1] += w * u.y;
+        acc[2] += w * u.z;
+        acc[3] += w * u.w;
+        acc[4] += w * v.x;
+        acc[5] += w * v.y;
+        acc[6] += w * v.z;
+        acc[7] += w * v.w;
+      }
     }
   }
+  float* out = a.acc + (size_t)s0 * plane + (size_t)Y * a.N + X;
+#pragma unroll
+  for (int q = 0; q < kGatherSlices; ++q)
+    if (q < ns) out[q * plane] = acc[q];
 }
 
 // ---------------------------------------------------------------------------
@@ -1045,23 +1070,41 @@ __global__ void k_crop(CropArgs a) {
   a.dst[(size_t)s * a.N0 * a.N0 + i] = a.src[((size_t)s * a.N + y + a.off) * a.N + x + a.off];
 }
 
-cudaError_t launch_fwdT_polar(const FwdTPolarArgs& a, int S, int nblk, cudaStream_t st) {
-  if (nblk <= 0) return cudaSuccess;
+cudaError_t launch_fwdT_rows(const FwdTRowsArgs& a, int S, cudaStream_t st) {
+  if (a.nrows <= 0) return cudaSuccess;
+  cudaError_t pe;
+  if (g_use_p2 && (p2_fwdT_rows(a, S, st, &pe) || mr_fwdT_rows(a, S, st, &pe))) return pe;
   const size_t sm = fft_bytes(a.Nrho, 1) + 2 * (size_t)a.Nrho * sizeof(float);
   if (smem_ok(sm) != cudaSuccess) return cudaErrorInvalidConfiguration;
-  cudaFuncSetAttribute(k_fwdT_polar, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
-  dim3 grid(S, nblk);
-  k_fwdT_polar<<<grid, 256, sm, st>>>(a);
+  cudaFuncSetAttribute(k_fwdT_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+  dim3 grid(S, (a.nrows + 1) / 2);
+  k_fwdT_rows<<<grid, 256, sm, st>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t launch_fwdT_cart(const FwdTCartArgs& a, int S, cudaStream_t st) {
+cudaError_t launch_fwdT_colsum(const FwdTColSumArgs& a, int S, int nblk, cudaStream_t st) {
+  if (nblk <= 0) return cudaSuccess;
+  if (a.CW != kColSumCW) return cudaErrorInvalidValue;
+  dim3 grid(S, nblk);
+  k_fwdT_colsum<<<grid, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st) {
   if (a.dhi < a.dlo) return cudaSuccess;
+  cudaError_t pe;
+  if (g_use_p2 && (p2_fwdT_cols(a, S, st, &pe) || mr_fwdT_cols(a, S, st, &pe))) return pe;
   const size_t sm = fft_bytes(a.Nrho, 1);
   if (smem_ok(sm) != cudaSuccess) return cudaErrorInvalidConfiguration;
-  cudaFuncSetAttribute(k_fwdT_cart, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+  cudaFuncSetAttribute(k_fwdT_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
   dim3 grid(S, (a.dhi - a.dlo + 2) / 2);
-  k_fwdT_cart<<<grid, 256, sm, st>>>(a);
+  k_fwdT_cols<<<grid, 256, sm, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fwdT_gather(const FwdTGatherArgs& a, int S, cudaStream_t st) {
+  dim3 grid((a.N + 31) / 32, (a.N + 7) / 8, (S + kGatherSlices - 1) / kGatherSlices);
+  k_fwdT_gather<<<grid, 256, 0, st>>>(a, S);
   return cudaGetLastError();
 }
 

@@ -146,26 +146,54 @@ void set_use_p2(bool on);
 
 namespace lpgb {
 // ---- exact transpose of the forward (autograd backward) --------------------
-struct FwdTPolarArgs {        // sinogram rows -> log-polar spectrum columns (transposed lp2polar)
+struct FwdTRowsArgs {         // sinogram rows -> their log-polar rho half spectra (transposed lp2polar, part 1)
   const float* Rin;           // [S][Nproj0][N0] caller's gradient
-  float2* spec;               // [S][Nk][Nth], zeroed; block owns columns [c0, c0+CW)
-  const int* thc;             // [Nproj] theta coordinate per internal row (fixed point)
+  float2* rowspec;            // [S][nrows][Nk] per row of the span: a_k x R2C of the transposed rho interpolation
   const int* rhoc;            // [Nproj][N] rho coordinate per polar point (fixed point)
   const int* rows;            // rows of the span (multiples of os), sorted
-  const int2* blk;            // per column block: [first, last) into rows
-  int N, N0, Nth, Nrho, Nk, Nproj0, os, cor_off, cubic, lo, CW;
+  const int* rbase;           // [Nproj] smallest first rho tap of each row
+  int nrows;
+  int N, N0, Nrho, Nk, Nproj0, os, cor_off, cubic;
   FFTPlan plan;               // length Nrho
+  int F;
+  float fsc;
+  int mono;                   // every row's first rho tap strictly monotone in x, spanning fewer than
+                              // 2 Nrho bins: the transposed interpolation runs as two passes per tap
+                              // (taps below and from rbase + Nrho) without conflicts; else one thread
+                              // per row adds in order
+};
+
+struct FwdTColSumArgs {       // row spectra -> spectrum columns (transposed theta taps, part 2)
+  const float2* rowspec;      // [S][nrows][Nk]
+  float2* spec;               // [S] spectra, tiled layout; columns [lo, hi] written
+  const int* thc;             // [Nproj] theta coordinate per internal row (fixed point)
+  const int* rows;            // rows of the span, sorted
+  const int2* blk;            // per column block of CW columns from lo: [first, last) into rows
+  int nrows, Nth, Nk, lo, hi, CW, cubic;
   int F;
   float fsc;
 };
 
-struct FwdTCartArgs {         // spectrum columns -> real log-polar columns -> scatter to the image
+// the exact transpose's real log-polar values are stored slice-interleaved in groups
+// of kGatherSlices slices, [S / kGatherSlices][W][Nrho][kGatherSlices], so the gather
+// reads a point's values for all slices of a group in two 16-byte loads
+constexpr int kGatherSlices = 8;
+
+struct FwdTColsArgs {         // spectrum columns -> real log-polar columns x e^rho
   const float2* spec;         // [S][Nk][Nth]
-  float* acc;                 // [S][N][N] accumulator (atomic adds)
-  const int2* c2lp;           // [Nth][Nrho] this span (fixed point)
+  float* G;                   // [S / kGatherSlices][dhi - dlo + 1][Nrho][kGatherSlices]
   const float* erho;          // [Nrho]
-  int N, Nth, Nrho, Nk, dlo, dhi, cubic;
+  int Nth, Nrho, Nk, dlo, dhi;
   FFTPlan plan;
+};
+
+struct FwdTGatherArgs {       // transposed Cartesian interpolation as a per-pixel gather, all spans
+  const float* G;             // [3][groups][W][Nrho][kGatherSlices] the spans' values (FwdTColsArgs)
+  size_t span_stride;         // floats from one span's values to the next
+  float* acc;                 // [S][N][N], written
+  const int* cell_off;        // [N*N + 1] CSR over image cells (floor of the point's coordinates)
+  const int4* pts;            // per cell: (x, y fixed point, (theta - dlo) * Nrho + rho, span), in (span, theta, rho) order
+  int N, W, Nrho, cubic;
   int F;
   float fsc;
 };
@@ -188,8 +216,10 @@ struct CropArgs {
   int N, N0, off;
 };
 
-cudaError_t launch_fwdT_polar(const FwdTPolarArgs& a, int S, int nblk, cudaStream_t st);
-cudaError_t launch_fwdT_cart(const FwdTCartArgs& a, int S, cudaStream_t st);
+cudaError_t launch_fwdT_rows(const FwdTRowsArgs& a, int S, cudaStream_t st);
+cudaError_t launch_fwdT_colsum(const FwdTColSumArgs& a, int S, int nblk, cudaStream_t st);
+cudaError_t launch_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st);
+cudaError_t launch_fwdT_gather(const FwdTGatherArgs& a, int S, cudaStream_t st);
 cudaError_t launch_prefilter_T_cols(const PrefilterTColsArgs& a, int S, cudaStream_t st);
 cudaError_t launch_prefilter_T_rows_crop(const PrefilterTRowsCropArgs& a, int S, cudaStream_t st);
 cudaError_t launch_crop(const CropArgs& a, int S, cudaStream_t st);

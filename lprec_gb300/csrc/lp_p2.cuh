@@ -540,6 +540,87 @@ __global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(4)) k_adj_lpcols_p
 }
 
 
+// exact transpose, row stage (k_fwdT_rows) on the register FFT: per signal one
+// pair of internal rows of the span; N = L/2 = 8T detector points per row
+template <int L>
+__global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(4)) k_fwdT_rows_p2(FwdTRowsArgs a) {
+  extern __shared__ float2 sm2[];
+  constexpr int T = P2<L>::T;
+  const int sig = threadIdx.x / T, t = threadIdx.x % T;
+  float2* sm = sm2 + sig * P2<L>::SLOTS;
+  float* smf = reinterpret_cast<float*>(sm);
+  const int s = blockIdx.x;
+  const int i0 = 2 * (blockIdx.y * P2<L>::NSIG + sig);
+  const bool live = i0 < a.nrows;
+  const int r0 = live ? a.rows[i0] : -1;
+  const int r1 = (live && i0 + 1 < a.nrows) ? a.rows[i0 + 1] : -1;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) sm[spad(t + i * T)] = make_float2(0.f, 0.f);
+  __syncthreads();
+  // row 0 accumulates in the real parts, row 1 in the imaginary parts
+  rho_scatter_T(a, s, r0, r1, t, T, [&](int q, int bin) -> float& { return smf[2 * spad(bin) + q]; });
+  float2 v[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = sm[spad(t + i * T)];
+  __syncthreads();
+  any_fft<L, -1>(v, sm, t);
+  if (!live) return;
+  float2* o0 = a.rowspec + ((size_t)s * a.nrows + i0) * a.Nk;
+  for (int k = t; k < a.Nk; k += T) {
+    float2 va, vb;
+    split_rows_T(sm[spad(k)], sm[spad(k == 0 ? 0 : L - k)], k, L, &va, &vb);
+    o0[k] = va;
+    if (r1 >= 0) o0[a.Nk + k] = vb;
+  }
+}
+
+// exact transpose, column stage (k_fwdT_cols) on the register FFT
+template <int L>
+__global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(4)) k_fwdT_cols_p2(FwdTColsArgs a) {
+  extern __shared__ float2 sm2[];
+  constexpr int T = P2<L>::T;
+  const int sig = threadIdx.x / T, t = threadIdx.x % T;
+  float2* sm = sm2 + sig * P2<L>::SLOTS;
+  const int s = blockIdx.x;
+  const int th0 = a.dlo + 2 * (blockIdx.y * P2<L>::NSIG + sig);
+  const bool live = th0 <= a.dhi;
+  const int th1 = (live && th0 + 1 <= a.dhi) ? th0 + 1 : -1;
+  const float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
+#pragma unroll
+  for (int m = 0; m <= L / 4 / T; ++m) {
+    const int kk = 2 * (t + m * T);
+    if (kk > L / 2) break;
+    float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (live) q0 = *reinterpret_cast<const float4*>(sp + sidx(kk, th0, a.Nth));
+    if (th1 >= 0) q1 = *reinterpret_cast<const float4*>(sp + sidx(kk, th1, a.Nth));
+    // b_k: 1 at k = 0 and L/2 (kk + 1 < L/2 always), 1/2 elsewhere
+    const float b0 = kk == 0 || kk == L / 2 ? 1.f : 0.5f;
+    const float2 a0 = cscale(make_float2(q0.x, q0.y), b0), a1 = cscale(make_float2(q1.x, q1.y), b0);
+    sm[spad(kk)] = pair_elem(kk, L, a0, a1);
+    if (kk > 0) sm[spad(L - kk)] = pair_elem(L - kk, L, a0, a1);
+    if (kk + 1 <= L / 2) {
+      const float2 c0 = cscale(make_float2(q0.z, q0.w), 0.5f), c1 = cscale(make_float2(q1.z, q1.w), 0.5f);
+      sm[spad(kk + 1)] = pair_elem(kk + 1, L, c0, c1);
+      sm[spad(L - kk - 1)] = pair_elem(L - kk - 1, L, c0, c1);
+    }
+  }
+  __syncthreads();
+  float2 v[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = sm[spad(t + i * T)];
+  __syncthreads();
+  any_fft<L, 1>(v, sm, t);
+  if (!live) return;
+  const int W = a.dhi - a.dlo + 1;
+  float* g0 = a.G + (((size_t)(s / kGatherSlices) * W + (th0 - a.dlo)) * L) * kGatherSlices + s % kGatherSlices;
+  for (int r = t; r < L; r += T) {
+    const float2 z = sm[spad(r)];
+    const float e = __ldg(a.erho + r);
+    g0[(size_t)r * kGatherSlices] = e * z.x;
+    if (th1 >= 0) g0[(size_t)(L + r) * kGatherSlices] = e * z.y;
+  }
+}
+
 // ---- launchers: one per kernel, for any length of a compile-time list ---------
 template <int... Ls>
 struct Lengths {};
@@ -569,6 +650,8 @@ void set_len_attrs(int optin) {
   if constexpr (L >= 1024) cudaFuncSetAttribute(k_adj_ingest_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_adj_polar2lp_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_adj_lpcols_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  cudaFuncSetAttribute(k_fwdT_rows_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  cudaFuncSetAttribute(k_fwdT_cols_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
 }
 template <int... Ls>
 cudaError_t set_attrs(Lengths<Ls...>, int optin) {
@@ -678,6 +761,32 @@ bool run_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st, cudaError_t*
   });
 }
 
+template <class LS>
+bool run_fwdT_rows(const FwdTRowsArgs& a, int S, cudaStream_t st, cudaError_t* err) {
+  return with_length(a.Nrho, LS(), [&](auto len) {
+    constexpr int LL = decltype(len)::value;
+    const int pairs = (a.nrows + 1) / 2;
+    const size_t sm = (size_t)P2<LL>::NSIG * P2<LL>::SLOTS * sizeof(float2);
+    if (!smem_fits(sm)) { *err = cudaErrorInvalidConfiguration; return; }
+    dim3 grid(S, (pairs + P2<LL>::NSIG - 1) / P2<LL>::NSIG);
+    k_fwdT_rows_p2<LL><<<grid, P2<LL>::BLOCK, sm, st>>>(a);
+    *err = cudaGetLastError();
+  });
+}
+
+template <class LS>
+bool run_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st, cudaError_t* err) {
+  return with_length(a.Nrho, LS(), [&](auto len) {
+    constexpr int LL = decltype(len)::value;
+    const int npairs = (a.dhi - a.dlo + 2) / 2;
+    const size_t sm = (size_t)P2<LL>::NSIG * P2<LL>::SLOTS * sizeof(float2);
+    if (!smem_fits(sm)) { *err = cudaErrorInvalidConfiguration; return; }
+    dim3 grid(S, (npairs + P2<LL>::NSIG - 1) / P2<LL>::NSIG);
+    k_fwdT_cols_p2<LL><<<grid, P2<LL>::BLOCK, sm, st>>>(a);
+    *err = cudaGetLastError();
+  });
+}
+
 // the register-FFT kernels of one list of lengths (lp_kernels.cu: powers of two;
 // lp_kernels_mr.cu: mixed lengths); false when the list does not hold the length
 #define LP_DECLARE_LENGTH_SET(PFX)                                                            \
@@ -687,7 +796,9 @@ bool run_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st, cudaError_t*
   bool PFX##_fwd_lp2polar(const FwdLP2PolarArgs& a, int S, cudaStream_t st, cudaError_t* err); \
   bool PFX##_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st, cudaError_t* err);    \
   bool PFX##_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st, cudaError_t* err); \
-  bool PFX##_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st, cudaError_t* err);
+  bool PFX##_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st, cudaError_t* err);    \
+  bool PFX##_fwdT_rows(const FwdTRowsArgs& a, int S, cudaStream_t st, cudaError_t* err);      \
+  bool PFX##_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st, cudaError_t* err);
 
 #define LP_DEFINE_LENGTH_SET(PFX, LIST)                                                           \
   cudaError_t PFX##_configure(int optin) { return set_attrs(LIST(), optin); }                    \
@@ -708,6 +819,12 @@ bool run_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st, cudaError_t*
   }                                                                                              \
   bool PFX##_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st, cudaError_t* err) {      \
     return run_adj_lpcols<LIST>(a, S, st, err);                                                 \
+  }                                                                                              \
+  bool PFX##_fwdT_rows(const FwdTRowsArgs& a, int S, cudaStream_t st, cudaError_t* err) {        \
+    return run_fwdT_rows<LIST>(a, S, st, err);                                                  \
+  }                                                                                              \
+  bool PFX##_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st, cudaError_t* err) {        \
+    return run_fwdT_cols<LIST>(a, S, st, err);                                                  \
   }
 
 LP_DECLARE_LENGTH_SET(p2)

@@ -173,3 +173,26 @@ def test_n4096_dot_product(torch_cuda):
     lhs = float(np.sum(Rn * g))
     assert abs(lhs - float(np.sum(f.astype(np.float64) * fT))) / abs(lhs) < 1e-6
     assert abs(lhs - float(np.sum(f.astype(np.float64) * fa.cpu().double().numpy()))) / abs(lhs) < 1e-2
+
+
+@pytest.mark.parametrize("args", [(512, 768, 256, 'cubic', 16), (96, 144, 45, 'cubic', 3), (128, 192, 64, 'linear', 2),
+                                  (64, 40, 32.5, 'cubic', 2), (512, 768, 253, 'cubic', 9)])
+def test_transpose_bit_reproducible(torch_cuda, args):
+    """The backward has no atomics: two calls on the same input give the same bits, also
+    after the scratch buffers were poisoned in between (odd padded sizes, a non-integer
+    axis and a slice count that is not a multiple of the gather's slice group included)."""
+    torch = torch_cuda
+    N0, Nproj, cor, interp, S = args
+    lp = _lp(N0, Nproj, S, cor, interp)
+    g = torch.as_tensor(np.random.default_rng(9).standard_normal((S, Nproj, N0)).astype(np.float32)).cuda()
+    f1 = torch.empty((S, N0, N0), device='cuda')
+    f2 = torch.empty((S, N0, N0), device='cuda')
+    lp.fwdp_T(f1, g, 0)
+    lp.clphandle[0].debug_fill_scratch(float('nan'), torch.cuda.current_stream().cuda_stream)
+    lp.fwdp_T(f2, g, 0)
+    torch.cuda.synchronize()
+    assert torch.isfinite(f1).all()
+    assert torch.equal(f1, f2)
+    tr = O.Transform.from_packed(*lp.tables())
+    gs = g[:2].cpu().double().numpy()
+    assert O.rel_l2(f1[:2].cpu().double().numpy(), tr.fwd_T(gs)) < 1e-5
