@@ -6,12 +6,17 @@
     b.run()                                          # one graph launch
     b.output_R(i), b.output_f(i)
 
-Requests with the same (N, Nproj) share one native handle and are
-concatenated into one batch.  The groups run one after another inside the
-graph, smallest geometry first (running them on parallel graph branches was
-measured slower: the large groups already fill the GPU and the branches only
-compete for L2).  The graph records an event when each group finishes, which
-gives per-request latencies measured from the start of the launch.
+Requests with the same (N, Nproj) share one native handle whose batch
+schedule the autotuner picks for the geometry (lp_autotune: slice chunks,
+streams, theta-convolution block), and are concatenated into one batch,
+fewest slices first.  The groups run one after another inside the graph,
+smallest geometry first (shortest work first: running them on parallel graph
+branches was measured slower, the large groups already fill the GPU and the
+branches only compete for L2).  Within a group the requests run in waves of
+consecutive requests of up to about 32 slices' worth of N=2048 work
+(wave_slices), so a request completes with its wave instead of with its whole
+group; the graph records an event after each wave, which gives per-request
+latencies measured from the start of the launch.
 """
 import time
 
@@ -32,9 +37,10 @@ def wait_event(ev, timeout_s, poll_s=0.001, clock=time.monotonic, sleep=time.sle
 
 
 def group_requests(requests):
-    """Requests (N, Nproj, slices) grouped by geometry, smallest N first.  Returns the
-    groups as (N, Nproj, total slices, request indices) and, per request, its
-    (group, slice offset in the group, slices)."""
+    """Requests (N, Nproj, slices) grouped by geometry, smallest N first, each group's
+    requests fewest slices first.  Returns the groups as (N, Nproj, total slices,
+    request indices in batch order) and, per request, its (group, slice offset in the
+    group, slices)."""
     requests = [tuple(int(v) for v in r) for r in requests]
     for N, Nproj, S in requests:
         if N < 1 or Nproj < 1 or S < 1:
@@ -44,6 +50,7 @@ def group_requests(requests):
         byg.setdefault((N, Nproj), []).append(i)
     groups, where = [], {}
     for (N, Nproj), idx in sorted(byg.items(), key=lambda kv: kv[0]):
+        idx = sorted(idx, key=lambda i: (requests[i][2], i))  # fewest slices first
         off = 0
         for i in idx:
             where[i] = (len(groups), off, requests[i][2])
@@ -52,8 +59,27 @@ def group_requests(requests):
     return groups, where
 
 
+def plan_waves(requests, idx, N, wave_slices=32):
+    """Consecutive runs of a group's requests (in batch order) whose slices add up to
+    at most wave_slices * (2048 / N)^2 (one request at least): [(first slice, end
+    slice, request indices)]."""
+    cap = max(1, int(wave_slices * (2048.0 / N) ** 2))
+    waves, cur, a, b = [], [], 0, 0
+    for i in idx:
+        S = requests[i][2]
+        if cur and b - a + S > cap:
+            waves.append((a, b, cur))
+            cur, a = [], b
+        cur.append(i)
+        b += S
+    if cur:
+        waves.append((a, b, cur))
+    return waves
+
+
 class UnevenBatch:
-    def __init__(self, requests, filter_type="ramp", interp_type="cubic", gpu=0, precision="reference"):
+    def __init__(self, requests, filter_type="ramp", interp_type="cubic", gpu=0, precision="reference",
+                 wave_slices=32, autotune=True):
         self.gpu = gpu
         self.dev = torch.device("cuda", gpu)
         self.requests = [tuple(int(v) for v in r) for r in requests]
@@ -63,7 +89,10 @@ class UnevenBatch:
             lp = lpTransform(N, Nproj, total, filter_type, N / 2, interp_type, precision)
             lp.precompute(1)
             lp.initcmem(1, gpu)
-            g = dict(lp=lp, N=N, Nproj=Nproj, S=total, idx=idx,
+            waves = plan_waves(self.requests, idx, N, wave_slices)
+            if autotune:
+                lp.autotune(gpu, max(b - a for a, b, _ in waves))
+            g = dict(lp=lp, N=N, Nproj=Nproj, S=total, idx=idx, waves=waves,
                      f=torch.zeros((total, N, N), device=self.dev),
                      R=torch.zeros((total, Nproj, N), device=self.dev),
                      Rout=torch.zeros((total, Nproj, N), device=self.dev),
@@ -87,34 +116,39 @@ class UnevenBatch:
     def output_f(self, i):
         return self._view(i, "fout")
 
-    def _work(self, g):
-        g["lp"].fwdp(g["Rout"], g["f"], self.gpu)
-        g["lp"].adjp(g["fout"], g["R"], self.gpu)
+    def _work(self, g, a, b):
+        g["lp"].fwdp(g["Rout"][a:b], g["f"][a:b], self.gpu)
+        g["lp"].adjp(g["fout"][a:b], g["R"][a:b], self.gpu)
 
     def run_eager(self):
-        """The same work without the graph (one group after the other)."""
+        """The same work without the graph (one wave after the other)."""
         for g in self.groups:
-            self._work(g)
+            for a, b, _ in g["waves"]:
+                self._work(g, a, b)
 
     def capture(self):
         main = torch.cuda.Stream(self.dev)
         with torch.cuda.stream(main):
             self.run_eager()  # warm-up outside capture
         torch.cuda.synchronize(self.dev)
+        waves = [(g, a, b, reqs) for g in self.groups for a, b, reqs in g["waves"]]
         try:
             self.t_start = torch.cuda.Event(enable_timing=True, external=True)
-            self.t_done = [torch.cuda.Event(enable_timing=True, external=True) for _ in self.groups]
+            self.t_done = [torch.cuda.Event(enable_timing=True, external=True) for _ in waves]
         except TypeError:  # torch without event-record graph nodes: no per-request latencies
             self.t_start = None
-            self.t_done = [None for _ in self.groups]
+            self.t_done = [None for _ in waves]
+        self._wave_of = {}
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph, stream=main):
             if self.t_start is not None:
                 self.t_start.record(main)
-            for g, ev in zip(self.groups, self.t_done):
-                self._work(g)
+            for w, ((g, a, b, reqs), ev) in enumerate(zip(waves, self.t_done)):
+                self._work(g, a, b)
                 if ev is not None:
                     ev.record(main)
+                for i in reqs:
+                    self._wave_of[i] = w
         self._main = main
 
     def run(self, timeout_s=None):
@@ -133,12 +167,12 @@ class UnevenBatch:
         wait_event(ev, timeout_s)
 
     def latencies_ms(self):
-        """Per-request latency of the last run: start of the launch to its group's end."""
+        """Per-request latency of the last run: start of the launch to its wave's end."""
         torch.cuda.synchronize(self.dev)
         if self.t_start is None:
             return None
-        per_group = [self.t_start.elapsed_time(ev) for ev in self.t_done]
-        return [per_group[self.where[i][0]] for i in range(len(self.requests))]
+        per_wave = [self.t_start.elapsed_time(ev) for ev in self.t_done]
+        return [per_wave[self._wave_of[i]] for i in range(len(self.requests))]
 
     @property
     def slices(self):

@@ -215,14 +215,22 @@ def test_host_pipeline_rejects_bad_arrays():
 
 def test_uneven_request_grouping():
     """Requests of the same geometry share one handle and one graph segment, smallest
-    geometry first; each request keeps its slice range in its group."""
+    geometry first, fewest slices first within a geometry; each request keeps its slice
+    range in its group; waves pack consecutive requests up to the slice budget."""
     pytest.importorskip("torch")
-    from lprec_gb300.batch import group_requests
-    groups, where = group_requests([(512, 768, 2), (256, 384, 3), (512, 768, 1), (256, 384, 4), (1024, 96, 1)])
-    assert groups == [(256, 384, 7, [1, 3]), (512, 768, 3, [0, 2]), (1024, 96, 1, [4])]
-    assert where == {1: (0, 0, 3), 3: (0, 3, 4), 0: (1, 0, 2), 2: (1, 2, 1), 4: (2, 0, 1)}
+    from lprec_gb300.batch import group_requests, plan_waves
+    reqs = [(512, 768, 2), (256, 384, 3), (512, 768, 1), (256, 384, 4), (1024, 96, 1)]
+    groups, where = group_requests(reqs)
+    assert groups == [(256, 384, 7, [1, 3]), (512, 768, 3, [2, 0]), (1024, 96, 1, [4])]
+    assert where == {1: (0, 0, 3), 3: (0, 3, 4), 2: (1, 0, 1), 0: (1, 1, 2), 4: (2, 0, 1)}
     with pytest.raises(ValueError):
         group_requests([(256, 384, 0)])
+    big = [(2048, 3000, s) for s in (5, 20, 9, 40, 3)]
+    (_, _, total, idx), = group_requests(big)[0]
+    assert idx == [4, 0, 2, 1, 3] and total == 77
+    waves = plan_waves(big, idx, 2048, 32)
+    assert waves == [(0, 17, [4, 0, 2]), (17, 37, [1]), (37, 77, [3])]
+    assert plan_waves(big, idx, 1024, 32) == [(0, 77, [4, 0, 2, 1, 3])]
 
 
 @pytest.mark.parametrize("precision", ["fp64", "reference"])
