@@ -1051,7 +1051,7 @@ __global__ void k_prefilter_T_rows_crop(PrefilterTRowsCropArgs a) {
   __syncthreads();
   const float w0 = line[0];
   float* dst = a.out + ((size_t)s * a.N0 + yo) * a.N0 - a.off;
-  for (int x = max(threadIdx.x, a.off); x < a.off + a.N0; x += blockDim.x) {
+  for (int x = a.off + threadIdx.x; x < a.off + a.N0; x += blockDim.x) {
     float v = LP_LAMBDA * line[x];
     if (x < 12) {
       float zn = z;

@@ -679,7 +679,8 @@ template <class LS>
 bool run_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st, cudaError_t* err) {
   return with_length(a.Nth, LS(), [&](auto len) {
     constexpr int LL = decltype(len)::value;
-    if (a.block == 512 || LL > 4096) {
+    // mixed lengths: one row per thread (two rows' odd-radix stages would spill)
+    if (a.block == 512 || LL > 4096 || !P2<LL>::POW2) {
       auto go = [&](auto blk) {
         constexpr int B = decltype(blk)::value;
         using C = TC<LL, B>;
