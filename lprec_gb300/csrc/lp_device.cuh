@@ -3,6 +3,8 @@
 // addressing, the chunked prefilter recursion, and the packing of two real
 // signals into one complex FFT.
 #pragma once
+#include <climits>
+
 #include "lp_kernels.cuh"
 #include "fft_mr.cuh"
 
@@ -272,14 +274,17 @@ __device__ __forceinline__ void rho_scatter_T(const ArgsT& a, int s, int r0, int
   const int L = a.Nrho;
   if (a.mono) {
     // pass (j, h): tap j of the points whose first tap is below (h = 0) or from (h = 1)
-    // the row's smallest first tap + L, so no two points of a pass meet modulo L
+    // the row's smallest first tap + L, so no two points of a pass meet modulo L (rows
+    // that do not wrap skip the second pass; every thread still meets every barrier)
     for (int j = 0; j < ntap; ++j) {
       for (int h = 0; h < 2; ++h) {
         for (int q = 0; q < 2; ++q) {
           const int r = q == 0 ? r0 : r1;
           if (r < 0) continue;
+          const int base = __ldg(a.rbase + r);
+          if (h == 1 && base == kNoWrap) continue;  // every point went in the first pass
           const float* row = a.Rin + ((size_t)s * a.Nproj0 + r / a.os) * a.N0;
-          const int top = __ldg(a.rbase + r) + L;
+          const int top = base == kNoWrap ? INT_MAX : base + L;
           for (int x = tid; x < a.N; x += nth) {
             const int xo = x - a.cor_off;
             if (xo < 0 || xo >= a.N0) continue;

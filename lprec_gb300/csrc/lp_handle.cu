@@ -740,7 +740,8 @@ static int init_fwd_impl(lp_handle* h, const int32_t* pi, int64_t ni, const Real
           ++npt;
         }
         if (npt > 0 && cmax - cmin >= 2 * Nrho) F->rho_mono = 0;
-        rbase[row] = npt > 0 ? cmin : 0;
+        // rows whose first taps span fewer than Nrho bins need only the first pass
+        rbase[row] = (npt > 0 && cmax - cmin >= Nrho) ? cmin : kNoWrap;
         if (!F->rho_mono) break;
       }
   }

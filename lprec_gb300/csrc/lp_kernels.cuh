@@ -146,12 +146,15 @@ void set_use_p2(bool on);
 
 namespace lpgb {
 // ---- exact transpose of the forward (autograd backward) --------------------
+constexpr int kNoWrap = 1 << 28;  // FwdTRowsArgs::rbase of a row whose taps do not wrap onto themselves
+
 struct FwdTRowsArgs {         // sinogram rows -> their log-polar rho half spectra (transposed lp2polar, part 1)
   const float* Rin;           // [S][Nproj0][N0] caller's gradient
   float2* rowspec;            // [S][nrows][Nk] per row of the span: a_k x R2C of the transposed rho interpolation
   const int* rhoc;            // [Nproj][N] rho coordinate per polar point (fixed point)
   const int* rows;            // rows of the span (multiples of os), sorted
-  const int* rbase;           // [Nproj] smallest first rho tap of each row
+  const int* rbase;           // [Nproj] smallest first rho tap of each row whose first taps span Nrho
+                              // bins or more; kNoWrap for the others
   int nrows;
   int N, N0, Nrho, Nk, Nproj0, os, cor_off, cubic;
   FFTPlan plan;               // length Nrho
