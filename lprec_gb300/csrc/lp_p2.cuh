@@ -679,8 +679,11 @@ template <class LS>
 bool run_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st, cudaError_t* err) {
   return with_length(a.Nth, LS(), [&](auto len) {
     constexpr int LL = decltype(len)::value;
-    // mixed lengths: one row per thread (two rows' odd-radix stages would spill)
-    if (a.block == 512 || LL > 4096 || !P2<LL>::POW2) {
+    // mixed lengths whose FFT ends in an odd stage (T odd: 528, 1008): one row per
+    // thread (measured at N = 528: 1.00 against 1.21 ms with two rows per thread; at
+    // N = 2016 two rows per thread are faster, 1.29x against 1.40x the power-of-two
+    // rate per pixel)
+    if (a.block == 512 || LL > 4096 || (!P2<LL>::POW2 && pow2_part(LL / 16) == 1)) {
       auto go = [&](auto blk) {
         constexpr int B = decltype(blk)::value;
         using C = TC<LL, B>;
