@@ -728,12 +728,25 @@ def run_ours(args):
     windows = []
     for w in range(3):
         lb = link if w == 0 else link_gbs()
+        traces = []
         q0.record(stream)
         for _ in range(ke):
-            e2e_step()
+            tf_, ta_ = [], []
+            lp.fwd(fh, dev, out=Rh_out, trace=tf_)
+            lp.adj(Rh, dev, out=fh_out, trace=ta_)
+            traces.append((tf_, ta_))
         q1.record(stream)
         torch.cuda.synchronize()
-        windows.append({"ms_per_step": round(q0.elapsed_time(q1) / ke, 2), "link_gbs_before": lb})
+        # per window: the transforms' busy time, the gaps in which they waited (on copies
+        # or on the host), and the copies' effective rates
+        tl = [e2e_timeline(a_, b_) for a_, b_ in traces]
+        busy = sum(t["fwd"]["compute_ms"] + t["adj"]["compute_ms"] for t in tl) / ke
+        h2d_ms = sum(t["fwd"]["h2d_ms"] + t["adj"]["h2d_ms"] for t in tl) / ke
+        d2h_ms = sum(t["fwd"]["d2h_ms"] + t["adj"]["d2h_ms"] for t in tl) / ke
+        nb = (f.numel() + R.numel()) * 4
+        windows.append({"ms_per_step": round(q0.elapsed_time(q1) / ke, 2), "link_gbs_before": lb,
+                        "transform_ms_per_step": round(busy, 2),
+                        "h2d_gbs": round(nb / (h2d_ms / 1e3) / 1e9, 1), "d2h_gbs": round(nb / (d2h_ms / 1e3) / 1e9, 1)})
     e2e_ms = statistics.median(wd["ms_per_step"] for wd in windows)
     link_after = link_gbs()
     # one more step with events around every chunk's copies and transform
