@@ -563,6 +563,7 @@ def run_side_configs(torch, dev, reps=5):
         lp = lpTransform(N0, Np, S, "shepp-logan", cor, "cubic")
         lp.precompute(1)
         lp.initcmem(1, dev)
+        lp.autotune(dev)  # as for the headline: the schedule of this geometry
         h = lp.clphandle[dev]
         f = phantoms_gpu(torch, N0, S, 10, 4, dev)
         R = torch.empty((S, Np, N0), device=dev)
@@ -572,7 +573,7 @@ def run_side_configs(torch, dev, reps=5):
             lp.fwdp(R, f, dev)
             lp.adjp(fo, R, dev)
         t = timed(step, reps)
-        res[name] = {"N": h.N, "Nrho": h.Nrho, "osangles": h.osangles, "slices": S, "ms": t,
+        res[name] = {"N": h.N, "Nrho": h.Nrho, "osangles": h.osangles, "slices": S, "ms": t, "schedule": h.schedule(),
                      "slices_per_s": S / t * 1e3, "ns_per_padded_pixel": t * 1e6 / (S * h.N * h.N)}
         lp.close()
         del f, R, fo

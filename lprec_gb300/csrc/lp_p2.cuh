@@ -120,7 +120,7 @@ struct TC {
   static constexpr int KT = NSIG0 < kSpecTile ? NSIG0 : kSpecTile;
   static constexpr int NSIG = NSIG0 / KT * KT;       // a multiple of KT
   static constexpr int BLOCK = NSIG * T;
-  static constexpr int MINB = (L & (L - 1)) == 0 ? 768 / BLOCK : (768 / BLOCK > 2 ? 2 : 768 / BLOCK);
+  static constexpr int MINB = (L & (L - 1)) == 0 ? 768 / BLOCK : (768 / BLOCK > 4 ? 4 : 768 / BLOCK);
   static constexpr int SLOTS = reg_fft_slots(L) + (KT > 1 ? 16 / KT : 0);
 };
 
