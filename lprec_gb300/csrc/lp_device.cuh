@@ -263,35 +263,39 @@ __device__ __forceinline__ float2 pair_elem(int p, int L, float2 v0, float2 v1) 
 // Transposed 1-D interpolation along rho of the internal sinogram rows r0 and r1
 // (r1 < 0: none) of slice s, added into acc(q, bin) for row q = 0, 1.  Called by
 // all threads of the block (the same number of barriers on every path); thread
-// tid of nth takes points x = tid, tid + nth, ...  With strictly monotone first
-// taps (a.mono) the points of one tap index and one window of Nrho first taps hit
-// distinct bins, so tap j of those points is added in one pass without
-// conflicts, in a fixed order; otherwise one thread per row adds its points' taps
-// in x order.
+// tid of nth takes its share of the points.  With strictly monotone first taps
+// (a.mono) the points of one residue class of x modulo the tap count and one window
+// of first taps hit distinct bins with all their taps, so they are added in one
+// pass without conflicts, in a fixed order; otherwise one thread per row adds its
+// points' taps in x order.
 template <class ArgsT, class Acc>
 __device__ __forceinline__ void rho_scatter_T(const ArgsT& a, int s, int r0, int r1, int tid, int nth, Acc acc) {
   const int ntap = a.cubic ? 4 : 2;
   const int L = a.Nrho;
   if (a.mono) {
-    // pass (j, h): tap j of the points whose first tap is below (h = 0) or from (h = 1)
-    // the row's smallest first tap + L, so no two points of a pass meet modulo L (rows
-    // that do not wrap skip the second pass; every thread still meets every barrier)
-    for (int j = 0; j < ntap; ++j) {
+    // pass (p, h): the points x = p (mod ntap) whose first tap is below (h = 0) or from
+    // (h = 1) the row's smallest first tap + L - ntap + 1, all taps of each.  First taps
+    // strictly monotone in x put the points of one residue class at least ntap apart,
+    // and a window spans at most L - ntap, so no two taps of a pass meet modulo L: each
+    // bin takes at most one addition per pass, in a fixed pass order (rows that do not
+    // wrap skip the second window; every thread still meets every barrier)
+    for (int p = 0; p < ntap; ++p) {
       for (int h = 0; h < 2; ++h) {
         for (int q = 0; q < 2; ++q) {
           const int r = q == 0 ? r0 : r1;
           if (r < 0) continue;
           const int base = __ldg(a.rbase + r);
-          if (h == 1 && base == kNoWrap) continue;  // every point went in the first pass
+          if (h == 1 && base == kNoWrap) continue;  // every point went in the first window
           const float* row = a.Rin + ((size_t)s * a.Nproj0 + r / a.os) * a.N0;
-          const int top = base == kNoWrap ? INT_MAX : base + L;
-          for (int x = tid; x < a.N; x += nth) {
+          const int top = base == kNoWrap ? INT_MAX : base + L - ntap + 1;
+          for (int x = p + ntap * tid; x < a.N; x += ntap * nth) {
             const int xo = x - a.cor_off;
             if (xo < 0 || xo >= a.N0) continue;
             float w[4];
             const int c = axis_weights_fx(__ldg(a.rhoc + (size_t)r * a.N + x), a.F, a.fsc, a.cubic, w);
             if ((c >= top) != (h == 1)) continue;
-            acc(q, wrapi(c + j, L)) += w[j] * __ldg(row + xo);
+            const float val = __ldg(row + xo);
+            for (int j = 0; j < ntap; ++j) acc(q, wrapi(c + j, L)) += w[j] * val;
           }
         }
         __syncthreads();

@@ -121,13 +121,19 @@ struct FwdDev {
   int rho_mono = 1;        // every row's first rho tap strictly monotone over the row (see FwdTRowsArgs)
   DevBuf<int> rbase;       // [Nproj] per internal row: its smallest first rho tap
   // exact transpose, built by its first call: the image cells' lists of log-polar
-  // points of all spans (CSR), the spans' real log-polar values (FwdTColsArgs) and
-  // the row spectra [Nslices][rows of a span][Nk]
+  // points of all spans (CSR), the points' real values in list order (FwdTColsArgs)
+  // and the row spectra [Nslices][rows of a span][rowspec_stride(Nk)]
   bool gather_ready = false;
   DevBuf<int> cell_off;
-  DevBuf<int4> cell_pts;
+  DevBuf<int2> cell_pts;
+  DevBuf<int> lppos[3];    // per span [W][Nrho]: a log-polar point's index in cell_pts, -1 for none
+  size_t npts = 0;
   DevBuf<float> lpg;
   DevBuf<float2> rowspec;
+  // per span, the theta columns' lists of (row, tap weight), rows ascending (CSR over
+  // the Nth columns): the theta convolution gathers its input from the row spectra
+  DevBuf<int> coff[3];
+  DevBuf<int2> cent[3];
 };
 static const int kTransposeCW = 8;
 
@@ -219,10 +225,13 @@ static void free_fwd(FwdDev* f) {
     f->c2lp[k].free_();
     f->rows[k].free_();
     f->blk[k].free_();
+    f->coff[k].free_();
+    f->cent[k].free_();
   }
   f->rbase.free_();
   f->cell_off.free_();
   f->cell_pts.free_();
+  for (int k = 0; k < 3; ++k) f->lppos[k].free_();
   f->lpg.free_();
   f->rowspec.free_();
   f->thc.free_();
@@ -716,11 +725,12 @@ static int init_fwd_impl(lp_handle* h, const int32_t* pi, int64_t ni, const Real
   }
   F->lo = lo;
   F->hi = hi;
-  // the transposed rho interpolation adds tap j of every point of a row in two passes
-  // (first taps below and from rbase + Nrho): that needs the rows' first taps strictly
-  // monotone in x (the log-polar rho of a polar point is the log of an affine function
-  // of s, and it steps by more than one texel per detector sample) spanning fewer than
-  // 2 Nrho bins -- a row's points at the low end of the rho range wrap onto its high end
+  // the transposed rho interpolation adds all taps of the points of one residue class
+  // of x per pass, in two windows of first taps (below and from rbase + Nrho - ntap + 1):
+  // that needs the rows' first taps strictly monotone in x (the log-polar rho of a
+  // polar point is the log of an affine function of s, and it steps by more than one
+  // texel per detector sample) spanning at most 2 (Nrho - ntap) + 1 bins -- a row's
+  // points at the low end of the rho range wrap onto its high end
   std::vector<int> rbase(Nproj, 0);
   {
     const int coff = N / 2 - h->cor;
@@ -739,9 +749,11 @@ static int init_fwd_impl(lp_handle* h, const int32_t* pi, int64_t ni, const Real
           cmax = std::max(cmax, c);
           ++npt;
         }
-        if (npt > 0 && cmax - cmin >= 2 * Nrho) F->rho_mono = 0;
-        // rows whose first taps span fewer than Nrho bins need only the first pass
-        rbase[row] = (npt > 0 && cmax - cmin >= Nrho) ? cmin : kNoWrap;
+        // two windows of first taps spanning at most Nrho - ntap each (rho_scatter_T)
+        const int ntap = h->cubic ? 4 : 2;
+        if (npt > 0 && cmax - cmin > 2 * (Nrho - ntap) + 1) F->rho_mono = 0;
+        // rows whose first taps span at most Nrho - ntap bins need only the first window
+        rbase[row] = (npt > 0 && cmax - cmin > Nrho - ntap) ? cmin : kNoWrap;
         if (!F->rho_mono) break;
       }
   }
@@ -1203,21 +1215,59 @@ static int build_transpose_tables(lp_handle* h) {
           if (p.x != LP_FX_NONE) off[cell(p) + 1]++;
         }
     for (size_t c = 0; c < (size_t)N * N; ++c) off[c + 1] += off[c];
-    std::vector<int4> pts(std::max(off[(size_t)N * N], 1), make_int4(0, 0, 0, 0));
+    const size_t npts = off[(size_t)N * N];
+    std::vector<int2> pts(std::max<size_t>(npts, 1), make_int2(0, 0));
     std::vector<int> fill(off.begin(), off.end() - 1);
-    for (int k = 0; k < 3; ++k)
+    for (int k = 0; k < 3; ++k) {
+      std::vector<int> pos((size_t)W * Nrho, -1);
       for (int t = F->dlo; t <= F->dhi; ++t)
         for (int r = 0; r < Nrho; ++r) {
           const int2 p = c2[k][(size_t)t * Nrho + r];
-          if (p.x != LP_FX_NONE) pts[fill[cell(p)]++] = make_int4(p.x, p.y, (t - F->dlo) * Nrho + r, k);
+          if (p.x == LP_FX_NONE) continue;
+          const int e = fill[cell(p)]++;
+          pts[e] = p;
+          pos[(size_t)(t - F->dlo) * Nrho + r] = e;
         }
+      CUDA_TRY(dev_upload(F->lppos[k], pos));
+    }
     CUDA_TRY(dev_upload(F->cell_off, off));
     CUDA_TRY(dev_upload(F->cell_pts, pts));
+    F->npts = npts;
     const size_t groups = (h->Nslices + kGatherSlices - 1) / kGatherSlices;
-    CUDA_TRY(dev_alloc(F->lpg, 3 * groups * kGatherSlices * W * Nrho));
+    CUDA_TRY(dev_alloc(F->lpg, groups * kGatherSlices * std::max<size_t>(npts, 1)));
   }
   const int nr = std::max(F->nrows[0], std::max(F->nrows[1], F->nrows[2]));
-  CUDA_TRY(dev_alloc(F->rowspec, (size_t)h->Nslices * std::max(nr, 1) * h->Nk));
+  CUDA_TRY(dev_alloc(F->rowspec, (size_t)h->Nslices * std::max(nr, 1) * rowspec_stride(h->Nk)));
+  // the theta columns' (row, tap) lists: a row's taps reach columns first_tap + j (mod
+  // Nth); entries of a column in ascending row order; the weights come from the same
+  // device function as the forward's theta interpolation (k_fwdT_tapw)
+  {
+    std::vector<int> thc(F->thc.n);
+    CUDA_TRY(cudaMemcpy(thc.data(), F->thc.p, thc.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    const int ntap = h->cubic ? 4 : 2;
+    for (int k = 0; k < 3; ++k) {
+      std::vector<int> rows(F->nrows[k]);
+      if (!rows.empty())
+        CUDA_TRY(cudaMemcpy(rows.data(), F->rows[k].p, rows.size() * sizeof(int), cudaMemcpyDeviceToHost));
+      std::vector<int> off(Nth + 1, 0);
+      auto col = [&](int i, int j) {
+        const int c = (first_tap(thc[rows[i]], F->F, h->cubic) + j) % Nth;
+        return c < 0 ? c + Nth : c;
+      };
+      for (int i = 0; i < (int)rows.size(); ++i)
+        for (int j = 0; j < ntap; ++j) off[col(i, j) + 1]++;
+      for (int c = 0; c < Nth; ++c) off[c + 1] += off[c];
+      std::vector<int2> ent(std::max(off[Nth], 1), make_int2(0, 0));
+      std::vector<int> fill(off.begin(), off.end() - 1);
+      for (int i = 0; i < (int)rows.size(); ++i)
+        for (int j = 0; j < ntap; ++j) ent[fill[col(i, j)]++] = make_int2(i, j);
+      CUDA_TRY(dev_upload(F->coff[k], off));
+      CUDA_TRY(dev_upload(F->cent[k], ent));
+      if (off[Nth] > 0)
+        CUDA_TRY(launch_fwdT_tapw(F->cent[k].p, off[Nth], F->rows[k].p, F->thc.p, F->F, F->fsc, h->cubic, 0));
+    }
+    CUDA_TRY(cudaStreamSynchronize(0));
+  }
   F->gather_ready = true;
   return LP_OK;
 }
@@ -1239,25 +1289,34 @@ int lp_fwd_transpose(lp_handle* h, float* f, const float* R, int S0, void* strea
   float* acc = F->fbuf.p;
   const int W = F->dhi - F->dlo + 1;
   if (W <= 0) CUDA_TRY(cudaMemsetAsync(acc, 0, (size_t)S0 * h->N * h->N * sizeof(float), st));
-  const size_t span_stride =
-      (size_t)(h->Nslices + kGatherSlices - 1) / kGatherSlices * kGatherSlices * (W > 0 ? W : 1) * h->Nrho;
+  // register-FFT theta lengths gather the theta convolution's input from the row
+  // spectra; the generic FFT sums them into the spectrum first (k_fwdT_colsum)
+  const bool gathered =
+      theta_conv_gathers(h->Nth, std::max(F->nrows[0], std::max(F->nrows[1], F->nrows[2])));
   for (int k = 0; k < 3 && W > 0; ++k) {
     FwdTRowsArgs a0{R, F->rowspec.p, F->rhoc.p, F->rows[k].p, F->rbase.p, F->nrows[k], h->N, h->N0, h->Nrho,
                     h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho, F->F, F->fsc, F->rho_mono};
     CUDA_TRY(launch(h, K_FWDT_ROWS, st, [&] { return launch_fwdT_rows(a0, S0, st); }));
-    FwdTColSumArgs a1{F->rowspec.p, h->spec.p, F->thc.p, F->rows[k].p, F->blk[k].p, F->nrows[k], h->Nth, h->Nk,
-                      F->lo, F->hi, kTransposeCW, h->cubic, F->F, F->fsc};
-    CUDA_TRY(launch(h, K_FWDT_COLSUM, st, [&] { return launch_fwdT_colsum(a1, S0, F->nblk[k], st); }));
+    if (!gathered) {
+      FwdTColSumArgs a1{F->rowspec.p, h->spec.p, F->thc.p, F->rows[k].p, F->blk[k].p, F->nrows[k], h->Nth, h->Nk,
+                        F->lo, F->hi, kTransposeCW, h->cubic, F->F, F->fsc};
+      CUDA_TRY(launch(h, K_FWDT_COLSUM, st, [&] { return launch_fwdT_colsum(a1, S0, F->nblk[k], st); }));
+    }
     ThetaConvArgs a2{h->spec.p, F->fz.p, h->Nth, h->Nk, F->lo, F->hi,
                      F->dlo, F->dhi, 1, h->plan_th, h->fwd_tblock};
+    if (gathered) {
+      a2.rowspec = F->rowspec.p;
+      a2.coff = F->coff[k].p;
+      a2.cent = F->cent[k].p;
+      a2.nrows = F->nrows[k];
+    }
     CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
-    FwdTColsArgs a3{h->spec.p, F->lpg.p + k * span_stride, h->erho.p, h->Nth, h->Nrho, h->Nk, F->dlo, F->dhi,
+    FwdTColsArgs a3{h->spec.p, F->lpg.p, F->lppos[k].p, F->npts, h->erho.p, h->Nth, h->Nrho, h->Nk, F->dlo, F->dhi,
                     h->plan_rho};
     CUDA_TRY(launch(h, K_FWDT_COLS, st, [&] { return launch_fwdT_cols(a3, S0, st); }));
   }
   if (W > 0) {
-    FwdTGatherArgs a4{F->lpg.p, span_stride, acc, F->cell_off.p, F->cell_pts.p, h->N, W, h->Nrho, h->cubic,
-                      F->F, F->fsc};
+    FwdTGatherArgs a4{F->lpg.p, F->npts, acc, F->cell_off.p, F->cell_pts.p, h->N, h->cubic, F->F, F->fsc};
     CUDA_TRY(launch(h, K_FWDT_GATHER, st, [&] { return launch_fwdT_gather(a4, S0, st); }));
   }
   if (h->cubic) {

@@ -731,9 +731,16 @@ cudaError_t launch_fwd_c2lp(const FwdC2LPArgs& a, int S, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+bool theta_conv_gathers(int Nth, int nrows) {
+  if (!g_use_p2) return false;
+  const size_t need = p2_has_length(Nth) ? p2_gather_smem(Nth, nrows) : mr_gather_smem(Nth, nrows);
+  return need > 0 && smem_fits(need);
+}
+
 cudaError_t launch_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
   if (g_use_p2 && (p2_theta_conv(a, S, st, &pe) || mr_theta_conv(a, S, st, &pe))) return pe;
+  if (a.rowspec) return cudaErrorNotSupported;  // the gathered input needs a register-FFT length
   if (smem_ok(smem_theta(a.Nth)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.Nk + 1) / 2);
   k_theta_conv<<<grid, kFFTThreads, smem_theta(a.Nth), st>>>(a);
@@ -826,12 +833,12 @@ __global__ void __launch_bounds__(256) k_fwdT_rows(FwdTRowsArgs a) {
   for (int i = threadIdx.x; i < L; i += blockDim.x) A.set(i, make_float2(u[i], u[L + i]));
   __syncthreads();
   const CBuf Z = fft_block<-1>(A, B, a.plan, 1, 0);
-  float2* o0 = a.rowspec + ((size_t)s * a.nrows + i0) * a.Nk;
+  float2* o0 = a.rowspec + ((size_t)s * a.nrows + i0) * rowspec_stride(a.Nk);
   for (int k = threadIdx.x; k < a.Nk; k += blockDim.x) {
     float2 va, vb;
     split_rows_T(Z.get(k), Z.get(k == 0 ? 0 : L - k), k, L, &va, &vb);
     o0[k] = va;
-    if (r1 >= 0) o0[a.Nk + k] = vb;
+    if (r1 >= 0) o0[rowspec_stride(a.Nk) + k] = vb;
   }
 }
 
@@ -846,7 +853,7 @@ __global__ void __launch_bounds__(256) k_fwdT_colsum(FwdTColSumArgs a) {
   const int c0 = a.lo + blockIdx.y * kColSumCW;
   const int2 rr = __ldg(a.blk + blockIdx.y);
   const int ntap = a.cubic ? 4 : 2;
-  const float2* rs = a.rowspec + (size_t)s * a.nrows * a.Nk;
+  const float2* rs = a.rowspec + (size_t)s * a.nrows * rowspec_stride(a.Nk);
   float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
   for (int k = threadIdx.x; k < a.Nk; k += blockDim.x) {
     float2 acc[kColSumCW];
@@ -855,7 +862,7 @@ __global__ void __launch_bounds__(256) k_fwdT_colsum(FwdTColSumArgs a) {
     for (int i = rr.x; i < rr.y; ++i) {
       float w[4];
       const int t0 = axis_weights_fx(__ldg(a.thc + __ldg(a.rows + i)), a.F, a.fsc, a.cubic, w);
-      const float2 z = __ldg(rs + (size_t)i * a.Nk + k);
+      const float2 z = __ldg(rs + (size_t)i * rowspec_stride(a.Nk) + k);
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         if (j >= ntap) break;
@@ -895,23 +902,34 @@ __global__ void __launch_bounds__(256) k_fwdT_cols(FwdTColsArgs a) {
   }
   __syncthreads();
   const CBuf z = fft_block<1>(A, B, a.plan, 1, 0);
-  const int W = a.dhi - a.dlo + 1;
-  float* g0 = a.G + (((size_t)(s / kGatherSlices) * W + (th0 - a.dlo)) * L) * kGatherSlices + s % kGatherSlices;
+  float* g0 = a.G + (size_t)(s / kGatherSlices) * a.npts * kGatherSlices + s % kGatherSlices;
+  const int* pos = a.pos + (size_t)(th0 - a.dlo) * L;
   for (int r = threadIdx.x; r < L; r += blockDim.x) {
     const float2 zv = z.get(r);
     const float e = __ldg(a.erho + r);
-    g0[(size_t)r * kGatherSlices] = e * zv.x;
-    if (th1 >= 0) g0[(size_t)(L + r) * kGatherSlices] = e * zv.y;
+    const int p0 = __ldg(pos + r);
+    if (p0 >= 0) g0[(size_t)p0 * kGatherSlices] = e * zv.x;
+    if (th1 >= 0) {
+      const int p1 = __ldg(pos + L + r);
+      if (p1 >= 0) g0[(size_t)p1 * kGatherSlices] = e * zv.y;
+    }
   }
 }
 
 // Transposed Cartesian interpolation as a gather: output pixel (X, Y) of the padded
 // grid sums, over the cells of the points whose taps reach it (cell = the integer
-// part of a point's coordinates), each point's value times its tap weight, in cell
-// and list order.  No atomics: the result is the same bits on every run.  A point
-// with integer part (ix, iy) reaches columns ix - o .. ix - o + n - 1 (o = 1, n = 4
-// cubic; o = 0, n = 2 linear), so pixel X reads cells ix = X + o - i for tap i.
-// A thread computes one pixel for the kGatherSlices slices of a group.
+// part of a point's coordinates), each point's value times its tap weight, in a
+// fixed order.  No atomics: the result is the same bits on every run.  A point with
+// integer part (ix, iy) reaches columns ix - o .. ix - o + n - 1 (o = 1, n = 4 cubic;
+// o = 0, n = 2 linear), so pixel X reads cells ix = X + o - i for tap i.  The n cells
+// of one cell row are consecutive in the cell-sorted list unless they wrap at the
+// image edge, so away from the edge a pixel walks n runs of points (one per tap row
+// j) and takes each point's tap i from its own cell.  A thread computes one pixel for
+// the kGatherSlices slices of a group.
+__device__ __forceinline__ float pick_w(const float* w, int i) {
+  return i == 0 ? w[0] : (i == 1 ? w[1] : (i == 2 ? w[2] : w[3]));
+}
+
 __global__ void __launch_bounds__(256) k_fwdT_gather(FwdTGatherArgs a, int S) {
   const int X = blockIdx.x * 32 + (threadIdx.x & 31);
   const int Y = blockIdx.y * 8 + (threadIdx.x >> 5);
@@ -924,33 +942,55 @@ __global__ void __launch_bounds__(256) k_fwdT_gather(FwdTGatherArgs a, int S) {
   for (int q = 0; q < kGatherSlices; ++q) acc[q] = 0.f;
   const int o = a.cubic ? 1 : 0;
   const int n = a.cubic ? 4 : 2;
-  // this slice group's values: [W][Nrho][kGatherSlices] per span
-  const float* G = a.G + (size_t)blockIdx.z * a.W * a.Nrho * kGatherSlices;
+  // this slice group's values, [npts][kGatherSlices] in list order
+  const float* G = a.G + (size_t)blockIdx.z * a.npts * kGatherSlices;
+  auto add = [&](int e, int2 p, int i, int j) {
+    float wx[4], wy[4];
+    axis_weights_fx(p.x, a.F, a.fsc, a.cubic, wx);
+    axis_weights_fx(p.y, a.F, a.fsc, a.cubic, wy);
+    const float w = pick_w(wy, j) * pick_w(wx, i);
+    const float4* g = reinterpret_cast<const float4*>(G + (size_t)e * kGatherSlices);
+    const float4 u = __ldg(g), v = __ldg(g + 1);
+    acc[0] += w * u.x;
+    acc[1] += w * u.y;
+    acc[2] += w * u.z;
+    acc[3] += w * u.w;
+    acc[4] += w * v.x;
+    acc[5] += w * v.y;
+    acc[6] += w * v.z;
+    acc[7] += w * v.w;
+  };
+  const int xlo = X + o - (n - 1), xhi = X + o;
+  if (xlo >= 0 && xhi < a.N) {
+    // the n runs walked side by side (independent load chains), run j in list order
+    int e[4], e1[4], m = 0;
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    if (j >= n) break;
-    const int cy = wrapi(Y + o - j, a.N);
+    for (int j = 0; j < 4; ++j) {
+      e[j] = e1[j] = 0;
+      if (j < n) {
+        const int* co = a.cell_off + (size_t)wrapi(Y + o - j, a.N) * a.N;
+        e[j] = __ldg(co + xlo);
+        e1[j] = __ldg(co + xhi + 1);
+        m = max(m, e1[j] - e[j]);
+      }
+    }
+    for (int step = 0; step < m; ++step) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      if (i >= n) break;
-      const int c = cy * a.N + wrapi(X + o - i, a.N);
-      const int e1 = __ldg(a.cell_off + c + 1);
-      for (int e = __ldg(a.cell_off + c); e < e1; ++e) {
-        const int4 p = __ldg(a.pts + e);
-        float wx[4], wy[4];
-        axis_weights_fx(p.x, a.F, a.fsc, a.cubic, wx);
-        axis_weights_fx(p.y, a.F, a.fsc, a.cubic, wy);
-        const float w = wy[j] * wx[i];
-        const float4* g = reinterpret_cast<const float4*>(G + p.w * a.span_stride + (size_t)p.z * kGatherSlices);
-        const float4 u = __ldg(g), v = __ldg(g + 1);
-        acc[0] += w * u.x;
-        acc[1] += w * u.y;
-        acc[2] += w * u.z;
-        acc[3] += w * u.w;
-        acc[4] += w * v.x;
-        acc[5] += w * v.y;
-        acc[6] += w * v.z;
-        acc[7] += w * v.w;
+      for (int j = 0; j < 4; ++j) {
+        if (e[j] < e1[j]) {
+          const int2 p = __ldg(a.pts + e[j]);
+          add(e[j], p, xhi - wrapi(fx_int(p.x, a.F), a.N), j);
+          ++e[j];
+        }
+      }
+    }
+  } else {
+    for (int j = 0; j < n; ++j) {
+      const int* co = a.cell_off + (size_t)wrapi(Y + o - j, a.N) * a.N;
+      for (int i = 0; i < n; ++i) {
+        const int cx = wrapi(X + o - i, a.N);
+        const int e1 = __ldg(co + cx + 1);
+        for (int e = __ldg(co + cx); e < e1; ++e) add(e, __ldg(a.pts + e), i, j);
       }
     }
   }
@@ -1099,6 +1139,25 @@ cudaError_t launch_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st) {
   cudaFuncSetAttribute(k_fwdT_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
   dim3 grid(S, (a.dhi - a.dlo + 2) / 2);
   k_fwdT_cols<<<grid, 256, sm, st>>>(a);
+  return cudaGetLastError();
+}
+
+// the theta columns' tap weights of the exact transpose: entry (i, j) -> (i, bits of
+// tap j's weight of the span's row i), the weight the forward's theta interpolation uses
+__global__ void k_fwdT_tapw(int2* cent, int n, const int* rows, const int* thc, int F, float fsc, int cubic) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  int2 q = cent[e];
+  float w[4];
+  axis_weights_fx(__ldg(thc + __ldg(rows + q.x)), F, fsc, cubic, w);
+  q.y = __float_as_int(w[q.y & 3]);
+  cent[e] = q;
+}
+
+cudaError_t launch_fwdT_tapw(int2* cent, int n, const int* rows, const int* thc, int F, float fsc, int cubic,
+                             cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_fwdT_tapw<<<(n + 255) / 256, 256, 0, st>>>(cent, n, rows, thc, F, fsc, cubic);
   return cudaGetLastError();
 }
 

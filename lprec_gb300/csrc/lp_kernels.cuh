@@ -65,7 +65,19 @@ struct ThetaConvArgs {        // FFT along theta, multiply by the kernel, invers
   int conj_fz;
   FFTPlan plan;               // length Nth
   int block;                  // power-of-two kernels: threads per block (256 or 512; 0 = 256)
+  // exact transpose (register-FFT lengths only): with rowspec set, input column c of
+  // frequency k is the sum over cent[coff[c] .. coff[c+1]) in that order (rows ascending) of
+  // weight * rowspec[s][row][k] -- the transposed theta taps, gathered instead of summed
+  // into the spectrum by a separate pass
+  const float2* rowspec;      // [S][nrows][rowspec_stride(Nk)]
+  const int* coff;            // [Nth + 1]
+  const int2* cent;           // (row within the span, float bits of the tap weight)
+  int nrows;
 };
+
+// row stride of the transpose's row spectra: Nk rounded up to a multiple of 4, so that
+// frequencies k, k+1 (k even) of a row are one aligned 16-byte access
+__host__ __device__ inline int rowspec_stride(int Nk) { return spec_rows(Nk); }
 
 struct FwdLP2PolarArgs {      // inverse FFT along rho of theta-combined columns, polar gather
   const float2* spec;         // [S] spectra, tiled layout
@@ -133,6 +145,8 @@ cudaError_t launch_fwd_ingest(const FwdIngestArgs& a, int S, cudaStream_t st);
 cudaError_t launch_col_prefilter(const ColPrefilterArgs& a, int S, cudaStream_t st);
 cudaError_t launch_fwd_c2lp(const FwdC2LPArgs& a, int S, cudaStream_t st);
 cudaError_t launch_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st);
+// launch_theta_conv takes ThetaConvArgs::rowspec at this length and row count
+bool theta_conv_gathers(int Nth, int nrows);
 cudaError_t launch_fwd_lp2polar(const FwdLP2PolarArgs& a, int S, cudaStream_t st);
 cudaError_t launch_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st);
 cudaError_t launch_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st);
@@ -150,24 +164,26 @@ constexpr int kNoWrap = 1 << 28;  // FwdTRowsArgs::rbase of a row whose taps do 
 
 struct FwdTRowsArgs {         // sinogram rows -> their log-polar rho half spectra (transposed lp2polar, part 1)
   const float* Rin;           // [S][Nproj0][N0] caller's gradient
-  float2* rowspec;            // [S][nrows][Nk] per row of the span: a_k x R2C of the transposed rho interpolation
+  float2* rowspec;            // [S][nrows][rowspec_stride(Nk)] per row of the span: a_k x R2C of the
+                              // transposed rho interpolation
   const int* rhoc;            // [Nproj][N] rho coordinate per polar point (fixed point)
   const int* rows;            // rows of the span (multiples of os), sorted
-  const int* rbase;           // [Nproj] smallest first rho tap of each row whose first taps span Nrho
-                              // bins or more; kNoWrap for the others
+  const int* rbase;           // [Nproj] smallest first rho tap of each row whose first taps span more
+                              // than Nrho - ntap bins; kNoWrap for the others
   int nrows;
   int N, N0, Nrho, Nk, Nproj0, os, cor_off, cubic;
   FFTPlan plan;               // length Nrho
   int F;
   float fsc;
-  int mono;                   // every row's first rho tap strictly monotone in x, spanning fewer than
-                              // 2 Nrho bins: the transposed interpolation runs as two passes per tap
-                              // (taps below and from rbase + Nrho) without conflicts; else one thread
-                              // per row adds in order
+  int mono;                   // every row's first rho tap strictly monotone in x, spanning at most
+                              // 2 (Nrho - ntap) + 1 bins: the transposed interpolation runs as two
+                              // windows per residue class of x modulo ntap (taps below and from
+                              // rbase + Nrho - ntap + 1) without conflicts; else one thread per row
+                              // adds in order
 };
 
 struct FwdTColSumArgs {       // row spectra -> spectrum columns (transposed theta taps, part 2)
-  const float2* rowspec;      // [S][nrows][Nk]
+  const float2* rowspec;      // [S][nrows][rowspec_stride(Nk)]
   float2* spec;               // [S] spectra, tiled layout; columns [lo, hi] written
   const int* thc;             // [Nproj] theta coordinate per internal row (fixed point)
   const int* rows;            // rows of the span, sorted
@@ -178,25 +194,29 @@ struct FwdTColSumArgs {       // row spectra -> spectrum columns (transposed the
 };
 
 // the exact transpose's real log-polar values are stored slice-interleaved in groups
-// of kGatherSlices slices, [S / kGatherSlices][W][Nrho][kGatherSlices], so the gather
-// reads a point's values for all slices of a group in two 16-byte loads
+// of kGatherSlices slices and in the order of the cell-sorted point list the gather
+// walks, [S / kGatherSlices][npts][kGatherSlices]: a point's values for all slices of
+// a group are two 16-byte loads, and the points of consecutive cells are consecutive
 constexpr int kGatherSlices = 8;
 
 struct FwdTColsArgs {         // spectrum columns -> real log-polar columns x e^rho
   const float2* spec;         // [S][Nk][Nth]
-  float* G;                   // [S / kGatherSlices][dhi - dlo + 1][Nrho][kGatherSlices]
+  float* G;                   // [S / kGatherSlices][npts][kGatherSlices]
+  const int* pos;             // [dhi - dlo + 1][Nrho] of this span: the point's index in the cell-sorted
+                              // list, -1 for no point
+  size_t npts;
   const float* erho;          // [Nrho]
   int Nth, Nrho, Nk, dlo, dhi;
   FFTPlan plan;
 };
 
 struct FwdTGatherArgs {       // transposed Cartesian interpolation as a per-pixel gather, all spans
-  const float* G;             // [3][groups][W][Nrho][kGatherSlices] the spans' values (FwdTColsArgs)
-  size_t span_stride;         // floats from one span's values to the next
+  const float* G;             // [groups][npts][kGatherSlices] the points' values (FwdTColsArgs)
+  size_t npts;
   float* acc;                 // [S][N][N], written
   const int* cell_off;        // [N*N + 1] CSR over image cells (floor of the point's coordinates)
-  const int4* pts;            // per cell: (x, y fixed point, (theta - dlo) * Nrho + rho, span), in (span, theta, rho) order
-  int N, W, Nrho, cubic;
+  const int2* pts;            // per cell: (x, y) fixed point, in (span, theta, rho) order within a cell
+  int N, cubic;
   int F;
   float fsc;
 };
@@ -222,6 +242,8 @@ struct CropArgs {
 cudaError_t launch_fwdT_rows(const FwdTRowsArgs& a, int S, cudaStream_t st);
 cudaError_t launch_fwdT_colsum(const FwdTColSumArgs& a, int S, int nblk, cudaStream_t st);
 cudaError_t launch_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st);
+cudaError_t launch_fwdT_tapw(int2* cent, int n, const int* rows, const int* thc, int F, float fsc, int cubic,
+                             cudaStream_t st);
 cudaError_t launch_fwdT_gather(const FwdTGatherArgs& a, int S, cudaStream_t st);
 cudaError_t launch_prefilter_T_cols(const PrefilterTColsArgs& a, int S, cudaStream_t st);
 cudaError_t launch_prefilter_T_rows_crop(const PrefilterTRowsCropArgs& a, int S, cudaStream_t st);

@@ -126,7 +126,7 @@ struct TC {
 
 // per rho frequency: FFT along theta, multiply by the kernel (which carries the
 // 1/(Nrho*Ntheta) of the two unnormalised transforms), inverse; NSIG rows per block
-template <int L, int BLK>
+template <int L, int BLK, bool GATHER = false>
 __global__ void __launch_bounds__(TC<L, BLK>::BLOCK, TC<L, BLK>::MINB) k_theta_conv_p2(ThetaConvArgs a) {
   extern __shared__ float2 sm2[];
   using C = TC<L, BLK>;
@@ -139,10 +139,57 @@ __global__ void __launch_bounds__(TC<L, BLK>::BLOCK, TC<L, BLK>::MINB) k_theta_c
   const bool live = k < a.Nk;
   float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, L);
   float2 v[16];
+  if constexpr (GATHER) {
+    // the block's NSIG frequencies of every row of the span are staged in shared memory
+    // after the signals' buffers ([nrows][NSIG]); each column's sum goes through the
+    // signal's own buffer slots, so no input register is live across the gather loops
+    float2* stg = sm2 + C::NSIG * C::SLOTS;
+    const int k0 = blockIdx.y * C::NSIG;
+    const float2* rs = a.rowspec + (size_t)s * a.nrows * rowspec_stride(a.Nk);
+    for (int q = threadIdx.x; q < a.nrows * C::NSIG; q += C::BLOCK) {
+      const int i = q / C::NSIG, kk = k0 + q % C::NSIG;
+      stg[q] = kk < a.Nk ? __ldg(rs + (size_t)i * rowspec_stride(a.Nk) + kk) : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    // four columns' lists walked side by side (independent load chains)
+#pragma unroll 1
+    for (int i0 = 0; i0 < 16; i0 += 4) {
+      int e[4], e1[4], m = 0;
+      float2 acc[4];
 #pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    const int c = t + i * T;
-    v[i] = (live && c >= a.in_lo && c <= a.in_hi) ? sp[sidx(k, c, L)] : make_float2(0.f, 0.f);
+      for (int u = 0; u < 4; ++u) {
+        const int c = t + (i0 + u) * T;
+        const bool in = c >= a.in_lo && c <= a.in_hi;
+        e[u] = in ? __ldg(a.coff + c) : 0;
+        e1[u] = in ? __ldg(a.coff + c + 1) : 0;
+        m = max(m, e1[u] - e[u]);
+        acc[u] = make_float2(0.f, 0.f);
+      }
+      for (int step = 0; step < m; ++step) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (e[u] < e1[u]) {
+            const int2 q = __ldg(a.cent + e[u]);
+            const float w = __int_as_float(q.y);
+            const float2 z = stg[q.x * C::NSIG + sig];
+            acc[u].x = fmaf(w, z.x, acc[u].x);
+            acc[u].y = fmaf(w, z.y, acc[u].y);
+            ++e[u];
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) sm[spad(t + (i0 + u) * T)] = acc[u];
+    }
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = sm[spad(t + i * T)];
+    __syncthreads();  // the transform's first stage writes other threads' slots
+  } else {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int c = t + i * T;
+      v[i] = (live && c >= a.in_lo && c <= a.in_hi) ? sp[sidx(k, c, L)] : make_float2(0.f, 0.f);
+    }
   }
   // the forward transform leaves X[t + i*T] in v[i]: the kernel multiply needs no
   // shared-memory round trip
@@ -565,12 +612,12 @@ __global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(4)) k_fwdT_rows_p2
   __syncthreads();
   any_fft<L, -1>(v, sm, t);
   if (!live) return;
-  float2* o0 = a.rowspec + ((size_t)s * a.nrows + i0) * a.Nk;
+  float2* o0 = a.rowspec + ((size_t)s * a.nrows + i0) * rowspec_stride(a.Nk);
   for (int k = t; k < a.Nk; k += T) {
     float2 va, vb;
     split_rows_T(sm[spad(k)], sm[spad(k == 0 ? 0 : L - k)], k, L, &va, &vb);
     o0[k] = va;
-    if (r1 >= 0) o0[a.Nk + k] = vb;
+    if (r1 >= 0) o0[rowspec_stride(a.Nk) + k] = vb;
   }
 }
 
@@ -611,13 +658,18 @@ __global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(4)) k_fwdT_cols_p2
   __syncthreads();
   any_fft<L, 1>(v, sm, t);
   if (!live) return;
-  const int W = a.dhi - a.dlo + 1;
-  float* g0 = a.G + (((size_t)(s / kGatherSlices) * W + (th0 - a.dlo)) * L) * kGatherSlices + s % kGatherSlices;
+  // each point's value to its place in the cell-sorted list
+  float* g0 = a.G + (size_t)(s / kGatherSlices) * a.npts * kGatherSlices + s % kGatherSlices;
+  const int* pos = a.pos + (size_t)(th0 - a.dlo) * L;
   for (int r = t; r < L; r += T) {
     const float2 z = sm[spad(r)];
     const float e = __ldg(a.erho + r);
-    g0[(size_t)r * kGatherSlices] = e * z.x;
-    if (th1 >= 0) g0[(size_t)(L + r) * kGatherSlices] = e * z.y;
+    const int p0 = __ldg(pos + r);
+    if (p0 >= 0) g0[(size_t)p0 * kGatherSlices] = e * z.x;
+    if (th1 >= 0) {
+      const int p1 = __ldg(pos + L + r);
+      if (p1 >= 0) g0[(size_t)p1 * kGatherSlices] = e * z.y;
+    }
   }
 }
 
@@ -645,6 +697,7 @@ void set_len_attrs(int optin) {
   cudaFuncSetAttribute(k_fwd_c2lp_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_theta_conv_p2<L, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_theta_conv_p2<L, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  cudaFuncSetAttribute(k_theta_conv_p2<L, 256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   if constexpr (L <= 4096) cudaFuncSetAttribute(k_theta_conv2_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_fwd_lp2polar_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   if constexpr (L >= 1024) cudaFuncSetAttribute(k_adj_ingest_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -675,6 +728,17 @@ bool run_fwd_c2lp(const FwdC2LPArgs& a, int S, cudaStream_t st, cudaError_t* err
   });
 }
 
+// shared memory of the exact transpose's theta convolution (0: not a length of the list)
+template <class LS>
+size_t theta_gather_smem(int L, int nrows) {
+  size_t r = 0;
+  with_length(L, LS(), [&](auto len) {
+    using C = TC<decltype(len)::value, 256>;
+    r = ((size_t)C::NSIG * C::SLOTS + (size_t)nrows * C::NSIG) * sizeof(float2);
+  });
+  return r;
+}
+
 template <class LS>
 bool run_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st, cudaError_t* err) {
   return with_length(a.Nth, LS(), [&](auto len) {
@@ -683,7 +747,15 @@ bool run_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st, cudaError_t*
     // thread (measured at N = 528: 1.00 against 1.21 ms with two rows per thread; at
     // N = 2016 two rows per thread are faster, 1.29x against 1.40x the power-of-two
     // rate per pixel)
-    if (a.block == 512 || LL > 4096 || (!P2<LL>::POW2 && pow2_part(LL / 16) == 1)) {
+    if (a.rowspec) {
+      // exact transpose: the input gathered from the row spectra (one row per thread)
+      using C = TC<LL, 256>;
+      const size_t sm = ((size_t)C::NSIG * C::SLOTS + (size_t)a.nrows * C::NSIG) * sizeof(float2);
+      if (!smem_fits(sm)) { *err = cudaErrorInvalidConfiguration; return; }
+      dim3 grid(S, (a.Nk + C::NSIG - 1) / C::NSIG);
+      k_theta_conv_p2<LL, 256, true><<<grid, C::BLOCK, sm, st>>>(a);
+      *err = cudaGetLastError();
+    } else if (a.block == 512 || LL > 4096 || (!P2<LL>::POW2 && pow2_part(LL / 16) == 1)) {
       auto go = [&](auto blk) {
         constexpr int B = decltype(blk)::value;
         using C = TC<LL, B>;
@@ -802,7 +874,9 @@ bool run_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st, cudaError_t* e
   bool PFX##_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st, cudaError_t* err); \
   bool PFX##_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st, cudaError_t* err);    \
   bool PFX##_fwdT_rows(const FwdTRowsArgs& a, int S, cudaStream_t st, cudaError_t* err);      \
-  bool PFX##_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st, cudaError_t* err);
+  bool PFX##_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st, cudaError_t* err);      \
+  bool PFX##_has_length(int L);                                                               \
+  size_t PFX##_gather_smem(int L, int nrows);
 
 #define LP_DEFINE_LENGTH_SET(PFX, LIST)                                                           \
   cudaError_t PFX##_configure(int optin) { return set_attrs(LIST(), optin); }                    \
@@ -829,7 +903,9 @@ bool run_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st, cudaError_t* e
   }                                                                                              \
   bool PFX##_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st, cudaError_t* err) {        \
     return run_fwdT_cols<LIST>(a, S, st, err);                                                  \
-  }
+  }                                                                                              \
+  bool PFX##_has_length(int L) { return with_length(L, LIST(), [](auto) {}); }                  \
+  size_t PFX##_gather_smem(int L, int nrows) { return theta_gather_smem<LIST>(L, nrows); }
 
 LP_DECLARE_LENGTH_SET(p2)
 LP_DECLARE_LENGTH_SET(mr)
