@@ -134,8 +134,14 @@ struct FwdDev {
   // the Nth columns): the theta convolution gathers its input from the row spectra
   DevBuf<int> coff[3];
   DevBuf<int2> cent[3];
+  // small handles run the three spans on their own streams: the row spectra then hold
+  // one region per span and spans 1 and 2 take their spectra from tspec
+  bool tspread = false;
+  DevBuf<float2> tspec;
 };
 static const int kTransposeCW = 8;
+// extra device memory the exact transpose may take to run its spans concurrently
+static const size_t kTransposeSpreadBytes = (size_t)1 << 30;
 
 struct AdjDev {
   int F = 16;              // fixed-point fraction bits of every coordinate table below
@@ -228,6 +234,7 @@ static void free_fwd(FwdDev* f) {
     f->coff[k].free_();
     f->cent[k].free_();
   }
+  f->tspec.free_();
   f->rbase.free_();
   f->cell_off.free_();
   f->cell_pts.free_();
@@ -1031,6 +1038,8 @@ int lp_debug_fill_scratch(lp_handle* h, float value, void* stream) {
   if (e == cudaSuccess && h->fwd && h->fwd->lpg.p) e = fill_async(h->fwd->lpg.p, h->fwd->lpg.n, value, st);
   if (e == cudaSuccess && h->fwd && h->fwd->rowspec.p)
     e = fill_async((float*)h->fwd->rowspec.p, 2 * h->fwd->rowspec.n, value, st);
+  if (e == cudaSuccess && h->fwd && h->fwd->tspec.p)
+    e = fill_async((float*)h->fwd->tspec.p, 2 * h->fwd->tspec.n, value, st);
   if (e == cudaSuccess && h->adj) {
     e = fill_async(h->adj->rbuf.p, h->adj->rbuf.n, value, st);
     if (e == cudaSuccess && h->adj->rin.p) e = fill_async(h->adj->rin.p, h->adj->rin.n, value, st);
@@ -1237,7 +1246,11 @@ static int build_transpose_tables(lp_handle* h) {
     CUDA_TRY(dev_alloc(F->lpg, groups * kGatherSlices * std::max<size_t>(npts, 1)));
   }
   const int nr = std::max(F->nrows[0], std::max(F->nrows[1], F->nrows[2]));
-  CUDA_TRY(dev_alloc(F->rowspec, (size_t)h->Nslices * std::max(nr, 1) * rowspec_stride(h->Nk)));
+  const size_t rs_slots = (size_t)h->Nslices * std::max(nr, 1) * rowspec_stride(h->Nk);
+  const size_t spec_slots = (size_t)h->Nslices * spec_slice(h->Nk, h->Nth);
+  F->tspread = (2 * rs_slots + 2 * spec_slots) * sizeof(float2) <= kTransposeSpreadBytes;
+  CUDA_TRY(dev_alloc(F->rowspec, (F->tspread ? 3 : 1) * rs_slots));
+  if (F->tspread) CUDA_TRY(dev_alloc(F->tspec, 2 * spec_slots));
   // the theta columns' (row, tap) lists: a row's taps reach columns first_tap + j (mod
   // Nth); entries of a column in ascending row order; the weights come from the same
   // device function as the forward's theta interpolation (k_fwdT_tapw)
@@ -1291,30 +1304,37 @@ int lp_fwd_transpose(lp_handle* h, float* f, const float* R, int S0, void* strea
   if (W <= 0) CUDA_TRY(cudaMemsetAsync(acc, 0, (size_t)S0 * h->N * h->N * sizeof(float), st));
   // register-FFT theta lengths gather the theta convolution's input from the row
   // spectra; the generic FFT sums them into the spectrum first (k_fwdT_colsum)
-  const bool gathered =
-      theta_conv_gathers(h->Nth, std::max(F->nrows[0], std::max(F->nrows[1], F->nrows[2])));
+  const int nr = std::max(F->nrows[0], std::max(F->nrows[1], F->nrows[2]));
+  const bool gathered = theta_conv_gathers(h->Nth, nr);
+  // spans on their own streams for calls of at most kSpreadSamples image samples
+  const bool spread = F->tspread && (double)S0 * h->N * h->N <= kSpreadSamples;
+  if (spread && W > 0) CUDA_TRY(span_fork(h, st));
   for (int k = 0; k < 3 && W > 0; ++k) {
-    FwdTRowsArgs a0{R, F->rowspec.p, F->rhoc.p, F->rows[k].p, F->rbase.p, F->nrows[k], h->N, h->N0, h->Nrho,
+    const cudaStream_t sk = spread && k > 0 ? h->span_st[k - 1] : st;
+    float2* rsk = F->rowspec.p + (spread ? (size_t)k * h->Nslices * std::max(nr, 1) * rowspec_stride(h->Nk) : 0);
+    float2* spk = spread && k > 0 ? F->tspec.p + (size_t)(k - 1) * h->Nslices * spec_slice(h->Nk, h->Nth) : h->spec.p;
+    FwdTRowsArgs a0{R, rsk, F->rhoc.p, F->rows[k].p, F->rbase.p, F->nrows[k], h->N, h->N0, h->Nrho,
                     h->Nk, h->Nproj0, h->os, h->N / 2 - h->cor, h->cubic, h->plan_rho, F->F, F->fsc, F->rho_mono};
-    CUDA_TRY(launch(h, K_FWDT_ROWS, st, [&] { return launch_fwdT_rows(a0, S0, st); }));
+    CUDA_TRY(launch(h, K_FWDT_ROWS, sk, [&] { return launch_fwdT_rows(a0, S0, sk); }));
     if (!gathered) {
-      FwdTColSumArgs a1{F->rowspec.p, h->spec.p, F->thc.p, F->rows[k].p, F->blk[k].p, F->nrows[k], h->Nth, h->Nk,
+      FwdTColSumArgs a1{rsk, spk, F->thc.p, F->rows[k].p, F->blk[k].p, F->nrows[k], h->Nth, h->Nk,
                         F->lo, F->hi, kTransposeCW, h->cubic, F->F, F->fsc};
-      CUDA_TRY(launch(h, K_FWDT_COLSUM, st, [&] { return launch_fwdT_colsum(a1, S0, F->nblk[k], st); }));
+      CUDA_TRY(launch(h, K_FWDT_COLSUM, sk, [&] { return launch_fwdT_colsum(a1, S0, F->nblk[k], sk); }));
     }
-    ThetaConvArgs a2{h->spec.p, F->fz.p, h->Nth, h->Nk, F->lo, F->hi,
+    ThetaConvArgs a2{spk, F->fz.p, h->Nth, h->Nk, F->lo, F->hi,
                      F->dlo, F->dhi, 1, h->plan_th, h->fwd_tblock};
     if (gathered) {
-      a2.rowspec = F->rowspec.p;
+      a2.rowspec = rsk;
       a2.coff = F->coff[k].p;
       a2.cent = F->cent[k].p;
       a2.nrows = F->nrows[k];
     }
-    CUDA_TRY(launch(h, K_THETA_CONV, st, [&] { return launch_theta_conv(a2, S0, st); }));
-    FwdTColsArgs a3{h->spec.p, F->lpg.p, F->lppos[k].p, F->npts, h->erho.p, h->Nth, h->Nrho, h->Nk, F->dlo, F->dhi,
+    CUDA_TRY(launch(h, K_THETA_CONV, sk, [&] { return launch_theta_conv(a2, S0, sk); }));
+    FwdTColsArgs a3{spk, F->lpg.p, F->lppos[k].p, F->npts, h->erho.p, h->Nth, h->Nrho, h->Nk, F->dlo, F->dhi,
                     h->plan_rho};
-    CUDA_TRY(launch(h, K_FWDT_COLS, st, [&] { return launch_fwdT_cols(a3, S0, st); }));
+    CUDA_TRY(launch(h, K_FWDT_COLS, sk, [&] { return launch_fwdT_cols(a3, S0, sk); }));
   }
+  if (spread && W > 0) CUDA_TRY(span_join(h, st));
   if (W > 0) {
     FwdTGatherArgs a4{F->lpg.p, F->npts, acc, F->cell_off.p, F->cell_pts.p, h->N, h->cubic, F->F, F->fsc};
     CUDA_TRY(launch(h, K_FWDT_GATHER, st, [&] { return launch_fwdT_gather(a4, S0, st); }));
