@@ -12,10 +12,12 @@ streams, theta-convolution block), and are concatenated into one batch,
 fewest slices first.  The groups run one after another inside the graph,
 smallest geometry first (shortest work first: running them on parallel graph
 branches was measured slower, the large groups already fill the GPU and the
-branches only compete for L2).  Within a group the requests run in waves of
-consecutive requests of up to about 32 slices' worth of N=2048 work
-(wave_slices), so a request completes with its wave instead of with its whole
-group; the graph records an event after each wave, which gives per-request
+branches only compete for L2).  A group runs as one batch, except that the last
+group's largest request runs alone after the others (last_alone), so every other
+request completes before the launch does; wave_slices bounds a group's batches to
+about that many slices' worth of N=2048 work, so requests complete with their wave
+rather than with their whole group (lower latency for large requests, at some
+throughput).  The graph records an event after each wave, which gives per-request
 latencies measured from the start of the launch.
 """
 import time
@@ -59,11 +61,12 @@ def group_requests(requests):
     return groups, where
 
 
-def plan_waves(requests, idx, N, wave_slices=32):
+def plan_waves(requests, idx, N, wave_slices=None, last_alone=False):
     """Consecutive runs of a group's requests (in batch order) whose slices add up to
-    at most wave_slices * (2048 / N)^2 (one request at least): [(first slice, end
-    slice, request indices)]."""
-    cap = max(1, int(wave_slices * (2048.0 / N) ** 2))
+    at most wave_slices * (2048 / N)^2 (one request at least; None: no bound):
+    [(first slice, end slice, request indices)].  With last_alone, the group's last
+    request gets a wave of its own (the others then complete before it)."""
+    cap = float("inf") if wave_slices is None else max(1, int(wave_slices * (2048.0 / N) ** 2))
     waves, cur, a, b = [], [], 0, 0
     for i in idx:
         S = requests[i][2]
@@ -74,22 +77,26 @@ def plan_waves(requests, idx, N, wave_slices=32):
         b += S
     if cur:
         waves.append((a, b, cur))
+    if last_alone and len(waves[-1][2]) > 1:
+        a, b, reqs = waves.pop()
+        S = requests[reqs[-1]][2]
+        waves += [(a, b - S, reqs[:-1]), (b - S, b, reqs[-1:])]
     return waves
 
 
 class UnevenBatch:
     def __init__(self, requests, filter_type="ramp", interp_type="cubic", gpu=0, precision="reference",
-                 wave_slices=32, autotune=True):
+                 wave_slices=None, autotune=True, last_alone=True):
         self.gpu = gpu
         self.dev = torch.device("cuda", gpu)
         self.requests = [tuple(int(v) for v in r) for r in requests]
         plan, self.where = group_requests(self.requests)
         self.groups = []
-        for N, Nproj, total, idx in plan:
+        for gi, (N, Nproj, total, idx) in enumerate(plan):
             lp = lpTransform(N, Nproj, total, filter_type, N / 2, interp_type, precision)
             lp.precompute(1)
             lp.initcmem(1, gpu)
-            waves = plan_waves(self.requests, idx, N, wave_slices)
+            waves = plan_waves(self.requests, idx, N, wave_slices, last_alone and gi == len(plan) - 1)
             if autotune:
                 lp.autotune(gpu, max(b - a for a, b, _ in waves))
             g = dict(lp=lp, N=N, Nproj=Nproj, S=total, idx=idx, waves=waves,

@@ -216,7 +216,8 @@ def test_host_pipeline_rejects_bad_arrays():
 def test_uneven_request_grouping():
     """Requests of the same geometry share one handle and one graph segment, smallest
     geometry first, fewest slices first within a geometry; each request keeps its slice
-    range in its group; waves pack consecutive requests up to the slice budget."""
+    range in its group; waves pack consecutive requests up to the slice budget, and the
+    last request can be split off into a wave of its own."""
     pytest.importorskip("torch")
     from lprec_gb300.batch import group_requests, plan_waves
     reqs = [(512, 768, 2), (256, 384, 3), (512, 768, 1), (256, 384, 4), (1024, 96, 1)]
@@ -231,6 +232,11 @@ def test_uneven_request_grouping():
     waves = plan_waves(big, idx, 2048, 32)
     assert waves == [(0, 17, [4, 0, 2]), (17, 37, [1]), (37, 77, [3])]
     assert plan_waves(big, idx, 1024, 32) == [(0, 77, [4, 0, 2, 1, 3])]
+    # no bound: one wave; the last request alone at the end on request
+    assert plan_waves(big, idx, 2048) == [(0, 77, [4, 0, 2, 1, 3])]
+    assert plan_waves(big, idx, 2048, None, True) == [(0, 37, [4, 0, 2, 1]), (37, 77, [3])]
+    assert plan_waves(big, idx, 2048, 32, True) == waves  # its last wave is one request already
+    assert plan_waves(big[:1], [0], 2048, None, True) == [(0, 5, [0])]
 
 
 @pytest.mark.parametrize("precision", ["fp64", "reference"])
