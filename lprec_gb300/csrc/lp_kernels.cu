@@ -950,7 +950,8 @@ __global__ void __launch_bounds__(256) k_fwdT_gather(FwdTGatherArgs a, int S) {
     axis_weights_fx(p.y, a.F, a.fsc, a.cubic, wy);
     const float w = pick_w(wy, j) * pick_w(wx, i);
     const float4* g = reinterpret_cast<const float4*>(G + (size_t)e * kGatherSlices);
-    const float4 u = __ldg(g), v = __ldg(g + 1);
+    const float4 u = __ldg(g);
+    const float4 v = ns > 4 ? __ldg(g + 1) : make_float4(0.f, 0.f, 0.f, 0.f);  // block-uniform
     acc[0] += w * u.x;
     acc[1] += w * u.y;
     acc[2] += w * u.z;

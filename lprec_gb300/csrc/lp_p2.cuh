@@ -621,18 +621,56 @@ __global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(4)) k_fwdT_rows_p2
   }
 }
 
-// exact transpose, column stage (k_fwdT_cols) on the register FFT
+// exact transpose, column stage (k_fwdT_cols) on the register FFT.  The block's
+// NSIG signals (up to 1024 threads) are SL consecutive slices (a power of two
+// dividing kGatherSlices) of PAIRS column pairs, so each point's values of the SL
+// slices go out as one vector store into the slice-interleaved point list instead
+// of SL scattered 4-byte stores.
 template <int L>
-__global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(4)) k_fwdT_cols_p2(FwdTColsArgs a) {
+struct TCols {
+  static constexpr int T = L / 16;
+  // powers of two: up to kGatherSlices slices in blocks of up to 1024 threads at 64
+  // registers; mixed lengths (whose odd stages hold more values) keep the other
+  // kernels' blocks, SL the largest power of two dividing their signal count
+  static constexpr int FIT = 1024 / T > kGatherSlices ? kGatherSlices : 1024 / T;
+  static constexpr int NS0 = P2<L>::NSIG;
+  static constexpr int SL = P2<L>::POW2 ? (FIT >= 8 ? 8 : FIT >= 4 ? 4 : FIT >= 2 ? 2 : 1)
+                          : (NS0 % 8 == 0 ? 8 : NS0 % 4 == 0 ? 4 : NS0 % 2 == 0 ? 2 : 1);
+  static constexpr int NSIG = P2<L>::POW2 ? SL : NS0;
+  static constexpr int PAIRS = NSIG / SL;
+  static constexpr int BLOCK = NSIG * T;
+  static constexpr int MINB = P2<L>::POW2 ? (1024 / BLOCK > 0 ? 1024 / BLOCK : 1) : P2<L>::blocks(4);
+};
+
+template <int N>
+__device__ __forceinline__ void store_vec(float* p, const float* v) {
+  if constexpr (N == 8) {
+    reinterpret_cast<float4*>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
+    reinterpret_cast<float4*>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
+  } else if constexpr (N == 4) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  } else if constexpr (N == 2) {
+    *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+  } else {
+    *p = v[0];
+  }
+}
+
+template <int L>
+__global__ void __launch_bounds__(TCols<L>::BLOCK, TCols<L>::MINB)
+    k_fwdT_cols_p2(FwdTColsArgs a, int S) {
   extern __shared__ float2 sm2[];
-  constexpr int T = P2<L>::T;
+  using C = TCols<L>;
+  constexpr int T = P2<L>::T, SL = C::SL;
   const int sig = threadIdx.x / T, t = threadIdx.x % T;
   float2* sm = sm2 + sig * P2<L>::SLOTS;
-  const int s = blockIdx.x;
-  const int th0 = a.dlo + 2 * (blockIdx.y * P2<L>::NSIG + sig);
-  const bool live = th0 <= a.dhi;
+  const int s0 = blockIdx.x * SL;  // the block's first slice (SL divides kGatherSlices)
+  const int s = s0 + sig % SL;
+  const int pr = blockIdx.y * C::PAIRS + sig / SL;
+  const int th0 = a.dlo + 2 * pr;
+  const bool live = th0 <= a.dhi && s < S;
   const int th1 = (live && th0 + 1 <= a.dhi) ? th0 + 1 : -1;
-  const float2* sp = a.spec + (size_t)s * spec_slice(a.Nk, a.Nth);
+  const float2* sp = a.spec + (size_t)(live ? s : 0) * spec_slice(a.Nk, a.Nth);
 #pragma unroll
   for (int m = 0; m <= L / 4 / T; ++m) {
     const int kk = 2 * (t + m * T);
@@ -657,19 +695,24 @@ __global__ void __launch_bounds__(P2<L>::BLOCK, P2<L>::blocks(4)) k_fwdT_cols_p2
   for (int i = 0; i < 16; ++i) v[i] = sm[spad(t + i * T)];
   __syncthreads();
   any_fft<L, 1>(v, sm, t);
-  if (!live) return;
-  // each point's value to its place in the cell-sorted list
-  float* g0 = a.G + (size_t)(s / kGatherSlices) * a.npts * kGatherSlices + s % kGatherSlices;
-  const int* pos = a.pos + (size_t)(th0 - a.dlo) * L;
-  for (int r = t; r < L; r += T) {
-    const float2 z = sm[spad(r)];
-    const float e = __ldg(a.erho + r);
-    const int p0 = __ldg(pos + r);
-    if (p0 >= 0) g0[(size_t)p0 * kGatherSlices] = e * z.x;
-    if (th1 >= 0) {
-      const int p1 = __ldg(pos + L + r);
-      if (p1 >= 0) g0[(size_t)p1 * kGatherSlices] = e * z.y;
+  __syncthreads();  // the stores below read every signal's buffer
+  // each point's values of the SL slices to its place in the cell-sorted list (slices
+  // past S write their slots too: padding of the group, never read)
+  float* g0 = a.G + (size_t)(s0 / kGatherSlices) * a.npts * kGatherSlices + s0 % kGatherSlices;
+  for (int q = threadIdx.x; q < C::PAIRS * 2 * L; q += C::BLOCK) {
+    const int p = q / (2 * L), c = (q / L) & 1, r = q % L;
+    const int th = a.dlo + 2 * (blockIdx.y * C::PAIRS + p) + c;
+    if (th > a.dhi) continue;
+    const int e = __ldg(a.pos + (size_t)(th - a.dlo) * L + r);
+    if (e < 0) continue;
+    const float er = __ldg(a.erho + r);
+    float vals[SL];
+#pragma unroll
+    for (int j = 0; j < SL; ++j) {
+      const float2 z = sm2[(p * SL + j) * P2<L>::SLOTS + spad(r)];
+      vals[j] = er * (c == 0 ? z.x : z.y);
     }
+    store_vec<SL>(g0 + (size_t)e * kGatherSlices, vals);
   }
 }
 
@@ -854,11 +897,12 @@ template <class LS>
 bool run_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st, cudaError_t* err) {
   return with_length(a.Nrho, LS(), [&](auto len) {
     constexpr int LL = decltype(len)::value;
+    using C = TCols<LL>;
     const int npairs = (a.dhi - a.dlo + 2) / 2;
-    const size_t sm = (size_t)P2<LL>::NSIG * P2<LL>::SLOTS * sizeof(float2);
+    const size_t sm = (size_t)C::NSIG * P2<LL>::SLOTS * sizeof(float2);
     if (!smem_fits(sm)) { *err = cudaErrorInvalidConfiguration; return; }
-    dim3 grid(S, (npairs + P2<LL>::NSIG - 1) / P2<LL>::NSIG);
-    k_fwdT_cols_p2<LL><<<grid, P2<LL>::BLOCK, sm, st>>>(a);
+    dim3 grid((S + C::SL - 1) / C::SL, (npairs + C::PAIRS - 1) / C::PAIRS);
+    k_fwdT_cols_p2<LL><<<grid, C::BLOCK, sm, st>>>(a, S);
     *err = cudaGetLastError();
   });
 }
