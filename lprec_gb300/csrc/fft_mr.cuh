@@ -18,7 +18,13 @@
 //
 // Odd butterflies fold the inputs into sums and differences of mirrored pairs
 // (x_i +- x_{R-i}) so an output pair costs (R-1)/2 real-by-complex products of
-// each kind; their roots cos/sin(2 pi m / R) are compile-time constants.
+// each kind; their roots cos/sin(2 pi m / R) are compile-time constants.  A
+// prime factor above 13 (N = 2064 = 16 * 3 * 43 for an axis 3 pixels off centre
+// at N0 = 2048) would hold 2R values per thread that way, so it runs output-
+// parallel instead (mr_big_stage): the folded sums and differences are formed in
+// the shared buffer, then each butterfly's output pairs are split between
+// threads that each read the R folded values once and accumulate their pairs
+// with compile-time roots.
 // Stage twiddles are built from two sincospif() calls per butterfly and short
 // products, as in fft_reg.cuh.  Same sign convention (DIR = -1 forward).
 #pragma once
@@ -40,19 +46,65 @@ __host__ __device__ constexpr int small_odd_factor(int n) {
   return n % 3 == 0 ? 3 : n % 5 == 0 ? 5 : n % 7 == 0 ? 7 : n % 11 == 0 ? 11 : n % 13 == 0 ? 13 : 0;
 }
 
-// L = 16 T with T's odd part a product of 3, 5, 7, 11, 13 and T not a power of two
+// smallest prime factor of odd n > 1
+__host__ __device__ constexpr int odd_prime_factor(int n) {
+  for (int f = 3; f * f <= n; f += 2)
+    if (n % f == 0) return f;
+  return n;
+}
+
+// the largest prime factor above 13 the output-parallel stage takes (instantiated and
+// checked against the oracle at 43; a thread holds about R float2 of accumulators)
+constexpr int kBigPrimeMax = 43;
+
+// L = 16 T with T not a power of two, T's odd part a product of primes up to
+// kBigPrimeMax, those above 13 each leaving at least one thread per butterfly
 __host__ __device__ constexpr bool mr_length(int L) {
   if (L < 32 || L % 16 != 0) return false;
   const int T = L / 16;
   int o = T / pow2_part(T);
   if (o == 1) return false;
   while (o > 1) {
-    const int f = small_odd_factor(o);
-    if (f == 0) return false;
+    const int f = odd_prime_factor(o);
+    if (f > kBigPrimeMax || (f > 13 && L / f > T)) return false;
     o /= f;
   }
   return true;
 }
+
+// cos and sin of 2 pi m / R in double precision, at compile time (Taylor series
+// after reducing the angle to [-pi, pi])
+__host__ __device__ constexpr double ct_sin_red(double x) {
+  double term = x, sum = x;
+  for (int n = 1; n < 30; ++n) {
+    term *= -x * x / ((2.0 * n) * (2.0 * n + 1.0));
+    sum += term;
+  }
+  return sum;
+}
+__host__ __device__ constexpr double ct_cos_red(double x) {
+  double term = 1.0, sum = 1.0;
+  for (int n = 1; n < 30; ++n) {
+    term *= -x * x / ((2.0 * n - 1.0) * (2.0 * n));
+    sum += term;
+  }
+  return sum;
+}
+__host__ __device__ constexpr double ct_angle(int m, int R) {
+  const double pi = 3.14159265358979323846264338327950288;
+  const int mm = ((m % R) + R) % R;
+  return 2.0 * pi * (2 * mm > R ? mm - R : mm) / R;
+}
+template <int R>
+struct PrimeRoots {
+  float c[R], s[R];
+  constexpr PrimeRoots() : c(), s() {
+    for (int m = 0; m < R; ++m) {
+      c[m] = (float)ct_cos_red(ct_angle(m, R));
+      s[m] = (float)ct_sin_red(ct_angle(m, R));
+    }
+  }
+};
 
 // cos(2 pi m / R), sin(2 pi m / R) for 1 <= m <= (R-1)/2 (m a compile-time constant at every use)
 template <int R>
@@ -183,12 +235,123 @@ __device__ __forceinline__ void mr_odd_stage(float2* sm, int t) {
   __syncthreads();
 }
 
+// output pairs q = Q0 .. Q1 of one folded butterfly (x_0 at p0, S_i at p0 + i stride,
+// D_i at p0 + (R - i) stride, i = 1 .. h, in the shared buffer) into out[]: with
+// Q0 = 0, out[0] = X_0 and X_q, X_{R-q} at out[2q - 1], out[2q]; otherwise X_q,
+// X_{R-q} at out[2 (q - Q0)], out[2 (q - Q0) + 1]
+template <int R, int DIR, int Q0, int Q1>
+__device__ __forceinline__ void big_prime_pairs(const float2* sm, int p0, int stride, float2* out) {
+  constexpr int h = (R - 1) / 2;
+  constexpr int NQ = Q1 - Q0 + 1;
+  constexpr PrimeRoots<R> rt{};
+  float2 A[NQ], B[NQ];
+#pragma unroll
+  for (int u = 0; u < NQ; ++u) A[u] = B[u] = make_float2(0.f, 0.f);
+  const float2 x0 = sm[spad(p0)];
+#pragma unroll
+  for (int i = 1; i <= h; ++i) {
+    const float2 S = sm[spad(p0 + i * stride)], D = sm[spad(p0 + (R - i) * stride)];
+#pragma unroll
+    for (int u = 0; u < NQ; ++u) {
+      const int q = Q0 + u;
+      if (q == 0) {
+        A[u] = cadd(A[u], S);
+      } else {
+        const int m = (i * q) % R;
+        const float c = rt.c[m], sn = rt.s[m];
+        A[u].x = fmaf(S.x, c, A[u].x);
+        A[u].y = fmaf(S.y, c, A[u].y);
+        B[u].x = fmaf(D.x, sn, B[u].x);
+        B[u].y = fmaf(D.y, sn, B[u].y);
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < NQ; ++u) {
+    const int q = Q0 + u;
+    const float2 m0 = cadd(x0, A[u]);
+    if (q == 0) {
+      out[0] = m0;
+    } else {
+      const float2 iB = make_float2(-DIR * B[u].y, DIR * B[u].x);  // DIR * i * B
+      const int o = Q0 == 0 ? 2 * q - 1 : 2 * (q - Q0);
+      out[o] = cadd(m0, iB);
+      out[o + 1] = csub(m0, iB);
+    }
+  }
+}
+
+// One stage of a prime radix R > 13 through the shared buffer, output-parallel (see
+// the file comment).  Phase 1: (butterfly, i) items twiddle x_i and x_{R-i} and
+// store S_i = x_i + x_{R-i} at i and D_i = x_i - x_{R-i} at R - i.  Phase 2: PB
+// threads per butterfly (consecutive lanes take consecutive butterflies) each form
+// their share of the output pairs in registers.  Phase 3: the outputs go to their
+// sorted positions.  NS is the product of the radices already applied.  Ends with
+// a barrier.
+template <int L, int DIR, int R, int NS>
+__device__ __forceinline__ void mr_big_stage(float2* sm, int t) {
+  constexpr int T = L / 16;
+  constexpr int NBUT = L / R;
+  static_assert(NBUT <= T, "one thread per butterfly at least");
+  constexpr int h = (R - 1) / 2;
+  constexpr int PB = T / NBUT >= 2 ? 2 : 1;  // threads per butterfly
+  constexpr int QA = PB == 2 ? h / 2 : h;    // thread 0 of a butterfly: q = 0 .. QA; thread 1: QA + 1 .. h
+  // phase 1: twiddle and fold
+  for (int it = t; it < NBUT * h; it += T) {
+    const int jp = it % NBUT, i = 1 + it / NBUT;
+    float2 a = sm[spad(jp + i * NBUT)], b = sm[spad(jp + (R - i) * NBUT)];
+    if constexpr (NS > 1) {
+      const int k = jp % NS;
+      float sa, ca, sb, cb;
+      sincospif(2.0f * (float)((i * k) % (NS * R)) * (1.0f / (float)(NS * R)), &sa, &ca);
+      sincospif(2.0f * (float)(((R - i) * k) % (NS * R)) * (1.0f / (float)(NS * R)), &sb, &cb);
+      a = cmul(a, make_float2(ca, DIR * sa));
+      b = cmul(b, make_float2(cb, DIR * sb));
+    }
+    sm[spad(jp + i * NBUT)] = cadd(a, b);
+    sm[spad(jp + (R - i) * NBUT)] = csub(a, b);
+  }
+  __syncthreads();
+  // phase 2: output pairs in registers
+  constexpr int NOUT0 = 1 + 2 * QA, NOUT1 = 2 * (h - QA);
+  constexpr int NOUT = NOUT0 > NOUT1 ? NOUT0 : NOUT1;
+  float2 out[NOUT];
+  const int jp = t % NBUT, part = t / NBUT;
+  const bool act = t < PB * NBUT;
+  if (act) {
+    if (part == 0) big_prime_pairs<R, DIR, 0, QA>(sm, jp, NBUT, out);
+    else if constexpr (PB == 2) big_prime_pairs<R, DIR, QA + 1, h>(sm, jp, NBUT, out);
+  }
+  __syncthreads();
+  // phase 3: sorted positions
+  if (act) {
+    const int k = jp % NS;
+    const int base = (jp - k) * R + k;
+    if (part == 0) {
+      sm[spad(base)] = out[0];
+#pragma unroll
+      for (int q = 1; q <= QA; ++q) {
+        sm[spad(base + q * NS)] = out[2 * q - 1];
+        sm[spad(base + (R - q) * NS)] = out[2 * q];
+      }
+    } else if constexpr (PB == 2) {
+#pragma unroll
+      for (int q = QA + 1; q <= h; ++q) {
+        sm[spad(base + q * NS)] = out[2 * (q - QA - 1)];
+        sm[spad(base + (R - q) * NS)] = out[2 * (q - QA - 1) + 1];
+      }
+    }
+  }
+  __syncthreads();
+}
+
 // the odd part O of T, one prime stage at a time (NS: radices applied so far)
 template <int L, int DIR, int O, int NS>
 __device__ __forceinline__ void mr_odd_stages(float2* sm, int t) {
   if constexpr (O > 1) {
-    constexpr int R = small_odd_factor(O);
-    mr_odd_stage<L, DIR, R, NS>(sm, t);
+    constexpr int R = odd_prime_factor(O);
+    if constexpr (R <= 13) mr_odd_stage<L, DIR, R, NS>(sm, t);
+    else mr_big_stage<L, DIR, R, NS>(sm, t);
     mr_odd_stages<L, DIR, O / R, NS * R>(sm, t);
   }
 }

@@ -953,5 +953,6 @@ bool run_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st, cudaError_t* e
 
 LP_DECLARE_LENGTH_SET(p2)
 LP_DECLARE_LENGTH_SET(mr)
+LP_DECLARE_LENGTH_SET(mr2)
 
 }  // namespace lpgb

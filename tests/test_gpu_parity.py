@@ -368,11 +368,13 @@ def test_prime_radix_lengths(torch_cuda, args):
 
 
 @pytest.mark.parametrize("args", [(512, 768, 'cubic', 'shepp-logan', 253), (1008, 1512, 'linear', 'hann', 504),
-                                  (1536, 2304, 'cubic', 'ramp', 768), (2016, 3024, 'cubic', 'parzen', 1008)])
+                                  (1536, 2304, 'cubic', 'ramp', 768), (2016, 3024, 'cubic', 'parzen', 1008),
+                                  (2048, 1024, 'cubic', 'shepp-logan', 1021)])
 def test_mixed_radix_lengths(torch_cuda, args):
     """Padded sizes that are not powers of two, served by the mixed-radix register FFT:
-    N = 528 = 16*3*11 (an off-centre axis at N0 = 512), 1008 = 16*63, 1536 = 16*96 and
-    2016 = 16*126 (Nrho = 2N: 1056, 2016, 3072, 4032), one slice each against the oracle."""
+    N = 528 = 16*3*11 (an off-centre axis at N0 = 512), 1008 = 16*63, 1536 = 16*96,
+    2016 = 16*126 and 2064 = 16*3*43 (an axis 3 pixels off centre at N0 = 2048: the prime
+    43 takes the output-parallel stage), Nrho = 2N; one slice each against the oracle."""
     from lprec_gb300 import _lib
     N0, Nproj, interp, filt, cor = args
     packed = _lib.precompute(N0, Nproj, 1, cor, interp, filt, precision='fp64')
