@@ -557,6 +557,7 @@ def run_side_configs(torch, dev, reps=5):
     # of the same detector width
     geos = [("n512", 512, 768, 256, 64), ("n528_cor253", 512, 768, 253, 64),
             ("n2048", 2048, 3000, 1024, 16), ("n2064_cor1021", 2048, 3000, 1021, 16),
+            ("n2080_cor1012", 2048, 3000, 1012, 16),
             ("n2016_foam", 2016, 299, 1008, 16)]
     res = {}
     for name, N0, Np, cor, S in geos:
@@ -577,7 +578,8 @@ def run_side_configs(torch, dev, reps=5):
                      "slices_per_s": S / t * 1e3, "ns_per_padded_pixel": t * 1e6 / (S * h.N * h.N)}
         lp.close()
         del f, R, fo
-    for name, ref in (("n528_cor253", "n512"), ("n2064_cor1021", "n2048"), ("n2016_foam", "n2048")):
+    for name, ref in (("n528_cor253", "n512"), ("n2064_cor1021", "n2048"), ("n2080_cor1012", "n2048"),
+                      ("n2016_foam", "n2048")):
         res[name]["per_pixel_vs_pow2"] = res[name]["ns_per_padded_pixel"] / res[ref]["ns_per_padded_pixel"]
     out["padded_sizes"] = res
 

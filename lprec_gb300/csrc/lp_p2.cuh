@@ -954,5 +954,7 @@ bool run_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st, cudaError_t* e
 LP_DECLARE_LENGTH_SET(p2)
 LP_DECLARE_LENGTH_SET(mr)
 LP_DECLARE_LENGTH_SET(mr2)
+LP_DECLARE_LENGTH_SET(mr3)
+LP_DECLARE_LENGTH_SET(mr4)
 
 }  // namespace lpgb

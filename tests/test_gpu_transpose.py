@@ -176,11 +176,13 @@ def test_n4096_dot_product(torch_cuda):
 
 
 @pytest.mark.parametrize("args", [(512, 768, 256, 'cubic', 16), (96, 144, 45, 'cubic', 3), (128, 192, 64, 'linear', 2),
-                                  (64, 40, 32.5, 'cubic', 2), (512, 768, 253, 'cubic', 9)])
+                                  (64, 40, 32.5, 'cubic', 2), (512, 768, 253, 'cubic', 9), (512, 768, 243, 'cubic', 5),
+                                  (2048, 512, 1021, 'cubic', 2)])
 def test_transpose_bit_reproducible(torch_cuda, args):
     """The backward has no atomics: two calls on the same input give the same bits, also
     after the scratch buffers were poisoned in between (odd padded sizes, a non-integer
-    axis and a slice count that is not a multiple of the gather's slice group included)."""
+    axis, a slice count that is not a multiple of the gather's slice group, and the
+    register FFT's prime-17 and prime-43 stages at N = 544 and 2064 included)."""
     torch = torch_cuda
     N0, Nproj, cor, interp, S = args
     lp = _lp(N0, Nproj, S, cor, interp)
