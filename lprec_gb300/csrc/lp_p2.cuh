@@ -743,7 +743,7 @@ void set_len_attrs(int optin) {
   cudaFuncSetAttribute(k_theta_conv_p2<L, 256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   if constexpr (L <= 4096) cudaFuncSetAttribute(k_theta_conv2_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_fwd_lp2polar_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-  if constexpr (L >= 1024) cudaFuncSetAttribute(k_adj_ingest_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  if constexpr (L >= 512) cudaFuncSetAttribute(k_adj_ingest_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_adj_polar2lp_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_adj_lpcols_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   cudaFuncSetAttribute(k_fwdT_rows_p2<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
@@ -839,10 +839,10 @@ bool run_fwd_lp2polar(const FwdLP2PolarArgs& a, int S, cudaStream_t st, cudaErro
 template <class LS>
 bool run_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st, cudaError_t* err) {
   const int L = 2 * a.N;
-  if (L < 1024) return false;  // needs T = L/16 >= 64 threads per row pair
+  if (L < 512) return false;  // T = L/16 >= 32: a warp per row pair, 16 threads per line's prefilter
   return with_length(L, LS(), [&](auto len) {
     constexpr int LL = decltype(len)::value;
-    if constexpr (LL >= 1024) {
+    if constexpr (LL >= 512) {
       const size_t sm = (a.H ? (size_t)P2<LL>::SLOTS * sizeof(float2) : 0) +
                         4 * (size_t)line_floats(LL / 2, P2<LL>::T / 2) * sizeof(float);
       if (!smem_fits(sm)) { *err = cudaErrorInvalidConfiguration; return; }
