@@ -16,6 +16,7 @@ does not build with CUDA 13) on the host cores, one slice per process.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -770,8 +771,19 @@ def run_ours(args):
     top = max(prof.items(), key=lambda kv: kv[1][0])
     name, (tms, nl) = top
     per_launch_ms = tms / max(nl, 1)
-    per_launch_bytes = kb[name] if name != "theta_conv" else kb[name]
+    per_launch_bytes = kb[name]
     achieved = per_launch_bytes / (per_launch_ms / 1000.0) / 1e9
+    # the theta convolution is transform-bound, not byte-bound: its FP32 rate by the usual
+    # FFT count (5 L log2 L per transform, two per rho frequency, and the complex product)
+    # against the FP32 FMA peak at the sampled maximum SM clock (152 SMs x 128 lanes x 2)
+    fft = None
+    if name == "theta_conv":
+        Lt = h.Ntheta
+        gflop = S * (h.Nrho // 2 + 1) * (2 * 5 * Lt * math.log2(Lt) + 6 * Lt) / 1e9
+        clk_max = clk.summary().get("sm_max_mhz") or 2070.0
+        peak_tf = 152 * 128 * 2 * clk_max * 1e6 / 1e12
+        fft = {"gflop_per_launch": round(gflop, 2), "tflops": round(gflop / per_launch_ms, 2),
+               "fp32_peak_tflops": round(peak_tf, 1), "frac": round(gflop / per_launch_ms / peak_tf, 3)}
     kernels = {k: {"ms_total": round(v[0], 3), "launches": v[1],
                    "share": round(v[0] / max(sum(x[0] for x in prof.values()), 1e-9), 4)}
                for k, v in prof.items() if v[1]}
@@ -795,7 +807,8 @@ def run_ours(args):
                          "traffic": (NCU_DRAM_BYTES_PER_SLICE[name] * S
                                      if (N, Nproj) == (2048, 3000) and name in NCU_DRAM_BYTES_PER_SLICE else None),
                          "traffic_source": "ncu dram__bytes_read+write, 8-slice capture scaled to the launch's slices",
-                         "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms},
+                         "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms,
+                         "fp32": fft},
             "step_roofline": {"algorithmic_bytes_per_slice": ALGO_BYTES_PER_SLICE, "achieved": step_gbs,
                               "peak": peak, "frac": step_gbs / peak},
             "kernels": kernels,
