@@ -282,8 +282,8 @@ __device__ __forceinline__ void big_prime_pairs(const float2* sm, int p0, int st
 }
 
 // One stage of a prime radix R > 13 through the shared buffer, output-parallel (see
-// the file comment).  Phase 1: (butterfly, i) items twiddle x_i and x_{R-i} and
-// store S_i = x_i + x_{R-i} at i and D_i = x_i - x_{R-i} at R - i.  Phase 2: PB
+// the file comment).  Phase 1: the PB threads of a butterfly twiddle x_i and x_{R-i}
+// over runs of i and store S_i = x_i + x_{R-i} at i and D_i = x_i - x_{R-i} at R - i.  Phase 2: PB
 // threads per butterfly (consecutive lanes take consecutive butterflies) each form
 // their share of the output pairs in registers.  Phase 3: the outputs go to their
 // sorted positions.  NS is the product of the radices already applied.  Ends with
@@ -296,20 +296,39 @@ __device__ __forceinline__ void mr_big_stage(float2* sm, int t) {
   constexpr int h = (R - 1) / 2;
   constexpr int PB = T / NBUT >= 2 ? 2 : 1;  // threads per butterfly
   constexpr int QA = PB == 2 ? h / 2 : h;    // thread 0 of a butterfly: q = 0 .. QA; thread 1: QA + 1 .. h
-  // phase 1: twiddle and fold
-  for (int it = t; it < NBUT * h; it += T) {
-    const int jp = it % NBUT, i = 1 + it / NBUT;
-    float2 a = sm[spad(jp + i * NBUT)], b = sm[spad(jp + (R - i) * NBUT)];
+  // phase 1: twiddle and fold, the PB threads of a butterfly on consecutive runs of i;
+  // the twiddles w^i and w^(R-i) of a run start from sincospif and step by w and
+  // conj(w) (at most IRUN - 1 products)
+  constexpr int IRUN = (h + PB - 1) / PB;
+  if (t < PB * NBUT) {
+    const int jp = t % NBUT, i0 = 1 + (t / NBUT) * IRUN;
+    const int k = jp % NS;
+    float2 w = make_float2(1.f, 0.f), wa = w, wb = w;
     if constexpr (NS > 1) {
-      const int k = jp % NS;
-      float sa, ca, sb, cb;
-      sincospif(2.0f * (float)((i * k) % (NS * R)) * (1.0f / (float)(NS * R)), &sa, &ca);
-      sincospif(2.0f * (float)(((R - i) * k) % (NS * R)) * (1.0f / (float)(NS * R)), &sb, &cb);
-      a = cmul(a, make_float2(ca, DIR * sa));
-      b = cmul(b, make_float2(cb, DIR * sb));
+      constexpr float inv = 1.0f / (float)(NS * R);
+      float s1, c1, sa, ca, sb, cb;
+      sincospif(2.0f * (float)k * inv, &s1, &c1);
+      sincospif(2.0f * (float)((i0 * k) % (NS * R)) * inv, &sa, &ca);
+      sincospif(2.0f * (float)(((R - i0) * k) % (NS * R)) * inv, &sb, &cb);
+      w = make_float2(c1, DIR * s1);
+      wa = make_float2(ca, DIR * sa);
+      wb = make_float2(cb, DIR * sb);
     }
-    sm[spad(jp + i * NBUT)] = cadd(a, b);
-    sm[spad(jp + (R - i) * NBUT)] = csub(a, b);
+#pragma unroll
+    for (int r = 0; r < IRUN; ++r) {
+      const int i = i0 + r;
+      if (i <= h) {
+        float2 a = sm[spad(jp + i * NBUT)], b = sm[spad(jp + (R - i) * NBUT)];
+        if constexpr (NS > 1) {
+          a = cmul(a, wa);
+          b = cmul(b, wb);
+          wa = cmul(wa, w);
+          wb = cmul(wb, make_float2(w.x, -w.y));
+        }
+        sm[spad(jp + i * NBUT)] = cadd(a, b);
+        sm[spad(jp + (R - i) * NBUT)] = csub(a, b);
+      }
+    }
   }
   __syncthreads();
   // phase 2: output pairs in registers
