@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblprec_gb300.so")
 SOURCES = ["lp_kernels.cu", "lp_kernels_mr.cu", "lp_kernels_mr2.cu", "lp_kernels_mr3.cu", "lp_kernels_mr4.cu",
-           "lp_handle.cu", "lp_solver.cu", "precompute.cpp"]
+           "lp_kernels_mr5.cu", "lp_handle.cu", "lp_solver.cu", "precompute.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

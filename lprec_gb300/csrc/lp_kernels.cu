@@ -692,7 +692,8 @@ cudaError_t configure_kernels(int N) {
   if (e == cudaSuccess) e = mr_configure(optin);
   if (e == cudaSuccess) e = mr2_configure(optin);
   if (e == cudaSuccess) e = mr3_configure(optin);
-  return e == cudaSuccess ? mr4_configure(optin) : e;
+  if (e == cudaSuccess) e = mr4_configure(optin);
+  return e == cudaSuccess ? mr5_configure(optin) : e;
 }
 
 void set_use_p2(bool on) { g_use_p2 = on; }
@@ -727,7 +728,7 @@ cudaError_t launch_col_prefilter(const ColPrefilterArgs& a, int S, cudaStream_t 
 
 cudaError_t launch_fwd_c2lp(const FwdC2LPArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && (p2_fwd_c2lp(a, S, st, &pe) || mr_fwd_c2lp(a, S, st, &pe) || mr2_fwd_c2lp(a, S, st, &pe) || mr3_fwd_c2lp(a, S, st, &pe) || mr4_fwd_c2lp(a, S, st, &pe))) return pe;
+  if (g_use_p2 && (p2_fwd_c2lp(a, S, st, &pe) || mr_fwd_c2lp(a, S, st, &pe) || mr2_fwd_c2lp(a, S, st, &pe) || mr3_fwd_c2lp(a, S, st, &pe) || mr4_fwd_c2lp(a, S, st, &pe) || mr5_fwd_c2lp(a, S, st, &pe))) return pe;
   if (smem_ok(smem_c2lp(a.Nrho)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.Nth + 1) / 2);
   k_fwd_c2lp<<<grid, kFFTThreads, smem_c2lp(a.Nrho), st>>>(a);
@@ -740,13 +741,14 @@ bool theta_conv_gathers(int Nth, int nrows) {
                       : mr_has_length(Nth)  ? mr_gather_smem(Nth, nrows)
                       : mr2_has_length(Nth) ? mr2_gather_smem(Nth, nrows)
                       : mr3_has_length(Nth) ? mr3_gather_smem(Nth, nrows)
-                                            : mr4_gather_smem(Nth, nrows);
+                      : mr4_has_length(Nth) ? mr4_gather_smem(Nth, nrows)
+                                            : mr5_gather_smem(Nth, nrows);
   return need > 0 && smem_fits(need);
 }
 
 cudaError_t launch_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && (p2_theta_conv(a, S, st, &pe) || mr_theta_conv(a, S, st, &pe) || mr2_theta_conv(a, S, st, &pe) || mr3_theta_conv(a, S, st, &pe) || mr4_theta_conv(a, S, st, &pe))) return pe;
+  if (g_use_p2 && (p2_theta_conv(a, S, st, &pe) || mr_theta_conv(a, S, st, &pe) || mr2_theta_conv(a, S, st, &pe) || mr3_theta_conv(a, S, st, &pe) || mr4_theta_conv(a, S, st, &pe) || mr5_theta_conv(a, S, st, &pe))) return pe;
   if (a.rowspec) return cudaErrorNotSupported;  // the gathered input needs a register-FFT length
   if (smem_ok(smem_theta(a.Nth)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.Nk + 1) / 2);
@@ -756,7 +758,7 @@ cudaError_t launch_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st) {
 
 cudaError_t launch_fwd_lp2polar(const FwdLP2PolarArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && (p2_fwd_lp2polar(a, S, st, &pe) || mr_fwd_lp2polar(a, S, st, &pe) || mr2_fwd_lp2polar(a, S, st, &pe) || mr3_fwd_lp2polar(a, S, st, &pe) || mr4_fwd_lp2polar(a, S, st, &pe))) return pe;
+  if (g_use_p2 && (p2_fwd_lp2polar(a, S, st, &pe) || mr_fwd_lp2polar(a, S, st, &pe) || mr2_fwd_lp2polar(a, S, st, &pe) || mr3_fwd_lp2polar(a, S, st, &pe) || mr4_fwd_lp2polar(a, S, st, &pe) || mr5_fwd_lp2polar(a, S, st, &pe))) return pe;
   if (a.nrows <= 0) return cudaSuccess;
   if (smem_ok(smem_c2lp(a.Nrho)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.nrows + 1) / 2);
@@ -766,7 +768,7 @@ cudaError_t launch_fwd_lp2polar(const FwdLP2PolarArgs& a, int S, cudaStream_t st
 
 cudaError_t launch_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && (p2_adj_ingest(a, S, st, &pe) || mr_adj_ingest(a, S, st, &pe) || mr2_adj_ingest(a, S, st, &pe) || mr3_adj_ingest(a, S, st, &pe) || mr4_adj_ingest(a, S, st, &pe))) return pe;
+  if (g_use_p2 && (p2_adj_ingest(a, S, st, &pe) || mr_adj_ingest(a, S, st, &pe) || mr2_adj_ingest(a, S, st, &pe) || mr3_adj_ingest(a, S, st, &pe) || mr4_adj_ingest(a, S, st, &pe) || mr5_adj_ingest(a, S, st, &pe))) return pe;
   if (smem_ok(smem_adj_ingest(a.N, a.H != nullptr)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.Nproj0 + 1) / 2);
   k_adj_ingest<<<grid, kFFTThreads, smem_adj_ingest(a.N, a.H != nullptr), st>>>(a);
@@ -775,7 +777,7 @@ cudaError_t launch_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st) {
 
 cudaError_t launch_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && (p2_adj_polar2lp(a, S, st, &pe) || mr_adj_polar2lp(a, S, st, &pe) || mr2_adj_polar2lp(a, S, st, &pe) || mr3_adj_polar2lp(a, S, st, &pe) || mr4_adj_polar2lp(a, S, st, &pe))) return pe;
+  if (g_use_p2 && (p2_adj_polar2lp(a, S, st, &pe) || mr_adj_polar2lp(a, S, st, &pe) || mr2_adj_polar2lp(a, S, st, &pe) || mr3_adj_polar2lp(a, S, st, &pe) || mr4_adj_polar2lp(a, S, st, &pe) || mr5_adj_polar2lp(a, S, st, &pe))) return pe;
   if (a.chi < a.clo) return cudaSuccess;
   if (smem_ok(smem_polar2lp(a.Nrho, a.N)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.chi - a.clo + 2) / 2);
@@ -785,7 +787,7 @@ cudaError_t launch_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st
 
 cudaError_t launch_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && (p2_adj_lpcols(a, S, st, &pe) || mr_adj_lpcols(a, S, st, &pe) || mr2_adj_lpcols(a, S, st, &pe) || mr3_adj_lpcols(a, S, st, &pe) || mr4_adj_lpcols(a, S, st, &pe))) return pe;
+  if (g_use_p2 && (p2_adj_lpcols(a, S, st, &pe) || mr_adj_lpcols(a, S, st, &pe) || mr2_adj_lpcols(a, S, st, &pe) || mr3_adj_lpcols(a, S, st, &pe) || mr4_adj_lpcols(a, S, st, &pe) || mr5_adj_lpcols(a, S, st, &pe))) return pe;
   if (smem_ok(smem_c2lp(a.Nrho)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.hi2 - a.lo2 + 2) / 2);
   k_adj_lpcols<<<grid, kFFTThreads, smem_c2lp(a.Nrho), st>>>(a);
@@ -1121,7 +1123,7 @@ __global__ void k_crop(CropArgs a) {
 cudaError_t launch_fwdT_rows(const FwdTRowsArgs& a, int S, cudaStream_t st) {
   if (a.nrows <= 0) return cudaSuccess;
   cudaError_t pe;
-  if (g_use_p2 && (p2_fwdT_rows(a, S, st, &pe) || mr_fwdT_rows(a, S, st, &pe) || mr2_fwdT_rows(a, S, st, &pe) || mr3_fwdT_rows(a, S, st, &pe) || mr4_fwdT_rows(a, S, st, &pe))) return pe;
+  if (g_use_p2 && (p2_fwdT_rows(a, S, st, &pe) || mr_fwdT_rows(a, S, st, &pe) || mr2_fwdT_rows(a, S, st, &pe) || mr3_fwdT_rows(a, S, st, &pe) || mr4_fwdT_rows(a, S, st, &pe) || mr5_fwdT_rows(a, S, st, &pe))) return pe;
   const size_t sm = fft_bytes(a.Nrho, 1) + 2 * (size_t)a.Nrho * sizeof(float);
   if (smem_ok(sm) != cudaSuccess) return cudaErrorInvalidConfiguration;
   cudaFuncSetAttribute(k_fwdT_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
@@ -1141,7 +1143,7 @@ cudaError_t launch_fwdT_colsum(const FwdTColSumArgs& a, int S, int nblk, cudaStr
 cudaError_t launch_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st) {
   if (a.dhi < a.dlo) return cudaSuccess;
   cudaError_t pe;
-  if (g_use_p2 && (p2_fwdT_cols(a, S, st, &pe) || mr_fwdT_cols(a, S, st, &pe) || mr2_fwdT_cols(a, S, st, &pe) || mr3_fwdT_cols(a, S, st, &pe) || mr4_fwdT_cols(a, S, st, &pe))) return pe;
+  if (g_use_p2 && (p2_fwdT_cols(a, S, st, &pe) || mr_fwdT_cols(a, S, st, &pe) || mr2_fwdT_cols(a, S, st, &pe) || mr3_fwdT_cols(a, S, st, &pe) || mr4_fwdT_cols(a, S, st, &pe) || mr5_fwdT_cols(a, S, st, &pe))) return pe;
   const size_t sm = fft_bytes(a.Nrho, 1);
   if (smem_ok(sm) != cudaSuccess) return cudaErrorInvalidConfiguration;
   cudaFuncSetAttribute(k_fwdT_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);

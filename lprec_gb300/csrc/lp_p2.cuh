@@ -956,5 +956,6 @@ LP_DECLARE_LENGTH_SET(mr)
 LP_DECLARE_LENGTH_SET(mr2)
 LP_DECLARE_LENGTH_SET(mr3)
 LP_DECLARE_LENGTH_SET(mr4)
+LP_DECLARE_LENGTH_SET(mr5)
 
 }  // namespace lpgb

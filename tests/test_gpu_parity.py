@@ -371,14 +371,15 @@ def test_prime_radix_lengths(torch_cuda, args):
                                   (1536, 2304, 'cubic', 'ramp', 768), (2016, 3024, 'cubic', 'parzen', 1008),
                                   (2048, 1024, 'cubic', 'shepp-logan', 1021), (512, 768, 'cubic', 'ramp', 243),
                                   (1024, 1536, 'linear', 'shepp-logan', 509), (1024, 1536, 'cubic', 'hann', 500),
-                                  (2048, 1024, 'cubic', 'shepp-logan', 1012)])
+                                  (2048, 1024, 'cubic', 'shepp-logan', 1012), (1280, 1920, 'cubic', 'ramp', 640),
+                                  (2560, 768, 'linear', 'shepp-logan', 1280)])
 def test_mixed_radix_lengths(torch_cuda, args):
     """Padded sizes that are not powers of two, served by the mixed-radix register FFT:
     N = 528 = 16*3*11 (an off-centre axis at N0 = 512), 1008 = 16*63, 1536 = 16*96,
     2016 = 16*126, 2064 = 16*3*43 (an axis 3 pixels off centre at N0 = 2048: the prime
     43 takes the output-parallel stage), 544 = 16*2*17, 1040 = 16*5*13, 1056 (Nrho 2112)
-    and 2080 = 16*2*5*13 (axes 3 to 16 pixels off centre), Nrho = 2N; one slice each
-    against the oracle."""
+    and 2080 = 16*2*5*13 (axes 3 to 16 pixels off centre), the detector widths 1280 and
+    2560 = 16*32*5, Nrho = 2N; one slice each against the oracle."""
     from lprec_gb300 import _lib
     N0, Nproj, interp, filt, cor = args
     packed = _lib.precompute(N0, Nproj, 1, cor, interp, filt, precision='fp64')
