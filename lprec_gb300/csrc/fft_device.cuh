@@ -241,7 +241,7 @@ __device__ __forceinline__ void fft_stage(const CBuf in, const CBuf out, const f
   }
 }
 
-// Any odd radix R > 7 the planner leaves (primes 11, 13, 17, ...).  The thread's R
+// Odd radix 11 or 13, one thread per butterfly.  The thread's R
 // inputs belong to its butterfly alone, so they are twiddled and folded in place in
 // the source buffer: S_i = x_i + x_{R-i} and D_i = x_i - x_{R-i}, i = 1..h, h = (R-1)/2.
 // With c = cos(2 pi i q / R) and s = sin(2 pi i q / R),
@@ -250,7 +250,7 @@ __device__ __forceinline__ void fft_stage(const CBuf in, const CBuf out, const f
 // products of each kind.  The root index i q mod R advances by additions; the roots
 // come from the length-L table (exp(-2 pi i t / L) at t = m L / R).
 template <int DIR>
-__device__ void fft_stage_dyn(const CBuf in, const CBuf out, const float2* __restrict__ tw, int L, int Ns, int R,
+__device__ void fft_stage_dyn_serial(const CBuf in, const CBuf out, const float2* __restrict__ tw, int L, int Ns, int R,
                               int nfft, int stride) {
   const int Lr = L / R;
   const int total = nfft * Lr;
@@ -296,6 +296,78 @@ __device__ void fft_stage_dyn(const CBuf in, const CBuf out, const float2* __res
   }
 }
 
+// A prime radix above 13 the planner leaves (17, 19, ...), output-parallel (with few
+// butterflies per signal, one thread per butterfly would leave most threads idle).
+// Phase 1, one (signal, butterfly, i) item per thread step: twiddle x_i and x_{R-i}
+// in place and fold them into S_i = x_i + x_{R-i} (at i) and D_i = x_i - x_{R-i} (at
+// R - i), i = 1..h, h = (R-1)/2.  Phase 2, one (signal, butterfly, q) unit per thread
+// step: with c = cos(2 pi i q / R) and s = sin(2 pi i q / R),
+//   X_0 = x_0 + sum_i S_i,  X_q = x_0 + A_q + DIR i B_q,  X_{R-q} = x_0 + A_q - DIR i B_q,
+// A_q = sum_i S_i c, B_q = sum_i D_i s, written straight to the output buffer (the
+// stage is out of place).  The root index i q mod R advances by additions; the roots
+// come from the length-L table (exp(-2 pi i t / L) at t = m L / R).  Every thread of
+// the block calls it (one barrier between the phases).
+template <int DIR>
+__device__ void fft_stage_dyn(const CBuf in, const CBuf out, const float2* __restrict__ tw, int L, int Ns, int R,
+                              int nfft, int stride) {
+  const int Lr = L / R;
+  const int tstep = L / (Ns * R);
+  const int h = (R - 1) / 2;
+  // items and units are numbered with i (q) outermost, so the lanes of a warp work on
+  // consecutive butterflies with the same i (q): conflict-free shared loads and one
+  // root for the whole warp
+  const int nb = nfft * Lr;
+  for (int it = threadIdx.x; it < nb * h; it += blockDim.x) {
+    const int i = 1 + it / nb;
+    const int t = it - (i - 1) * nb;
+    const int f = t / Lr;
+    const int j = t - f * Lr;
+    const int k = j % Ns;
+    const CBuf src = in.offset(f * stride);
+    float2 a = src.get(j + i * Lr), b = src.get(j + (R - i) * Lr);
+    if (Ns > 1) {
+      a = cmul(a, twid<DIR>(tw, i * k * tstep));
+      b = cmul(b, twid<DIR>(tw, (R - i) * k * tstep));
+    }
+    src.set(j + i * Lr, cadd(a, b));
+    src.set(j + (R - i) * Lr, csub(a, b));
+  }
+  __syncthreads();
+  for (int u = threadIdx.x; u < nb * (h + 1); u += blockDim.x) {
+    const int q = u / nb;
+    const int t = u - q * nb;
+    const int f = t / Lr;
+    const int j = t - f * Lr;
+    const int k = j % Ns;
+    const CBuf src = in.offset(f * stride);
+    const CBuf dst = out.offset(f * stride);
+    const int base = (j - k) * R + k;
+    const float2 x0 = src.get(j);
+    if (q == 0) {
+      float2 sum = x0;
+      for (int i = 1; i <= h; ++i) sum = cadd(sum, src.get(j + i * Lr));
+      dst.set(base, sum);
+      continue;
+    }
+    float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
+    int m = 0;
+    for (int i = 1; i <= h; ++i) {
+      m += q;
+      if (m >= R) m -= R;
+      const float2 w = __ldg(tw + m * Lr);  // (cos, -sin) of 2 pi m / R
+      const float2 si = src.get(j + i * Lr), di = src.get(j + (R - i) * Lr);
+      A.x += si.x * w.x;
+      A.y += si.y * w.x;
+      B.x -= di.x * w.y;
+      B.y -= di.y * w.y;
+    }
+    // DIR i B = (-DIR B.y, DIR B.x)
+    const float2 iB = make_float2(-DIR * B.y, DIR * B.x);
+    dst.set(base + q * Ns, cadd(cadd(x0, A), iB));
+    dst.set(base + (R - q) * Ns, csub(cadd(x0, A), iB));
+  }
+}
+
 // Run the transform on `nfft` signals; data starts in `a`, `b` is scratch of
 // the same shape.  Returns the buffer holding the result.  All threads of the
 // block must call it; it ends with a __syncthreads().
@@ -313,7 +385,10 @@ __device__ CBuf fft_block(CBuf a, CBuf b, const FFTPlan& p, int nfft, int stride
       case 3: fft_stage<DIR, 3>(in, out, p.tw, p.L, Ns, nfft, stride); break;
       case 5: fft_stage<DIR, 5>(in, out, p.tw, p.L, Ns, nfft, stride); break;
       case 7: fft_stage<DIR, 7>(in, out, p.tw, p.L, Ns, nfft, stride); break;
-      default: fft_stage_dyn<DIR>(in, out, p.tw, p.L, Ns, R, nfft, stride); break;
+      default:
+        if (R <= 13) fft_stage_dyn_serial<DIR>(in, out, p.tw, p.L, Ns, R, nfft, stride);
+        else fft_stage_dyn<DIR>(in, out, p.tw, p.L, Ns, R, nfft, stride);
+        break;
     }
     __syncthreads();
     Ns *= R;

@@ -353,10 +353,10 @@ def test_prefilter_chunk_edges(torch_cuda, args):
 
 
 @pytest.mark.parametrize("args", [(176, 264, 88, 'cubic', 'ramp'), (272, 408, 136, 'cubic', 'shepp-logan'),
-                                  (208, 150, 104, 'linear', 'hann')])
+                                  (208, 150, 104, 'linear', 'hann'), (368, 552, 184, 'cubic', 'parzen')])
 def test_prime_radix_lengths(torch_cuda, args):
-    """Padded sizes with a prime factor above 7 (176 = 16*11, 272 = 16*17, 208 = 16*13):
-    the generic FFT's odd-prime stage against the oracle."""
+    """Padded sizes with a prime factor above 7 (176 = 16*11, 272 = 16*17, 208 = 16*13,
+    368 = 16*23): the generic FFT's output-parallel odd-prime stage against the oracle."""
     from lprec_gb300 import _lib
     N0, Nproj, cor, interp, filt = args
     packed = _lib.precompute(N0, Nproj, 2, cor, interp, filt, precision='fp64')
