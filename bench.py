@@ -69,6 +69,14 @@ class Clocks:
         self.dev = dev
         self.proc = None
         self.path = None
+        self._summary = None
+
+    def _lines(self):
+        try:
+            with open(self.path) as fh:
+                return sum(1 for _ in fh)
+        except OSError:
+            return 0
 
     def __enter__(self):
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -78,10 +86,15 @@ class Clocks:
         os.close(fd)
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+        # the sampler's first line before the timed region starts (nvidia-smi takes a
+        # moment to come up; a short region would otherwise end before any sample)
+        t_end = time.time() + 5.0
+        while self.proc is not None and self._lines() == 0 and time.time() < t_end and self.proc.poll() is None:
+            time.sleep(0.02)
         return self
 
     def __exit__(self, *a):
@@ -93,6 +106,10 @@ class Clocks:
                 self.proc.kill()
 
     def summary(self):
+        """Median SM clock, maximum clock and active throttle reasons of the samples
+        (computed once; later calls return the same record)."""
+        if self._summary is not None:
+            return self._summary
         out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
         if not self.path or not os.path.exists(self.path):
             return out
@@ -114,6 +131,7 @@ class Clocks:
         if sm:
             out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
                    "samples": len(sm)}
+        self._summary = out
         return out
 
 

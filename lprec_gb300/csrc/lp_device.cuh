@@ -278,9 +278,13 @@ __device__ __forceinline__ void rho_scatter_T(const ArgsT& a, int s, int r0, int
     // strictly monotone in x put the points of one residue class at least ntap apart,
     // and a window spans at most L - ntap, so no two taps of a pass meet modulo L: each
     // bin takes at most one addition per pass, in a fixed pass order (rows that do not
-    // wrap skip the second window; every thread still meets every barrier)
+    // wrap skip the second window; every thread still meets every barrier, and a block
+    // none of whose rows wraps runs no second-window passes at all)
+    const bool wraps = __syncthreads_or((r0 >= 0 && __ldg(a.rbase + r0) != kNoWrap) ||
+                                        (r1 >= 0 && __ldg(a.rbase + r1) != kNoWrap));
+    const int nwin = wraps ? 2 : 1;
     for (int p = 0; p < ntap; ++p) {
-      for (int h = 0; h < 2; ++h) {
+      for (int h = 0; h < nwin; ++h) {
         for (int q = 0; q < 2; ++q) {
           const int r = q == 0 ? r0 : r1;
           if (r < 0) continue;

@@ -4,6 +4,8 @@ import ctypes
 import glob
 import os
 import re
+import sys
+import time
 
 import numpy as np
 import pytest
@@ -282,3 +284,23 @@ int main(void) {
     got = [int(v) for v in out.stdout.split()]
     arrays = lib.precompute(64, 96, 1, 32.0, 'cubic', 'ramp')
     assert got == [a.size for a in arrays]
+
+
+def test_bench_clock_sampler(tmp_path, monkeypatch):
+    """The bench's clock record: samples of a stand-in nvidia-smi (one per 100 ms),
+    the first one present before the timed region starts, median and maximum clock and
+    the active throttle reasons; a second summary() returns the same record."""
+    fake = tmp_path / "nvidia-smi"
+    fake.write_text("#!/bin/sh\nwhile true; do echo '0, 1965, 2070, 900.5, 0x4, Not Active, Not Active, "
+                    "Not Active, Active'; sleep 0.1; done\n")
+    fake.chmod(0o755)
+    monkeypatch.setenv("PATH", str(tmp_path) + os.pathsep + os.environ.get("PATH", ""))
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), ".."))
+    import bench
+    with bench.Clocks(0) as clk:
+        assert clk._lines() >= 1
+        time.sleep(0.35)
+    first = clk.summary()
+    assert first["sm_mhz"] == 1965 and first["sm_max_mhz"] == 2070 and first["samples"] >= 2
+    assert first["reasons"] == ["sw_power_cap"]
+    assert clk.summary() == first
