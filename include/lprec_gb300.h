@@ -126,7 +126,10 @@ int lp_adj(lp_handle* h, float* f, const float* R, int S0, void* stream);
  * (its own kernel fZadj and grids, src/lprec/initsadj.py) and only
  * approximately the transpose.  R is read only.  No atomics: repeated calls give
  * the same bits.  The first call on a handle builds the gather tables and
- * allocates their buffers (make it outside stream capture).
+ * allocates their buffers (make it outside stream capture); when the row spectra
+ * and spectra of the three spans fit in 1 GiB more, it allocates them per span
+ * and calls of at most 8 * 2048^2 image samples run the spans on the handle's
+ * span streams (joined on the caller's stream before the Cartesian gather).
  */
 int lp_fwd_transpose(lp_handle* h, float* f, const float* R, int S0, void* stream);
 
