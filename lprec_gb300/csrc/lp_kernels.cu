@@ -670,6 +670,10 @@ using Pow2Lengths = Lengths<256, 512, 1024, 2048, 4096, 8192>;
 LP_DEFINE_LENGTH_SET(p2, Pow2Lengths)
 // generic (any N) kernels are used when g_use_p2 is false or no register-FFT length fits
 static bool g_use_p2 = true;
+// the register-FFT launcher of FN for the length, from whichever length list holds it
+#define LP_REGISTER_FFT(FN, A, S, ST, PE)                                                   \
+  (g_use_p2 && (p2_##FN(A, S, ST, PE) || mr_##FN(A, S, ST, PE) || mr2_##FN(A, S, ST, PE) || \
+                mr3_##FN(A, S, ST, PE) || mr4_##FN(A, S, ST, PE) || mr5_##FN(A, S, ST, PE)))
 
 // Allow every kernel the device's opt-in shared memory; launches check their
 // own need against it.
@@ -728,7 +732,7 @@ cudaError_t launch_col_prefilter(const ColPrefilterArgs& a, int S, cudaStream_t 
 
 cudaError_t launch_fwd_c2lp(const FwdC2LPArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && (p2_fwd_c2lp(a, S, st, &pe) || mr_fwd_c2lp(a, S, st, &pe) || mr2_fwd_c2lp(a, S, st, &pe) || mr3_fwd_c2lp(a, S, st, &pe) || mr4_fwd_c2lp(a, S, st, &pe) || mr5_fwd_c2lp(a, S, st, &pe))) return pe;
+  if (LP_REGISTER_FFT(fwd_c2lp, a, S, st, &pe)) return pe;
   if (smem_ok(smem_c2lp(a.Nrho)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.Nth + 1) / 2);
   k_fwd_c2lp<<<grid, kFFTThreads, smem_c2lp(a.Nrho), st>>>(a);
@@ -748,7 +752,7 @@ bool theta_conv_gathers(int Nth, int nrows) {
 
 cudaError_t launch_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && (p2_theta_conv(a, S, st, &pe) || mr_theta_conv(a, S, st, &pe) || mr2_theta_conv(a, S, st, &pe) || mr3_theta_conv(a, S, st, &pe) || mr4_theta_conv(a, S, st, &pe) || mr5_theta_conv(a, S, st, &pe))) return pe;
+  if (LP_REGISTER_FFT(theta_conv, a, S, st, &pe)) return pe;
   if (a.rowspec) return cudaErrorNotSupported;  // the gathered input needs a register-FFT length
   if (smem_ok(smem_theta(a.Nth)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.Nk + 1) / 2);
@@ -758,7 +762,7 @@ cudaError_t launch_theta_conv(const ThetaConvArgs& a, int S, cudaStream_t st) {
 
 cudaError_t launch_fwd_lp2polar(const FwdLP2PolarArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && (p2_fwd_lp2polar(a, S, st, &pe) || mr_fwd_lp2polar(a, S, st, &pe) || mr2_fwd_lp2polar(a, S, st, &pe) || mr3_fwd_lp2polar(a, S, st, &pe) || mr4_fwd_lp2polar(a, S, st, &pe) || mr5_fwd_lp2polar(a, S, st, &pe))) return pe;
+  if (LP_REGISTER_FFT(fwd_lp2polar, a, S, st, &pe)) return pe;
   if (a.nrows <= 0) return cudaSuccess;
   if (smem_ok(smem_c2lp(a.Nrho)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.nrows + 1) / 2);
@@ -768,7 +772,7 @@ cudaError_t launch_fwd_lp2polar(const FwdLP2PolarArgs& a, int S, cudaStream_t st
 
 cudaError_t launch_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && (p2_adj_ingest(a, S, st, &pe) || mr_adj_ingest(a, S, st, &pe) || mr2_adj_ingest(a, S, st, &pe) || mr3_adj_ingest(a, S, st, &pe) || mr4_adj_ingest(a, S, st, &pe) || mr5_adj_ingest(a, S, st, &pe))) return pe;
+  if (LP_REGISTER_FFT(adj_ingest, a, S, st, &pe)) return pe;
   if (smem_ok(smem_adj_ingest(a.N, a.H != nullptr)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.Nproj0 + 1) / 2);
   k_adj_ingest<<<grid, kFFTThreads, smem_adj_ingest(a.N, a.H != nullptr), st>>>(a);
@@ -777,7 +781,7 @@ cudaError_t launch_adj_ingest(const AdjIngestArgs& a, int S, cudaStream_t st) {
 
 cudaError_t launch_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && (p2_adj_polar2lp(a, S, st, &pe) || mr_adj_polar2lp(a, S, st, &pe) || mr2_adj_polar2lp(a, S, st, &pe) || mr3_adj_polar2lp(a, S, st, &pe) || mr4_adj_polar2lp(a, S, st, &pe) || mr5_adj_polar2lp(a, S, st, &pe))) return pe;
+  if (LP_REGISTER_FFT(adj_polar2lp, a, S, st, &pe)) return pe;
   if (a.chi < a.clo) return cudaSuccess;
   if (smem_ok(smem_polar2lp(a.Nrho, a.N)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.chi - a.clo + 2) / 2);
@@ -787,7 +791,7 @@ cudaError_t launch_adj_polar2lp(const AdjPolar2LPArgs& a, int S, cudaStream_t st
 
 cudaError_t launch_adj_lpcols(const AdjLPColsArgs& a, int S, cudaStream_t st) {
   cudaError_t pe;
-  if (g_use_p2 && (p2_adj_lpcols(a, S, st, &pe) || mr_adj_lpcols(a, S, st, &pe) || mr2_adj_lpcols(a, S, st, &pe) || mr3_adj_lpcols(a, S, st, &pe) || mr4_adj_lpcols(a, S, st, &pe) || mr5_adj_lpcols(a, S, st, &pe))) return pe;
+  if (LP_REGISTER_FFT(adj_lpcols, a, S, st, &pe)) return pe;
   if (smem_ok(smem_c2lp(a.Nrho)) != cudaSuccess) return cudaErrorInvalidConfiguration;
   dim3 grid(S, (a.hi2 - a.lo2 + 2) / 2);
   k_adj_lpcols<<<grid, kFFTThreads, smem_c2lp(a.Nrho), st>>>(a);
@@ -1123,7 +1127,7 @@ __global__ void k_crop(CropArgs a) {
 cudaError_t launch_fwdT_rows(const FwdTRowsArgs& a, int S, cudaStream_t st) {
   if (a.nrows <= 0) return cudaSuccess;
   cudaError_t pe;
-  if (g_use_p2 && (p2_fwdT_rows(a, S, st, &pe) || mr_fwdT_rows(a, S, st, &pe) || mr2_fwdT_rows(a, S, st, &pe) || mr3_fwdT_rows(a, S, st, &pe) || mr4_fwdT_rows(a, S, st, &pe) || mr5_fwdT_rows(a, S, st, &pe))) return pe;
+  if (LP_REGISTER_FFT(fwdT_rows, a, S, st, &pe)) return pe;
   const size_t sm = fft_bytes(a.Nrho, 1) + 2 * (size_t)a.Nrho * sizeof(float);
   if (smem_ok(sm) != cudaSuccess) return cudaErrorInvalidConfiguration;
   cudaFuncSetAttribute(k_fwdT_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
@@ -1143,7 +1147,7 @@ cudaError_t launch_fwdT_colsum(const FwdTColSumArgs& a, int S, int nblk, cudaStr
 cudaError_t launch_fwdT_cols(const FwdTColsArgs& a, int S, cudaStream_t st) {
   if (a.dhi < a.dlo) return cudaSuccess;
   cudaError_t pe;
-  if (g_use_p2 && (p2_fwdT_cols(a, S, st, &pe) || mr_fwdT_cols(a, S, st, &pe) || mr2_fwdT_cols(a, S, st, &pe) || mr3_fwdT_cols(a, S, st, &pe) || mr4_fwdT_cols(a, S, st, &pe) || mr5_fwdT_cols(a, S, st, &pe))) return pe;
+  if (LP_REGISTER_FFT(fwdT_cols, a, S, st, &pe)) return pe;
   const size_t sm = fft_bytes(a.Nrho, 1);
   if (smem_ok(sm) != cudaSuccess) return cudaErrorInvalidConfiguration;
   cudaFuncSetAttribute(k_fwdT_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
