@@ -208,6 +208,10 @@ struct lp_handle {
   std::vector<float> erho_h;
   DevBuf<float> erho;
   DevBuf<float2> spec;     // [Nslices][Nk][Nth]
+  // spans 1 and 2 of a concurrent-span call that the handle's own spectrum slots do not
+  // hold 3 times over (a handle of few slices): [2][sspec_slices][Nk][Nth]
+  DevBuf<float2> sspec;
+  int sspec_slices = 0;
   DevBuf<float2> tw_rho;   // FFT twiddles for length Nrho (also the FBP filter's 2N)
   DevBuf<float2> tw_th;    // FFT twiddles for length Nth
   FwdDev* fwd = nullptr;
@@ -449,8 +453,19 @@ static void destroy_span_streams(lp_handle* h) {
 // Measured: up to 8 slices at N=2048 and 32 at N=1024 gain; larger calls fill
 // the GPU already and their concurrent spans compete.
 constexpr double kSpreadSamples = 8.0 * 2048 * 2048;
+// the extra spectrum regions of a handle of few slices may take at most this much
+static const size_t kSpreadSpecBytes = (size_t)1 << 30;
 static bool spread_spans(const lp_handle* h, int slot, int n, bool one_chunk) {
-  return one_chunk && (double)n * h->N * h->N <= kSpreadSamples && slot + 3 * n <= h->Nslices;
+  return one_chunk && (double)n * h->N * h->N <= kSpreadSamples &&
+         (slot + 3 * n <= h->Nslices || n <= h->sspec_slices);
+}
+// the spectrum of span k of a call of n slices from slot (spread: its own region)
+static float2* span_spec(lp_handle* h, int slot, int n, int k, bool spread) {
+  const size_t sl = spec_slice(h->Nk, h->Nth);
+  float2* spec = h->spec.p + (size_t)slot * sl;
+  if (!spread || k == 0) return spec;
+  if (slot + 3 * n <= h->Nslices) return spec + (size_t)k * n * sl;
+  return h->sspec.p + (size_t)(k - 1) * h->sspec_slices * sl;
 }
 static cudaError_t span_fork(lp_handle* h, cudaStream_t st) {
   cudaError_t e = cudaEventRecord(h->ev_sfork, st);
@@ -572,6 +587,16 @@ int lp_create(const float* glpars, int64_t n, int device, lp_handle** out) {
   if (e == cudaSuccess) e = dev_upload(h->tw_rho, twiddles(h->Nrho));
   if (e == cudaSuccess) e = dev_upload(h->tw_th, twiddles(h->Nth));
   if (e == cudaSuccess) e = dev_alloc(h->spec, (size_t)h->Nslices * spec_slice(h->Nk, h->Nth));
+  {
+    // concurrent spans for the calls that qualify (spread_spans) but would not fit 3
+    // times in the handle's own slots
+    const int nmax = (int)std::min<double>(h->Nslices, std::floor(kSpreadSamples / ((double)h->N * h->N)));
+    const size_t need = 2 * (size_t)std::max(nmax, 0) * spec_slice(h->Nk, h->Nth);
+    if (e == cudaSuccess && nmax > 0 && 3 * nmax > h->Nslices && need * sizeof(float2) <= kSpreadSpecBytes) {
+      e = dev_alloc(h->sspec, need);
+      if (e == cudaSuccess) h->sspec_slices = nmax;
+    }
+  }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
@@ -588,6 +613,7 @@ int lp_create(const float* glpars, int64_t n, int device, lp_handle** out) {
     h->tw_rho.free_();
     h->tw_th.free_();
     h->spec.free_();
+    h->sspec.free_();
     if (h->side) cudaStreamDestroy(h->side);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
@@ -995,6 +1021,7 @@ int lp_destroy(lp_handle* h) {
   free_adj(h->adj);
   h->erho.free_();
   h->spec.free_();
+  h->sspec.free_();
   h->tw_rho.free_();
   h->tw_th.free_();
   for (const ProfRec& r : h->prof) {
@@ -1034,6 +1061,7 @@ int lp_debug_fill_scratch(lp_handle* h, float value, void* stream) {
   DeviceGuard g(h->device);
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = fill_async((float*)h->spec.p, h->spec.n * 2, value, st);
+  if (e == cudaSuccess && h->sspec.p) e = fill_async((float*)h->sspec.p, h->sspec.n * 2, value, st);
   if (e == cudaSuccess && h->fwd) e = fill_async(h->fwd->fbuf.p, h->fwd->fbuf.n, value, st);
   if (e == cudaSuccess && h->fwd && h->fwd->lpg.p) e = fill_async(h->fwd->lpg.p, h->fwd->lpg.n, value, st);
   if (e == cudaSuccess && h->fwd && h->fwd->rowspec.p)
@@ -1051,7 +1079,7 @@ int lp_debug_fill_scratch(lp_handle* h, float value, void* stream) {
 
 int lp_device_bytes(const lp_handle* h, int64_t* bytes) {
   if (!h || !bytes) return set_err(LP_ERR_ARG, "lp_device_bytes: null pointer");
-  int64_t b = h->erho.n * 4 + h->spec.n * 8 + h->tw_rho.n * 8 + h->tw_th.n * 8;
+  int64_t b = h->erho.n * 4 + h->spec.n * 8 + h->sspec.n * 8 + h->tw_rho.n * 8 + h->tw_th.n * 8;
   if (h->fwd) {
     for (int k = 0; k < 3; ++k) b += h->fwd->c2lp[k].n * 8 + h->fwd->rows[k].n * 4;
     b += h->fwd->thc.n * 4 + h->fwd->rhoc.n * 4 + h->fwd->fz.n * 8 + h->fwd->fbuf.n * 4;
@@ -1117,7 +1145,7 @@ static int fwd_slices(lp_handle* h, float* R, const float* f, int s0, int n, cud
   if (spread) CUDA_TRY(span_fork(h, st));
   for (int k = 0; k < 3; ++k) {
     const cudaStream_t sk = spread && k > 0 ? h->span_st[k - 1] : st;
-    float2* spk = spread ? spec + (size_t)k * n * spec_slice(h->Nk, h->Nth) : spec;
+    float2* spk = span_spec(h, s0, n, k, spread);
     FwdC2LPArgs a1{fbuf, spk, F->c2lp[k].p, h->erho.p, h->N, h->Nth, h->Nrho, h->Nk, h->cubic,
                    h->plan_rho, tx, F->ival.p, F->dlo, F->dhi, F->F, F->fsc};
     CUDA_TRY(launch(h, K_FWD_C2LP, sk, [&] { return launch_fwd_c2lp(a1, n, sk); }));
@@ -1156,7 +1184,7 @@ static int adj_slices(lp_handle* h, float* f, const float* R, int s0, int n, cud
   if (spread) CUDA_TRY(span_fork(h, st));
   for (int k = 0; k < 3; ++k) {
     const cudaStream_t sk = spread && k > 0 ? h->span_st[k - 1] : st;
-    float2* spk = spread ? spec + (size_t)k * n * spec_slice(h->Nk, h->Nth) : spec;
+    float2* spk = span_spec(h, s0, n, k, spread);
     const bool tex = !A->tex_h[k].empty();
     if (A->chi[k] < A->clo[k]) {
       if (tex) return set_err(LP_ERR_UNSUPPORTED, "lp_adj: span %d has no log-polar points", k);

@@ -16,6 +16,8 @@
 // Texture fetches are replaced by explicit interpolation with wrap addressing
 // at index position (x, y), which is what sampling the reference's textures
 // at (x+0.5, y+0.5) means (src/include/main_kernels.cuh:21-84).
+#include <algorithm>
+
 #include "lp_p2.cuh"
 
 namespace lpgb {
@@ -939,42 +941,59 @@ __global__ void __launch_bounds__(256) k_fwdT_cols(FwdTColsArgs a) {
 // image edge, so away from the edge a pixel walks n runs of points (one per tap row
 // j) and takes each point's tap i from its own cell.  A thread computes one pixel for
 // the kGatherSlices slices of a group.
+constexpr int kGatherPixels = 2;  // pixels per thread of k_fwdT_gather (N is a multiple of 16)
+
 __device__ __forceinline__ float pick_w(const float* w, int i) {
   return i == 0 ? w[0] : (i == 1 ? w[1] : (i == 2 ? w[2] : w[3]));
 }
 
+// PX consecutive pixels X0 .. X0 + PX - 1 of a row per thread: their cells of one cell
+// row are one run of the list (X0 + o - n + 1 .. X0 + PX - 1 + o), walked once, each
+// point adding to the pixels its taps reach -- the points and values are loaded once
+// for the PX pixels instead of once per pixel.
+template <int PX>
 __global__ void __launch_bounds__(256) k_fwdT_gather(FwdTGatherArgs a, int S) {
-  const int X = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int X0 = (blockIdx.x * 32 + (threadIdx.x & 31)) * PX;
   const int Y = blockIdx.y * 8 + (threadIdx.x >> 5);
-  if (X >= a.N || Y >= a.N) return;
+  if (X0 >= a.N || Y >= a.N) return;
   const int s0 = blockIdx.z * kGatherSlices;
   const int ns = min(kGatherSlices, S - s0);
   const size_t plane = (size_t)a.N * a.N;
-  float acc[kGatherSlices];
+  float acc[PX][kGatherSlices];
 #pragma unroll
-  for (int q = 0; q < kGatherSlices; ++q) acc[q] = 0.f;
+  for (int x = 0; x < PX; ++x)
+#pragma unroll
+    for (int q = 0; q < kGatherSlices; ++q) acc[x][q] = 0.f;
   const int o = a.cubic ? 1 : 0;
   const int n = a.cubic ? 4 : 2;
   // this slice group's values, [npts][kGatherSlices] in list order
   const float* G = a.G + (size_t)blockIdx.z * a.npts * kGatherSlices;
-  auto add = [&](int e, int2 p, int i, int j) {
+  // point e (coordinates p) of cell column cx into the pixels whose tap it is, tap row j
+  auto add = [&](int e, int2 p, int cx, int j) {
     float wx[4], wy[4];
     axis_weights_fx(p.x, a.F, a.fsc, a.cubic, wx);
     axis_weights_fx(p.y, a.F, a.fsc, a.cubic, wy);
-    const float w = pick_w(wy, j) * pick_w(wx, i);
+    const float wyj = pick_w(wy, j);
     const float4* g = reinterpret_cast<const float4*>(G + (size_t)e * kGatherSlices);
     const float4 u = __ldg(g);
     const float4 v = ns > 4 ? __ldg(g + 1) : make_float4(0.f, 0.f, 0.f, 0.f);  // block-uniform
-    acc[0] += w * u.x;
-    acc[1] += w * u.y;
-    acc[2] += w * u.z;
-    acc[3] += w * u.w;
-    acc[4] += w * v.x;
-    acc[5] += w * v.y;
-    acc[6] += w * v.z;
-    acc[7] += w * v.w;
+#pragma unroll
+    for (int x = 0; x < PX; ++x) {
+      const int i = X0 + x + o - cx;
+      if (i >= 0 && i < n) {
+        const float w = wyj * pick_w(wx, i);
+        acc[x][0] += w * u.x;
+        acc[x][1] += w * u.y;
+        acc[x][2] += w * u.z;
+        acc[x][3] += w * u.w;
+        acc[x][4] += w * v.x;
+        acc[x][5] += w * v.y;
+        acc[x][6] += w * v.z;
+        acc[x][7] += w * v.w;
+      }
+    }
   };
-  const int xlo = X + o - (n - 1), xhi = X + o;
+  const int xlo = X0 + o - (n - 1), xhi = X0 + PX - 1 + o;
   if (xlo >= 0 && xhi < a.N) {
     // the n runs walked side by side (independent load chains), run j in list order
     int e[4], e1[4], m = 0;
@@ -993,25 +1012,56 @@ __global__ void __launch_bounds__(256) k_fwdT_gather(FwdTGatherArgs a, int S) {
       for (int j = 0; j < 4; ++j) {
         if (e[j] < e1[j]) {
           const int2 p = __ldg(a.pts + e[j]);
-          add(e[j], p, xhi - wrapi(fx_int(p.x, a.F), a.N), j);
+          add(e[j], p, wrapi(fx_int(p.x, a.F), a.N), j);
           ++e[j];
         }
       }
     }
   } else {
-    for (int j = 0; j < n; ++j) {
-      const int* co = a.cell_off + (size_t)wrapi(Y + o - j, a.N) * a.N;
-      for (int i = 0; i < n; ++i) {
-        const int cx = wrapi(X + o - i, a.N);
-        const int e1 = __ldg(co + cx + 1);
-        for (int e = __ldg(co + cx); e < e1; ++e) add(e, __ldg(a.pts + e), i, j);
+    // image edge: each pixel's cells one at a time (wrapped); a point of cell cx adds
+    // to pixel X0 + x through tap i = X0 + x + o - cx, taken modulo N here
+    for (int x = 0; x < PX; ++x) {
+      const int X = X0 + x;
+      for (int j = 0; j < n; ++j) {
+        const int* co = a.cell_off + (size_t)wrapi(Y + o - j, a.N) * a.N;
+        for (int i = 0; i < n; ++i) {
+          const int cx = wrapi(X + o - i, a.N);
+          const int e1 = __ldg(co + cx + 1);
+          for (int e = __ldg(co + cx); e < e1; ++e) {
+            const int2 p = __ldg(a.pts + e);
+            float wx[4], wy[4];
+            axis_weights_fx(p.x, a.F, a.fsc, a.cubic, wx);
+            axis_weights_fx(p.y, a.F, a.fsc, a.cubic, wy);
+            const float w = pick_w(wy, j) * pick_w(wx, i);
+            const float4* g = reinterpret_cast<const float4*>(G + (size_t)e * kGatherSlices);
+            const float4 u = __ldg(g);
+            const float4 v = ns > 4 ? __ldg(g + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int xx = 0; xx < PX; ++xx) {
+              if (xx == x) {
+                acc[xx][0] += w * u.x;
+                acc[xx][1] += w * u.y;
+                acc[xx][2] += w * u.z;
+                acc[xx][3] += w * u.w;
+                acc[xx][4] += w * v.x;
+                acc[xx][5] += w * v.y;
+                acc[xx][6] += w * v.z;
+                acc[xx][7] += w * v.w;
+              }
+            }
+          }
+        }
       }
     }
   }
-  float* out = a.acc + (size_t)s0 * plane + (size_t)Y * a.N + X;
+  float* out = a.acc + (size_t)s0 * plane + (size_t)Y * a.N + X0;
 #pragma unroll
-  for (int q = 0; q < kGatherSlices; ++q)
-    if (q < ns) out[q * plane] = acc[q];
+  for (int q = 0; q < kGatherSlices; ++q) {
+    if (q < ns) {
+#pragma unroll
+      for (int x = 0; x < PX; ++x) out[q * plane + x] = acc[x][q];
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1071,21 +1121,26 @@ __global__ void __launch_bounds__(32 * kColWarps) k_prefilter_T_cols(PrefilterTC
   }
 }
 
-// rows: one block per output row, the padded row in shared memory, chunks of odd
-// length per thread (distinct banks), the window [off, off + N0) of it written
-// into the caller's image (the crop of the forward's centring)
-__global__ void k_prefilter_T_rows_crop(PrefilterTRowsCropArgs a) {
+// rows: one warp per output row (kRowWarps rows per block), the padded row in shared
+// memory, chunks of odd length per lane (distinct banks; at N = 512 chunks of 17
+// against the recursions' 16-sample warm-ups), the window [off, off + N0) of it
+// written into the caller's image (the crop of the forward's centring)
+constexpr int kRowWarps = 4;
+
+__global__ void __launch_bounds__(32 * kRowWarps) k_prefilter_T_rows_crop(PrefilterTRowsCropArgs a) {
   extern __shared__ float smf[];
   const int N = a.N;
-  float* line = smf;
-  float* y1 = smf + N;
-  const int s = blockIdx.x, yo = blockIdx.y;
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int s = blockIdx.x, yo = blockIdx.y * (blockDim.x >> 5) + wp;
+  if (yo >= a.N0) return;  // warps are independent
+  float* line = smf + (size_t)wp * 2 * N;
+  float* y1 = line + N;
   const float* src = a.in + ((size_t)s * N + yo + a.off) * N;
-  for (int x = threadIdx.x; x < N; x += blockDim.x) line[x] = __ldg(src + x);
-  __syncthreads();
+  for (int x = lane; x < N; x += 32) line[x] = __ldg(src + x);
+  __syncwarp();
   const float z = LP_POLE, q = LP_POLE / (LP_POLE - 1.0f);
-  const int C = line_chunk(N, blockDim.x);
-  const int b = threadIdx.x * C, e = min(b + C, N);
+  const int C = line_chunk(N, 32);
+  const int b = lane * C, e = min(b + C, N);
   if (b < N) {
     float tc = 0.f;
     for (int m = max(0, b - LP_WARM); m < e; ++m) {
@@ -1093,7 +1148,7 @@ __global__ void k_prefilter_T_rows_crop(PrefilterTRowsCropArgs a) {
       if (m >= b) y1[m] = (m < N - 1) ? -z * tc : q * tc;
     }
   }
-  __syncthreads();
+  __syncwarp();
   if (b < N) {
     // the next chunks' causal outputs serve as this chunk's anticausal warm-up
     float w = 0.f;
@@ -1102,10 +1157,10 @@ __global__ void k_prefilter_T_rows_crop(PrefilterTRowsCropArgs a) {
       if (m < e) line[m] = w;
     }
   }
-  __syncthreads();
+  __syncwarp();
   const float w0 = line[0];
   float* dst = a.out + ((size_t)s * a.N0 + yo) * a.N0 - a.off;
-  for (int x = a.off + threadIdx.x; x < a.off + a.N0; x += blockDim.x) {
+  for (int x = a.off + lane; x < a.off + a.N0; x += 32) {
     float v = LP_LAMBDA * line[x];
     if (x < 12) {
       float zn = z;
@@ -1176,8 +1231,10 @@ cudaError_t launch_fwdT_tapw(int2* cent, int n, const int* rows, const int* thc,
 }
 
 cudaError_t launch_fwdT_gather(const FwdTGatherArgs& a, int S, cudaStream_t st) {
-  dim3 grid((a.N + 31) / 32, (a.N + 7) / 8, (S + kGatherSlices - 1) / kGatherSlices);
-  k_fwdT_gather<<<grid, 256, 0, st>>>(a, S);
+  constexpr int PX = kGatherPixels;
+  if (a.N % PX != 0) return cudaErrorInvalidValue;
+  dim3 grid((a.N / PX + 31) / 32, (a.N + 7) / 8, (S + kGatherSlices - 1) / kGatherSlices);
+  k_fwdT_gather<PX><<<grid, 256, 0, st>>>(a, S);
   return cudaGetLastError();
 }
 
@@ -1189,10 +1246,14 @@ cudaError_t launch_prefilter_T_cols(const PrefilterTColsArgs& a, int S, cudaStre
 }
 
 cudaError_t launch_prefilter_T_rows_crop(const PrefilterTRowsCropArgs& a, int S, cudaStream_t st) {
-  const size_t sm = 2 * (size_t)a.N * sizeof(float);
+  // up to kRowWarps rows per block, as many as the shared memory holds (2 N floats each)
+  const size_t row = 2 * (size_t)a.N * sizeof(float);
+  const int wpb = (int)std::max<size_t>(1, std::min<size_t>(kRowWarps, (size_t)g_smem_optin / row));
+  const size_t sm = wpb * row;
   if (smem_ok(sm) != cudaSuccess) return cudaErrorInvalidConfiguration;
-  dim3 grid(S, a.N0);
-  k_prefilter_T_rows_crop<<<grid, 128, sm, st>>>(a);
+  cudaFuncSetAttribute(k_prefilter_T_rows_crop, cudaFuncAttributeMaxDynamicSharedMemorySize, g_smem_optin);
+  dim3 grid(S, (a.N0 + wpb - 1) / wpb);
+  k_prefilter_T_rows_crop<<<grid, 32 * wpb, sm, st>>>(a);
   return cudaGetLastError();
 }
 
