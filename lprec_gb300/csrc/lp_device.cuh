@@ -283,6 +283,59 @@ __device__ __forceinline__ void rho_scatter_T(const ArgsT& a, int s, int r0, int
     const bool wraps = __syncthreads_or((r0 >= 0 && __ldg(a.rbase + r0) != kNoWrap) ||
                                         (r1 >= 0 && __ldg(a.rbase + r1) != kNoWrap));
     const int nwin = wraps ? 2 : 1;
+    if (2 * ntap * nth >= a.N) {
+      // at most two points per residue class and row per thread (N <= 2 ntap nth, as for
+      // every register-FFT length, N = L / 2 = 8 T): the thread's points of both rows,
+      // x = ntap tid + p + m ntap nth, are loaded once before the passes (no global
+      // load waits inside the barrier-separated passes)
+      float pv[2][2][4];
+      int pc[2][2][4];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const int r = q == 0 ? r0 : r1;
+        const float* row = r >= 0 ? a.Rin + ((size_t)s * a.Nproj0 + r / a.os) * a.N0 : a.Rin;
+#pragma unroll
+        for (int m = 0; m < 2; ++m)
+#pragma unroll
+          for (int p = 0; p < 4; ++p) {
+            const int x = ntap * tid + p + m * ntap * nth;
+            const int xo = x - a.cor_off;
+            const bool ok = r >= 0 && p < ntap && x < a.N && xo >= 0 && xo < a.N0;
+            pc[q][m][p] = ok ? __ldg(a.rhoc + (size_t)r * a.N + x) : LP_FX_NONE;
+            pv[q][m][p] = ok ? __ldg(row + xo) : 0.f;
+          }
+      }
+      for (int p = 0; p < ntap; ++p) {
+        for (int h = 0; h < nwin; ++h) {
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            const int r = q == 0 ? r0 : r1;
+            if (r < 0) continue;
+            const int base = __ldg(a.rbase + r);
+            if (h == 1 && base == kNoWrap) continue;
+            const int top = base == kNoWrap ? INT_MAX : base + L - ntap + 1;
+#pragma unroll
+            for (int m = 0; m < 2; ++m) {
+              int rc = pc[q][m][0];
+              float val = pv[q][m][0];
+#pragma unroll
+              for (int pp = 1; pp < 4; ++pp)
+                if (p == pp) {
+                  rc = pc[q][m][pp];
+                  val = pv[q][m][pp];
+                }
+              if (rc == LP_FX_NONE) continue;
+              float w[4];
+              const int c = axis_weights_fx(rc, a.F, a.fsc, a.cubic, w);
+              if ((c >= top) != (h == 1)) continue;
+              for (int j = 0; j < ntap; ++j) acc(q, wrapi(c + j, L)) += w[j] * val;
+            }
+          }
+          __syncthreads();
+        }
+      }
+      return;
+    }
     for (int p = 0; p < ntap; ++p) {
       for (int h = 0; h < nwin; ++h) {
         for (int q = 0; q < 2; ++q) {
