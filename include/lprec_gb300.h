@@ -76,7 +76,11 @@ int lp_precompute_f64(int N0, int Nproj, int Nslices, double cor, int cubic, con
 
 /*
  * Create a handle on `device` from glpars (replaces lpRgpu::lpRgpu(size_t
- * params, int gpu), src/cuda/lpRgpu.cu:7-39).  n = number of floats.
+ * params, int gpu), src/cuda/lpRgpu.cu:7-39).  n = number of floats.  Besides
+ * the spectrum of Nslices slices, a handle whose slices are too few to hold three
+ * spectra of a small call (at most 8 * 2048^2 image samples) takes two more spectrum
+ * regions of up to that many slices, if they fit in 1 GiB, so that its small calls
+ * run their three spans concurrently.
  */
 int lp_create(const float* glpars, int64_t n, int device, lp_handle** out);
 
