@@ -80,6 +80,7 @@ static cudaError_t dev_alloc(DevBuf<T>& b, size_t n) {
   if (n == 0) n = 1;
   cudaError_t e = cudaMalloc((void**)&b.p, n * sizeof(T));
   if (e == cudaSuccess) b.n = n;
+  else b.p = nullptr;
   return e;
 }
 
@@ -593,8 +594,9 @@ int lp_create(const float* glpars, int64_t n, int device, lp_handle** out) {
     const int nmax = (int)std::min<double>(h->Nslices, std::floor(kSpreadSamples / ((double)h->N * h->N)));
     const size_t need = 2 * (size_t)std::max(nmax, 0) * spec_slice(h->Nk, h->Nth);
     if (e == cudaSuccess && nmax > 0 && 3 * nmax > h->Nslices && need * sizeof(float2) <= kSpreadSpecBytes) {
-      e = dev_alloc(h->sspec, need);
-      if (e == cudaSuccess) h->sspec_slices = nmax;
+      // optional: without the regions the spans run in sequence
+      if (dev_alloc(h->sspec, need) == cudaSuccess) h->sspec_slices = nmax;
+      else (void)cudaGetLastError();
     }
   }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
@@ -1277,8 +1279,15 @@ static int build_transpose_tables(lp_handle* h) {
   const size_t rs_slots = (size_t)h->Nslices * std::max(nr, 1) * rowspec_stride(h->Nk);
   const size_t spec_slots = (size_t)h->Nslices * spec_slice(h->Nk, h->Nth);
   F->tspread = (2 * rs_slots + 2 * spec_slots) * sizeof(float2) <= kTransposeSpreadBytes;
-  CUDA_TRY(dev_alloc(F->rowspec, (F->tspread ? 3 : 1) * rs_slots));
-  if (F->tspread) CUDA_TRY(dev_alloc(F->tspec, 2 * spec_slots));
+  if (F->tspread && (dev_alloc(F->rowspec, 3 * rs_slots) != cudaSuccess ||
+                     dev_alloc(F->tspec, 2 * spec_slots) != cudaSuccess)) {
+    // optional: without the per-span regions the spans run in sequence
+    (void)cudaGetLastError();
+    F->rowspec.free_();
+    F->tspec.free_();
+    F->tspread = false;
+  }
+  if (!F->tspread) CUDA_TRY(dev_alloc(F->rowspec, rs_slots));
   // the theta columns' (row, tap) lists: a row's taps reach columns first_tap + j (mod
   // Nth); entries of a column in ascending row order; the weights come from the same
   // device function as the forward's theta interpolation (k_fwdT_tapw)
