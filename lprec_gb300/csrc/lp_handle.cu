@@ -1134,7 +1134,6 @@ static int fwd_slices(lp_handle* h, float* R, const float* f, int s0, int n, cud
   f += (size_t)s0 * h->N0 * h->N0;
   R += (size_t)s0 * h->Nproj0 * h->N0;
   float* fbuf = F->fbuf.p + (size_t)s0 * h->N * h->N;
-  float2* spec = h->spec.p + (size_t)s0 * spec_slice(h->Nk, h->Nth);
   const cudaTextureObject_t* tx = tex ? F->tex.p + s0 : nullptr;
   const cudaSurfaceObject_t* sf = tex ? F->surf.p + s0 : nullptr;
   FwdIngestArgs ia{f, fbuf, h->N, h->N0, h->N / 2 - h->N0 / 2, h->cubic};
@@ -1171,7 +1170,6 @@ static int adj_slices(lp_handle* h, float* f, const float* R, int s0, int n, cud
   float* rbuf = A->rbuf.p + (size_t)s0 * h->Nproj * h->N;
   // cubic: the ingest writes rin and the column prefilter rin -> rbuf (out of place)
   float* rin = h->cubic ? A->rin.p + (size_t)s0 * h->Nproj * h->N : rbuf;
-  float2* spec = h->spec.p + (size_t)s0 * spec_slice(h->Nk, h->Nth);
   const size_t gstride = (size_t)A->W2 * h->Nrho;
   AdjIngestArgs ia{R, rin, A->filter ? A->H.p : nullptr, h->N, h->N0, h->Nproj, h->Nproj0, h->os,
                    h->N / 2 - h->cor, h->cubic, h->plan_filt};
