@@ -7,8 +7,9 @@
     b.output_R(i), b.output_f(i)
 
 Requests with the same (N, Nproj) share one native handle whose batch
-schedule the autotuner picks for the geometry (lp_autotune: slice chunks,
-streams, theta-convolution block), and are concatenated into one batch,
+schedules the autotuner picks for the geometry and each of its wave sizes
+(lp_autotune: slice chunks, streams, theta-convolution block), and are
+concatenated into one batch,
 fewest slices first.  The groups run one after another inside the graph,
 smallest geometry first (shortest work first: running them on parallel graph
 branches was measured slower, the large groups already fill the GPU and the
@@ -97,9 +98,14 @@ class UnevenBatch:
             lp.precompute(1)
             lp.initcmem(1, gpu)
             waves = plan_waves(self.requests, idx, N, wave_slices, last_alone and gi == len(plan) - 1)
+            # one autotuned schedule per wave size of the group, set before each wave's
+            # launches (the graph records the launches of the schedule in force)
+            scheds = {}
             if autotune:
-                lp.autotune(gpu, max(b - a for a, b, _ in waves))
-            g = dict(lp=lp, N=N, Nproj=Nproj, S=total, idx=idx, waves=waves,
+                for size in sorted({b - a for a, b, _ in waves}):
+                    lp.autotune(gpu, size)
+                    scheds[size] = lp.clphandle[gpu].schedule()
+            g = dict(lp=lp, N=N, Nproj=Nproj, S=total, idx=idx, waves=waves, scheds=scheds,
                      f=torch.zeros((total, N, N), device=self.dev),
                      R=torch.zeros((total, Nproj, N), device=self.dev),
                      Rout=torch.zeros((total, Nproj, N), device=self.dev),
@@ -124,6 +130,8 @@ class UnevenBatch:
         return self._view(i, "fout")
 
     def _work(self, g, a, b):
+        if b - a in g["scheds"]:
+            g["lp"].set_schedule(self.gpu, **g["scheds"][b - a])
         g["lp"].fwdp(g["Rout"][a:b], g["f"][a:b], self.gpu)
         g["lp"].adjp(g["fout"][a:b], g["R"][a:b], self.gpu)
 
