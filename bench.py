@@ -742,13 +742,13 @@ def run_ours(args):
     for _ in range(max(2, args.warmup // 2)):
         e2e_step()
     torch.cuda.synchronize()
-    # three timed windows, each preceded by a measurement of the host link (shared with
+    # five timed windows, each preceded by a measurement of the host link (shared with
     # other jobs on the host: its device->host rate has been seen to drop from ~190 to
     # ~23 GB/s between windows); e2e is the median window
     q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ke = max(3, args.steps)
     windows = []
-    for w in range(3):
+    for w in range(5):
         lb = link if w == 0 else link_gbs()
         traces = []
         q0.record(stream)
