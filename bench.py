@@ -572,11 +572,11 @@ def run_side_configs(torch, dev, reps=5):
 
     # padded sizes that are not powers of two (an off-centre axis pads N0 to
     # ceil((N0 + 2|N0/2 - cor|)/16)*16; the reference's foam data has N = 2016, 299
-    # angles): fwd+adj throughput per image sample against the power-of-two size
-    # of the same detector width
+    # angles; 2560 is a common detector width): fwd+adj throughput per image sample
+    # against the power-of-two size of the same (or the nearest) detector width
     geos = [("n512", 512, 768, 256, 64), ("n528_cor253", 512, 768, 253, 64),
             ("n2048", 2048, 3000, 1024, 16), ("n2064_cor1021", 2048, 3000, 1021, 16),
-            ("n2080_cor1012", 2048, 3000, 1012, 16),
+            ("n2080_cor1012", 2048, 3000, 1012, 16), ("n2560", 2560, 3750, 1280, 16),
             ("n2016_foam", 2016, 299, 1008, 16)]
     res = {}
     for name, N0, Np, cor, S in geos:
@@ -598,7 +598,7 @@ def run_side_configs(torch, dev, reps=5):
         lp.close()
         del f, R, fo
     for name, ref in (("n528_cor253", "n512"), ("n2064_cor1021", "n2048"), ("n2080_cor1012", "n2048"),
-                      ("n2016_foam", "n2048")):
+                      ("n2016_foam", "n2048"), ("n2560", "n2048")):
         res[name]["per_pixel_vs_pow2"] = res[name]["ns_per_padded_pixel"] / res[ref]["ns_per_padded_pixel"]
     out["padded_sizes"] = res
 
