@@ -3,7 +3,8 @@
 ``radon(f, lp, gpu)`` applies the log-polar Radon transform to a CUDA tensor
 f[S, N0, N0] and returns R[S, Nproj, N0].  Its backward is the hand-written
 exact discrete transpose of the forward (``lp_fwd_transpose``): transposed
-interpolations (scatter with the same cubic weights), the conjugate kernel
+interpolations (the forward's cubic weights, summed in a fixed order without
+atomics, so a backward gives the same bits on every call), the conjugate kernel
 multiply and the transposed prefilter recursions -- not lprec's approximate
 adjoint.  Nothing from the forward is saved (the operator is linear).
 """
